@@ -1,0 +1,161 @@
+/*
+ * rtacx -- C ABI of the GB300 receiver-side reduction for rtac_simulation.
+ *
+ * The reference computes a sonar ping from ray-cast echo samples in three
+ * steps, all behind SensorInstance::compute_output():
+ *   sort(samples)          src/Receiver.cu:9-42 (thrust::sort by travel)
+ *   binner_.compute(...)   include/rtac_simulation/Binner.h:96-102,
+ *                          src/Binner.cu:24-136 (keys, segments, windows)
+ *   do_reduce(...)         src/SensorInstance2D.cu:44-119 (2D),
+ *                          src/SensorInstance1D.cu:35-89 (1D)
+ * This library replaces those three steps. Plain pointers and sizes only;
+ * device pointers are caller-owned (as SensorInstance owns receivedSamples_
+ * and the ping) and are never permuted: unlike the reference, the caller's
+ * sample buffer is left in its original order. Every call is stream-ordered
+ * on the caller's stream (a cudaStream_t passed as void*, NULL = legacy
+ * default stream) and returns without a device-wide synchronisation.
+ * Errors are status codes, never exceptions or device traps; the message of
+ * the last failure is available from rtacx_last_error().
+ *
+ * Sample layouts (include/rtac_simulation/Sample.h:101-161):
+ *   RTACX_SAMPLE_1D  SimSample1D {float re, im, travel}            12 bytes
+ *   RTACX_SAMPLE_2D  SimSample2D {float re, im, travel, bearing}   16 bytes
+ * A null sample has travel = -1 and value 0 (Sample.h:122-127, 155-160).
+ * Outputs are complex64 (interleaved float re, im): 1D ping [range_count],
+ * 2D ping row-major [range_count][bearing_count], i.e. cell (r, b) at
+ * r * bearing_count + b as out(blockIdx.y = r, blockIdx.x = b) in
+ * src/SensorInstance2D.cu:81.
+ */
+#ifndef RTACX_H
+#define RTACX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rtacx_ctx rtacx_ctx;
+typedef int rtacx_status;
+
+#define RTACX_OK                    0
+#define RTACX_ERR_INVALID_ARGUMENT  1  /* bad pointer, size or configuration */
+#define RTACX_ERR_NOT_CONFIGURED    2  /* call needs rtacx_configure_* first  */
+#define RTACX_ERR_CUDA              3  /* a CUDA runtime call failed          */
+#define RTACX_ERR_OUT_OF_MEMORY     4  /* scratch allocation failed           */
+#define RTACX_ERR_DEVICE            5  /* device error word set by a kernel   */
+#define RTACX_ERR_UNSUPPORTED       6  /* size or mode beyond this build      */
+
+/* Key of a sample outside [min - margin, max + margin] (Binner::Key::OutOfRange,
+ * include/rtac_simulation/Binner.h:27). */
+#define RTACX_KEY_OUT_OF_RANGE 0xFFFFFFFFu
+
+#define RTACX_SAMPLE_1D 1
+#define RTACX_SAMPLE_2D 2
+
+/* rtacx_sensor_1d.flags: use the literal 1D PSF scaling of the reference,
+ * scaling.x = 1.0f / duration * c (src/SensorInstance1D.cu:30), instead of
+ * the evident intent 1 / (duration * c) that the 2D path uses. */
+#define RTACX_FLAG_1D_LITERAL_SCALING 1u
+
+/* 1D echosounder (SensorInstance1D, include/rtac_simulation/SensorInstance1D.h). */
+typedef struct {
+    float range_min;        /* ranges_: Linspace<float>(min, max, count)     */
+    float range_max;
+    uint32_t range_count;
+    float sound_celerity;   /* soundCelerity_ (m/s)                           */
+    float pulse_duration;   /* waveform_->duration() (s)                      */
+    float margin;           /* Binner margin (m); the reference uses c*duration
+                               (src/SensorInstance.cu:32)                    */
+    const float* pulse;     /* host, pulse_len complex taps (Waveform table)  */
+    uint32_t pulse_len;
+    uint32_t flags;
+} rtacx_sensor_1d;
+
+/* 2D imaging sonar (SensorInstance2D, include/rtac_simulation/SensorInstance2D.h). */
+typedef struct {
+    float range_min;
+    float range_max;
+    uint32_t range_count;
+    float sound_celerity;
+    float pulse_duration;
+    float margin;
+    const float* pulse;     /* host, pulse_len complex taps: texture height    */
+    uint32_t pulse_len;
+    const float* beam;      /* host, beam_len real taps (BeamDirectivity):
+                               texture width (src/SensorInstance2D.cu:20-33)  */
+    uint32_t beam_len;
+    float beam_span;        /* BeamDirectivity::span() (rad)                  */
+    const float* bearings;  /* host, bearing_count output bearings (rad),
+                               SensorInfo2D::bearings()                       */
+    uint32_t bearing_count;
+    uint32_t flags;
+} rtacx_sensor_2d;
+
+/* Create a context bound to CUDA device `device`. Replaces the per-sensor
+ * state the reference keeps in SensorInstance (Binner, PSF texture, bins_). */
+rtacx_status rtacx_create(rtacx_ctx** ctx, int device);
+void rtacx_destroy(rtacx_ctx* ctx);
+const char* rtacx_last_error(const rtacx_ctx* ctx);
+const char* rtacx_version(void);
+
+/* Configure for a 1D / 2D sensor. Replaces SensorInstance::set_ranges
+ * (src/SensorInstance.cu:23-34: Binner::reconfigure + generate_psf_data,
+ * src/SensorInstance1D.cu:15-25, src/SensorInstance2D.cu:20-33) and the PSF
+ * scalings of kernel() (src/SensorInstance1D.cu:27-33,
+ * src/SensorInstance2D.cu:35-42). Tables are copied; synchronous. */
+rtacx_status rtacx_configure_1d(rtacx_ctx* ctx, const rtacx_sensor_1d* sensor);
+rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* sensor);
+
+/* Pre-size the scratch for up to max_samples samples so that later calls
+ * allocate nothing (e.g. before stream capture). Synchronous. */
+rtacx_status rtacx_reserve(rtacx_ctx* ctx, uint64_t max_samples);
+
+/* Sort + bin only (parity seam). Replaces sort() (src/Receiver.cu:9-42) and
+ * Binner::compute (include/rtac_simulation/Binner.h:96-102). Every output is
+ * optional (NULL to skip) and device-resident:
+ *   keys      [n]                 range key of each input sample, input order
+ *                                  (Binner::Key, Binner.h:47-53)
+ *   segments  [range_count][2]    {start, end} of each range bin in the
+ *                                  reference's travel-sorted order
+ *                                  (binIndexes_, src/Binner.cu:51-80)
+ *   windows   [range_count][2]    {offset, size} of each output bin's sample
+ *                                  view in that order (bins_, src/Binner.cu:82-136)
+ *   counts    [range_count]       samples per range bin
+ *   oor       [2] (uint64)        samples out of range below / above
+ * Positions are those of the reference's sorted array; this library's own
+ * sorted scratch groups samples by (range bin, bearing bin) instead. */
+rtacx_status rtacx_bin(rtacx_ctx* ctx, const void* samples, uint64_t n, int sample_kind,
+                       uint32_t* keys, uint32_t* segments, uint32_t* windows,
+                       uint32_t* counts, uint64_t* oor, void* stream);
+
+/* Full ping: sort, bin and sparse PSF reduction into `out` (device,
+ * complex64). Replaces SensorInstance1D::reduce_samples
+ * (include/rtac_simulation/SensorInstance1D.h:63-69) and
+ * SensorInstance2D::fill_ping / reduce_samples
+ * (include/rtac_simulation/SensorInstance2D.h:66-93). `samples` must match
+ * the configured sensor (12-byte records for 1D, 16-byte records for 2D). */
+rtacx_status rtacx_reduce(rtacx_ctx* ctx, const void* samples, uint64_t n,
+                          float* out, void* stream);
+
+/* Wait for `stream` and report the device error word of this context
+ * (RTACX_ERR_DEVICE if a kernel flagged an error since the last check).
+ * Clears the word. */
+rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
+
+/* Stage tracing (no counterpart in the reference, which has no timers):
+ * when enabled, rtacx_reduce records a CUDA event pair around each stage on
+ * the caller's stream. rtacx_stage_times waits for the last traced call and
+ * writes up to `max` stage durations in milliseconds, in the order
+ * count, column scan, bin scan, scatter, windows, reduce; returns the number
+ * of stages written (negative on error). */
+#define RTACX_STAGE_COUNT 6
+rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
+int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTACX_H */

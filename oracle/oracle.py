@@ -1,0 +1,148 @@
+"""ctypes wrapper of the oracle (oracle/rtacx_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline / reference arm of bench.py, never by the product package.
+Parity status: partially pinned (range key and pulse table against the
+reference's own headers, tests/golden/); the rest is a restatement.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "librtacx_oracle.so"
+
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_U64 = ctypes.c_uint64
+_F = ctypes.c_float
+_I = ctypes.c_int
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "librtacx_oracle.so"], check=True)
+    return LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    src = HERE / "rtacx_oracle.cpp"
+    if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+        build()
+    lib = ctypes.CDLL(str(LIB_PATH))
+    lib.rtacx_oracle_key_params.argtypes = [_U32, _F, _F, _F, ctypes.POINTER(_F), ctypes.POINTER(_F),
+                                            ctypes.POINTER(_F), ctypes.POINTER(_F)]
+    lib.rtacx_oracle_key_params.restype = None
+    lib.rtacx_oracle_range_keys.argtypes = [_U32, _F, _F, _F, _P, _U64, _U32, _P, _P]
+    lib.rtacx_oracle_range_keys.restype = None
+    lib.rtacx_oracle_bin_overlap.argtypes = [_F, _F, _U32, _F]
+    lib.rtacx_oracle_bin_overlap.restype = _I
+    lib.rtacx_oracle_linspace_at.argtypes = [_F, _F, _U32, _U32]
+    lib.rtacx_oracle_linspace_at.restype = _F
+    lib.rtacx_oracle_bearing_bins.argtypes = [_F, _F, _U32, _P, _U64, _U32, _P]
+    lib.rtacx_oracle_bearing_bins.restype = None
+    lib.rtacx_oracle_bin.argtypes = [_P, _U64, _U32, _U32, _F, _F, _U32, _F, _P, _P, _P,
+                                     ctypes.POINTER(_U64), ctypes.POINTER(_U64)]
+    lib.rtacx_oracle_bin.restype = _I
+    lib.rtacx_oracle_reduce.argtypes = [_U32, _P, _U64, _F, _F, _U32, _F, _F, _P, _U32, _F, _P, _U32,
+                                        _P, _U32, _I, _U32, _U32, _I, _P]
+    lib.rtacx_oracle_reduce.restype = None
+    _lib = lib
+    return lib
+
+
+def key_params(n_bins, min_bin, max_bin, margin):
+    lib = load()
+    a, b, lo, hi = _F(), _F(), _F(), _F()
+    lib.rtacx_oracle_key_params(n_bins, min_bin, max_bin, margin, ctypes.byref(a), ctypes.byref(b),
+                                ctypes.byref(lo), ctypes.byref(hi))
+    return np.float32(a.value), np.float32(b.value), np.float32(lo.value), np.float32(hi.value)
+
+
+def range_keys(n_bins, min_bin, max_bin, margin, travel):
+    """Range key and out-of-range side (-1, 0, +1) of every travel value."""
+    lib = load()
+    t = np.ascontiguousarray(travel, dtype=np.float32)
+    keys = np.empty(t.size, dtype=np.uint32)
+    side = np.empty(t.size, dtype=np.int8)
+    lib.rtacx_oracle_range_keys(n_bins, min_bin, max_bin, margin, t.ctypes.data, t.size, 1,
+                                keys.ctypes.data, side.ctypes.data)
+    return keys, side
+
+
+def bin_overlap(rmin, rmax, n, margin) -> int:
+    return load().rtacx_oracle_bin_overlap(rmin, rmax, n, margin)
+
+
+def linspace_at(rmin, rmax, n, r) -> np.float32:
+    return np.float32(load().rtacx_oracle_linspace_at(rmin, rmax, n, r))
+
+
+def bearing_bins(scale, offset, count, bearing):
+    t = np.ascontiguousarray(bearing, dtype=np.float32)
+    out = np.empty(t.size, dtype=np.uint32)
+    load().rtacx_oracle_bearing_bins(scale, offset, count, t.ctypes.data, t.size, 1, out.ctypes.data)
+    return out
+
+
+def bin_samples(samples: np.ndarray, sensor: dict):
+    """Reference segments, windows, counts and out-of-range counts."""
+    lib = load()
+    s = np.ascontiguousarray(samples, dtype=np.float32)
+    n, stride = s.shape
+    nR = sensor["range_count"]
+    seg = np.zeros((nR, 2), dtype=np.uint32)
+    win = np.zeros((nR, 2), dtype=np.uint32)
+    cnt = np.zeros(nR, dtype=np.uint32)
+    lo, hi = _U64(), _U64()
+    ov = lib.rtacx_oracle_bin(s.ctypes.data, n, stride, 2 if stride == 4 else 1,
+                              sensor["range_min"], sensor["range_max"], nR, sensor["margin"],
+                              seg.ctypes.data, win.ctypes.data, cnt.ctypes.data,
+                              ctypes.byref(lo), ctypes.byref(hi))
+    return dict(segments=seg, windows=win, counts=cnt, oor=np.array([lo.value, hi.value], dtype=np.uint64),
+                overlap=ov)
+
+
+def pulse_scale(sensor: dict, literal_1d: bool = False) -> np.float32:
+    d, c = np.float32(sensor["pulse_duration"]), np.float32(sensor["sound_celerity"])
+    if literal_1d:
+        return np.float32(np.float32(np.float32(1.0) / d) * c)
+    return np.float32(np.float32(1.0) / np.float32(d * c))
+
+
+def reduce(samples: np.ndarray, sensor: dict, mode: int = 0, rows=None, threads: int = 0,
+           literal_1d: bool = False) -> np.ndarray:
+    """Oracle ping. mode 0: FP64 (complex128), mode 1: FP32 reference
+    arithmetic (complex64). rows = (begin, end) restricts the output rows."""
+    lib = load()
+    s = np.ascontiguousarray(samples, dtype=np.float32)
+    n, stride = s.shape
+    dims = 2 if stride == 4 else 1
+    nR = sensor["range_count"]
+    r0, r1 = rows if rows is not None else (0, nR)
+    pulse = np.ascontiguousarray(sensor["pulse"], dtype=np.complex64)
+    if dims == 2:
+        beam = np.ascontiguousarray(sensor["beam"], dtype=np.float32)
+        bearings = np.ascontiguousarray(sensor["bearings"], dtype=np.float32)
+        bscale = np.float32(np.float32(1.0) / np.float32(sensor["beam_span"]))
+        nB = bearings.size
+    else:
+        beam = np.zeros(1, dtype=np.float32)
+        bearings = np.zeros(1, dtype=np.float32)
+        bscale, nB = np.float32(0.0), 1
+    out = np.zeros((r1 - r0, nB), dtype=np.complex128 if mode == 0 else np.complex64)
+    threads = threads or (os.cpu_count() or 1)
+    lib.rtacx_oracle_reduce(dims, s.ctypes.data, n, sensor["range_min"], sensor["range_max"], nR,
+                            sensor["margin"], pulse_scale(sensor, literal_1d), pulse.ctypes.data, pulse.size,
+                            bscale, beam.ctypes.data, beam.size, bearings.ctypes.data, nB,
+                            mode, r0, r1, threads, out.ctypes.data)
+    return out[:, 0] if dims == 1 else out

@@ -1,0 +1,407 @@
+// rtacx oracle -- CPU restatement of rtac_simulation's receiver-side reduction.
+//
+// TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's
+// CPU-baseline / reference arm may load this library, and only as the checker
+// or as the timed CPU rendition of the reference algorithm. The product path
+// (librtacx.so) never links or calls it.
+//
+// Parity status: PARTIALLY PINNED. Binner::Key (range key) and Waveform_Sine
+// (pulse table) are pinned against golden vectors produced by compiling the
+// reference's own headers (oracle/ref_probe.cpp, tests/golden/). Everything
+// downstream of the keys -- segments, windows, the texture-equivalent PSF
+// lookup and the reductions -- is restated from the reference sources cited
+// below; the reference cannot be built here (rtac_base/rtac_cuda, yaml-cpp and
+// OptiX/GL are absent) and ships no test vectors, so that part is unpinned.
+//
+// Arithmetic contract (shared with the CUDA path):
+//   * Key parameters are computed in float exactly as the Key constructor does
+//     (include/rtac_simulation/Binner.h:34-45). The key itself is
+//     (int)fmaf(a, travel, b) with CUDA's float->int conversion (round toward
+//     zero, saturating, NaN -> 0), then the unit-mixing bound tests of
+//     include/rtac_simulation/Binner.h:47-53.
+//   * binOverlap = (int)(margin / ((max - min) / (binCount - 1))) in float
+//     (src/Binner.cu:112-113).
+//   * Segments and windows follow do_make_segments / do_make_bins literally
+//     (src/Binner.cu:51-69, 82-106) on travel-sorted samples
+//     (src/Receiver.cu:9-42), including the "istart >= iend -> empty view" rule.
+//   * PSF lookup: the reference samples a float2 texture with normalized
+//     coordinates, linear filtering and border addressing
+//     (src/SensorInstance2D.cu:14-15, 35-42; ReductionKernel.h:44-73). With
+//     u = scale * delta + 0.5 the texel coordinate is x = u * n - 0.5 and the
+//     value is (1 - frac(x)) T[floor(x)] + frac(x) T[floor(x) + 1], T = 0
+//     outside [0, n). The separable table PSF[h][w] = pulse[h] * beam[w]
+//     (src/SensorInstance2D.cu:20-33) makes the bilinear fetch the product of
+//     two 1D lerps. The coordinate deltas delta = travel - range_r and
+//     bearing_s - bearing_b are float subtractions as in the reference kernel
+//     (src/SensorInstance2D.cu:56-65); everything after them is exact (FP64)
+//     in FP64 mode. The hardware's 9-bit filter weights are NOT reproduced.
+//   * Output range r is Linspace[r] = min + r * ((max - min) / (n - 1)) in float
+//     (rtac_base Linspace, not vendored; r = 0 for n = 1).
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr uint32_t kOutOfRange = 0xFFFFFFFFu;
+
+// CUDA's cvt.rzi.s32.f32: truncate toward zero, saturate, NaN -> 0.
+inline int cuda_f2i_rz(float f)
+{
+    if(std::isnan(f)) return 0;
+    if(f >= 2147483648.0f)  return std::numeric_limits<int>::max();
+    if(f <= -2147483648.0f) return std::numeric_limits<int>::min();
+    return (int)f;
+}
+
+struct KeyParams {
+    uint32_t bin_count;
+    float a, b, lower, upper;
+};
+
+KeyParams make_key(uint32_t binCount, float minBin, float maxBin, float margin)
+{
+    // include/rtac_simulation/Binner.h:34-45
+    KeyParams k;
+    k.bin_count = binCount;
+    float resolution = (maxBin - minBin) / (float)binCount;
+    float m = minBin - 0.5f * resolution;
+    float M = maxBin + 0.5f * resolution;
+    k.a = (float)(binCount - 1u) / (M - m);
+    float ma = -m * k.a;
+    k.b = ma + 0.5f;
+    k.lower = m - margin;
+    k.upper = M + margin;
+    return k;
+}
+
+inline uint32_t range_key(const KeyParams& k, float travel, int* side = nullptr)
+{
+    // include/rtac_simulation/Binner.h:47-53
+    int res = cuda_f2i_rz(std::fmaf(k.a, travel, k.b));
+    if(side) *side = 0;
+    if(res < 0) {
+        if((float)res >= k.lower) return 0;
+        if(side) *side = -1;
+        return kOutOfRange;
+    }
+    if((uint32_t)res >= k.bin_count) {
+        if((float)res <= k.upper) return k.bin_count - 1;
+        if(side) *side = 1;
+        return kOutOfRange;
+    }
+    return (uint32_t)res;
+}
+
+int bin_overlap(float rmin, float rmax, uint32_t n, float margin)
+{
+    // src/Binner.cu:112-113: float resolution = length / (count - 1);
+    // int binOverlap = margin_ / resolution;
+    float resolution = (rmax - rmin) / (float)(n - 1u);
+    return cuda_f2i_rz(margin / resolution);
+}
+
+float linspace_at(float rmin, float rmax, uint32_t n, uint32_t r)
+{
+    if(n <= 1) return rmin;
+    float res = (rmax - rmin) / (float)(n - 1u);
+    float prod = res * (float)r;
+    return rmin + prod;
+}
+
+// Texture-equivalent 1D linear lookup with border addressing, exact weights.
+template <typename T>
+inline T lerp_border(const T* table, int n, double x)
+{
+    double fl = std::floor(x);
+    if(!(fl >= -1.0 && fl <= (double)(n - 1))) return T(0);
+    int i = (int)fl;
+    double alpha = x - fl;
+    T lo = (i >= 0)    ? table[i]     : T(0);
+    T hi = (i + 1 < n) ? table[i + 1] : T(0);
+    return lo * (1.0 - alpha) + hi * alpha;
+}
+
+// FP32 reference-arithmetic lookup: the float expressions of the reference
+// kernel (u = fmaf(scale, delta, 0.5f)) followed by a float texel coordinate.
+template <typename T>
+inline T lerp_border_f32(const T* table, int n, float u)
+{
+    float x = u * (float)n - 0.5f;
+    float fl = std::floor(x);
+    if(!(fl >= -1.0f && fl <= (float)(n - 1))) return T(0);
+    int i = (int)fl;
+    float alpha = x - fl;
+    T lo = (i >= 0)    ? table[i]     : T(0);
+    T hi = (i + 1 < n) ? table[i + 1] : T(0);
+    return lo * (1.0f - alpha) + hi * alpha;
+}
+
+struct Sensor {
+    uint32_t dims;          // 1 or 2
+    float rmin, rmax;
+    uint32_t nR;
+    float margin;
+    float pulse_scale;      // 1 / (duration * c) (2D), see the 1D quirk flag
+    uint32_t pulse_len;
+    const float* pulse;     // 2 * pulse_len floats (complex)
+    // 2D
+    float beam_scale;       // 1 / span
+    uint32_t beam_len;
+    const float* beam;      // beam_len floats
+    uint32_t nB;
+    const float* bearings;  // nB floats
+};
+
+struct SortedSample { float re, im, travel, bearing; uint32_t index; };
+
+// Travel sort + keys + reference segments + reference windows on the host.
+struct BinResult {
+    std::vector<SortedSample> sorted;
+    std::vector<uint32_t> keys;       // per sorted sample
+    std::vector<uint32_t> segments;   // nR * 2 {start, end}
+    std::vector<uint32_t> windows;    // nR * 2 {offset, size}
+    int overlap;
+};
+
+void do_bin(const float* samples, uint64_t n, uint32_t stride, uint32_t dims,
+            const KeyParams& key, float rmin, float rmax, uint32_t nR, float margin,
+            BinResult& out)
+{
+    out.sorted.resize(n);
+    for(uint64_t i = 0; i < n; i++) {
+        const float* s = samples + i * stride;
+        out.sorted[i] = SortedSample{s[0], s[1], s[2], dims == 2 ? s[3] : 0.0f, (uint32_t)i};
+    }
+    // src/Receiver.cu:9-42 sorts by travel; the order among equal travels is
+    // unspecified there, a stable order is one valid outcome.
+    std::stable_sort(out.sorted.begin(), out.sorted.end(),
+                     [](const SortedSample& l, const SortedSample& r) { return l.travel < r.travel; });
+    out.keys.resize(n);
+    for(uint64_t i = 0; i < n; i++) out.keys[i] = range_key(key, out.sorted[i].travel);
+
+    // src/Binner.cu:51-80 (memset, then do_make_segments)
+    out.segments.assign((size_t)nR * 2, 0u);
+    for(uint64_t tid = 0; tid < n; tid++) {
+        uint32_t k = out.keys[tid];
+        if(k == kOutOfRange) continue;
+        if(tid == 0) out.segments[0] = 0;
+        else if(out.keys[tid - 1] != k) out.segments[(size_t)k * 2] = (uint32_t)tid;
+        if(tid == n - 1) out.segments[(size_t)k * 2 + 1] = (uint32_t)n;
+        else if(k != out.keys[tid + 1]) out.segments[(size_t)k * 2 + 1] = (uint32_t)(tid + 1);
+    }
+
+    // src/Binner.cu:82-136 (do_make_bins)
+    int ov = bin_overlap(rmin, rmax, nR, margin);
+    out.overlap = ov;
+    out.windows.assign((size_t)nR * 2, 0u);
+    for(int tid = 0; tid < (int)nR; tid++) {
+        int istart = std::max(0, tid - ov);
+        int iend = std::min((int)nR - 1, tid + ov);
+        auto empty = [&](int i) { return out.segments[2 * i + 1] == out.segments[2 * i]; };
+        for(; istart < iend && empty(istart); istart++);
+        for(; iend > istart && empty(iend); iend--);
+        if(istart >= iend) {
+            out.windows[2 * tid] = 0; out.windows[2 * tid + 1] = 0;
+        }
+        else {
+            out.windows[2 * tid] = out.segments[2 * istart];
+            out.windows[2 * tid + 1] = out.segments[2 * iend + 1] - out.segments[2 * istart];
+        }
+    }
+}
+
+template <typename F>
+void parallel_rows(uint32_t row_begin, uint32_t row_end, int nthreads, F&& f)
+{
+    if(nthreads <= 1 || row_end - row_begin < 2) {
+        for(uint32_t r = row_begin; r < row_end; r++) f(r);
+        return;
+    }
+    std::atomic<uint32_t> next{row_begin};
+    std::vector<std::thread> pool;
+    for(int t = 0; t < nthreads; t++) {
+        pool.emplace_back([&]() {
+            for(uint32_t r = next.fetch_add(1); r < row_end; r = next.fetch_add(1)) f(r);
+        });
+    }
+    for(auto& th : pool) th.join();
+}
+
+// One output row of the reduction in FP64 (mode 0) or FP32 reference
+// arithmetic (mode 1). out points at nB complex values (doubles or floats).
+void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void* out_row)
+{
+    const uint32_t nB = (S.dims == 2) ? S.nB : 1u;
+    const float R = linspace_at(S.rmin, S.rmax, S.nR, r);
+    const uint32_t off = B.windows[2 * r], size = B.windows[2 * r + 1];
+    const std::complex<float>* pulse_f = reinterpret_cast<const std::complex<float>*>(S.pulse);
+    const int H = (int)S.pulse_len, W = (int)S.beam_len;
+    if(mode == 0) {
+        std::vector<std::complex<double>> pulse_d(pulse_f, pulse_f + H);
+        std::vector<double> beam_d(S.beam, S.beam + (S.dims == 2 ? W : 0));
+        std::complex<double>* o = static_cast<std::complex<double>*>(out_row);
+        const double ky = (double)S.pulse_scale * H, cy = 0.5 * H - 0.5;
+        const double kx = (double)S.beam_scale * W, cx = 0.5 * W - 0.5;
+        // Range factor does not depend on the bearing: evaluate once per sample.
+        std::vector<std::complex<double>> u(size);
+        for(uint32_t i = 0; i < size; i++) {
+            const SortedSample& s = B.sorted[off + i];
+            float d = s.travel - R;
+            u[i] = std::complex<double>(s.re, s.im) * lerp_border(pulse_d.data(), H, (double)d * ky + cy);
+        }
+        for(uint32_t b = 0; b < nB; b++) {
+            std::complex<double> acc(0.0, 0.0);
+            if(S.dims == 2) {
+                const float th = S.bearings[b];
+                for(uint32_t i = 0; i < size; i++) {
+                    float e = B.sorted[off + i].bearing - th;
+                    acc += u[i] * lerp_border(beam_d.data(), W, (double)e * kx + cx);
+                }
+            }
+            else {
+                for(uint32_t i = 0; i < size; i++) acc += u[i];
+            }
+            o[b] = acc;
+        }
+    }
+    else {
+        // Literal per-(sample, output) loop of do_sparse_convolve_2d_f /
+        // do_sparse_convolve_1d_f in float: one fused PSF evaluation per pair.
+        std::complex<float>* o = static_cast<std::complex<float>*>(out_row);
+        for(uint32_t b = 0; b < nB; b++) {
+            std::complex<float> acc(0.0f, 0.0f);
+            const float th = (S.dims == 2) ? S.bearings[b] : 0.0f;
+            for(uint32_t i = 0; i < size; i++) {
+                const SortedSample& s = B.sorted[off + i];
+                float uy = std::fmaf(S.pulse_scale, s.travel - R, 0.5f);
+                std::complex<float> w = lerp_border_f32(pulse_f, H, uy);
+                if(S.dims == 2) {
+                    float ux = std::fmaf(S.beam_scale, s.bearing - th, 0.5f);
+                    w *= lerp_border_f32(S.beam, W, ux);
+                }
+                acc += std::complex<float>(s.re, s.im) * w;
+            }
+            o[b] = acc;
+        }
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+// ---- range key (Binner::Key) ------------------------------------------------
+
+void rtacx_oracle_key_params(uint32_t binCount, float minBin, float maxBin, float margin,
+                             float* a, float* b, float* lower, float* upper)
+{
+    KeyParams k = make_key(binCount, minBin, maxBin, margin);
+    *a = k.a; *b = k.b; *lower = k.lower; *upper = k.upper;
+}
+
+// keys[i] = Key(travel[i * stride]); side[i] (optional) = -1 / 0 / +1 for
+// below-range out-of-range, in range, above-range out-of-range.
+void rtacx_oracle_range_keys(uint32_t binCount, float minBin, float maxBin, float margin,
+                             const float* travel, uint64_t n, uint32_t stride,
+                             uint32_t* keys, int8_t* side)
+{
+    KeyParams k = make_key(binCount, minBin, maxBin, margin);
+    for(uint64_t i = 0; i < n; i++) {
+        int sd;
+        keys[i] = range_key(k, travel[i * stride], &sd);
+        if(side) side[i] = (int8_t)sd;
+    }
+}
+
+int rtacx_oracle_bin_overlap(float rmin, float rmax, uint32_t n, float margin)
+{
+    return bin_overlap(rmin, rmax, n, margin);
+}
+
+float rtacx_oracle_linspace_at(float rmin, float rmax, uint32_t n, uint32_t r)
+{
+    return linspace_at(rmin, rmax, n, r);
+}
+
+// Bearing sub-bin of the (range-bin, bearing-bin) sort key used by the GPU
+// path (an extension: the reference keys by range only). With
+// q = fmaf(scale, bearing, offset): 0 if !(q >= 1) (NaN included),
+// count - 1 if q >= count, else (int)q. scale/offset are floats computed by the
+// caller.
+void rtacx_oracle_bearing_bins(float scale, float offset, uint32_t count,
+                               const float* bearing, uint64_t n, uint32_t stride, uint32_t* out)
+{
+    for(uint64_t i = 0; i < n; i++) {
+        float q = std::fmaf(scale, bearing[i * stride], offset);
+        uint32_t kb;
+        if(!(q >= 1.0f)) kb = 0;
+        else if(q >= (float)count) kb = count - 1;
+        else kb = (uint32_t)(int)q;
+        out[i] = kb;
+    }
+}
+
+// Reference segments (binIndexes_) and windows (bins_ as {offset, size}) for a
+// sample buffer; samples are AoS with `stride` floats per sample
+// (3 = SimSample1D, 4 = SimSample2D). Also returns the low/high out-of-range
+// counts and the overlap.
+int rtacx_oracle_bin(const float* samples, uint64_t n, uint32_t stride, uint32_t dims,
+                     float rmin, float rmax, uint32_t nR, float margin,
+                     uint32_t* segments, uint32_t* windows, uint32_t* counts,
+                     uint64_t* low_oor, uint64_t* high_oor)
+{
+    KeyParams key = make_key(nR, rmin, rmax, margin);
+    BinResult B;
+    do_bin(samples, n, stride, dims, key, rmin, rmax, nR, margin, B);
+    if(segments) std::memcpy(segments, B.segments.data(), B.segments.size() * 4);
+    if(windows) std::memcpy(windows, B.windows.data(), B.windows.size() * 4);
+    if(counts || low_oor || high_oor) {
+        uint64_t lo = 0, hi = 0;
+        if(counts) std::memset(counts, 0, (size_t)nR * 4);
+        for(uint64_t i = 0; i < n; i++) {
+            int sd; uint32_t k = range_key(key, samples[i * stride + 2], &sd);
+            if(k != kOutOfRange) { if(counts) counts[k]++; }
+            else if(sd < 0) lo++;
+            else hi++;
+        }
+        if(low_oor) *low_oor = lo;
+        if(high_oor) *high_oor = hi;
+    }
+    return B.overlap;
+}
+
+// Full reduction. mode 0: FP64 (out = 2 doubles per cell), mode 1: FP32
+// reference arithmetic (out = 2 floats per cell). Rows [row_begin, row_end)
+// only; nthreads worker threads. Returns the wall time of the sort+bin step
+// in seconds through bin_seconds (optional).
+void rtacx_oracle_reduce(uint32_t dims, const float* samples, uint64_t n,
+                         float rmin, float rmax, uint32_t nR, float margin,
+                         float pulse_scale, const float* pulse, uint32_t pulse_len,
+                         float beam_scale, const float* beam, uint32_t beam_len,
+                         const float* bearings, uint32_t nB,
+                         int mode, uint32_t row_begin, uint32_t row_end, int nthreads,
+                         void* out)
+{
+    Sensor S{dims, rmin, rmax, nR, margin, pulse_scale, pulse_len, pulse,
+             beam_scale, beam_len, beam, nB, bearings};
+    KeyParams key = make_key(nR, rmin, rmax, margin);
+    BinResult B;
+    do_bin(samples, n, dims == 2 ? 4u : 3u, dims, key, rmin, rmax, nR, margin, B);
+    const uint32_t nb = (dims == 2) ? nB : 1u;
+    const size_t cell = (mode == 0) ? 16 : 8;
+    row_end = std::min(row_end, nR);
+    parallel_rows(row_begin, row_end, nthreads, [&](uint32_t r) {
+        reduce_row(S, B, r, mode, static_cast<char*>(out) + (size_t)(r - row_begin) * nb * cell);
+    });
+}
+
+} // extern "C"

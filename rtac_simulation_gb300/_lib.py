@@ -1,0 +1,204 @@
+"""ctypes binding of librtacx.so (include/rtacx.h).
+
+The binding carries plain integers (device pointers, stream handles) across
+the C ABI; torch is not needed here. Loading fails loudly when the library has
+not been built: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "librtacx.so"
+
+RTACX_OK = 0
+RTACX_ERR_INVALID_ARGUMENT = 1
+RTACX_ERR_NOT_CONFIGURED = 2
+RTACX_ERR_CUDA = 3
+RTACX_ERR_OUT_OF_MEMORY = 4
+RTACX_ERR_DEVICE = 5
+RTACX_ERR_UNSUPPORTED = 6
+RTACX_KEY_OUT_OF_RANGE = 0xFFFFFFFF
+RTACX_SAMPLE_1D = 1
+RTACX_SAMPLE_2D = 2
+RTACX_FLAG_1D_LITERAL_SCALING = 1
+
+_STATUS_NAMES = {
+    RTACX_OK: "RTACX_OK",
+    RTACX_ERR_INVALID_ARGUMENT: "RTACX_ERR_INVALID_ARGUMENT",
+    RTACX_ERR_NOT_CONFIGURED: "RTACX_ERR_NOT_CONFIGURED",
+    RTACX_ERR_CUDA: "RTACX_ERR_CUDA",
+    RTACX_ERR_OUT_OF_MEMORY: "RTACX_ERR_OUT_OF_MEMORY",
+    RTACX_ERR_DEVICE: "RTACX_ERR_DEVICE",
+    RTACX_ERR_UNSUPPORTED: "RTACX_ERR_UNSUPPORTED",
+}
+
+# Every entry point include/rtacx.h declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_U64 = ctypes.c_uint64
+_I = ctypes.c_int
+
+
+class Sensor1D(ctypes.Structure):
+    _fields_ = [("range_min", ctypes.c_float), ("range_max", ctypes.c_float), ("range_count", _U32),
+                ("sound_celerity", ctypes.c_float), ("pulse_duration", ctypes.c_float),
+                ("margin", ctypes.c_float), ("pulse", _P), ("pulse_len", _U32), ("flags", _U32)]
+
+
+class Sensor2D(ctypes.Structure):
+    _fields_ = [("range_min", ctypes.c_float), ("range_max", ctypes.c_float), ("range_count", _U32),
+                ("sound_celerity", ctypes.c_float), ("pulse_duration", ctypes.c_float),
+                ("margin", ctypes.c_float), ("pulse", _P), ("pulse_len", _U32),
+                ("beam", _P), ("beam_len", _U32), ("beam_span", ctypes.c_float),
+                ("bearings", _P), ("bearing_count", _U32), ("flags", _U32)]
+
+
+SIGNATURES = {
+    "rtacx_version": (ctypes.c_char_p, []),
+    "rtacx_create": (_I, [ctypes.POINTER(_P), _I]),
+    "rtacx_destroy": (None, [_P]),
+    "rtacx_last_error": (ctypes.c_char_p, [_P]),
+    "rtacx_configure_1d": (_I, [_P, ctypes.POINTER(Sensor1D)]),
+    "rtacx_configure_2d": (_I, [_P, ctypes.POINTER(Sensor2D)]),
+    "rtacx_reserve": (_I, [_P, _U64]),
+    "rtacx_bin": (_I, [_P, _P, _U64, _I, _P, _P, _P, _P, _P, _P]),
+    "rtacx_reduce": (_I, [_P, _P, _U64, _P, _P]),
+    "rtacx_stream_status": (_I, [_P, _P]),
+    "rtacx_set_tracing": (_I, [_P, _I]),
+    "rtacx_stage_times": (_I, [_P, ctypes.POINTER(ctypes.c_float), _I]),
+}
+
+STAGES = ("count", "colscan", "binscan", "scatter", "windows", "reduce")
+
+_lib = None
+
+
+class RtacxError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def load() -> ctypes.CDLL:
+    """Load librtacx.so, binding every declared entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m rtac_simulation_gb300.build`")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(x) -> int | None:
+    """Device pointer of a torch tensor, an int, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _stream(s) -> int | None:
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+class Context:
+    """One rtacx context (a configured sensor plus its device scratch)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = _P()
+        st = self._lib.rtacx_create(ctypes.byref(h), device)
+        if st != RTACX_OK:
+            raise RtacxError(st, f"rtacx_create(device={device}) failed")
+        self._h = h
+        self.device = device
+        self.dims = 0
+        self._keep = []
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.rtacx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def last_error(self) -> str:
+        msg = self._lib.rtacx_last_error(self._h)
+        return msg.decode() if msg else ""
+
+    def _check(self, st: int) -> None:
+        if st != RTACX_OK:
+            raise RtacxError(st, self.last_error())
+
+    def configure_1d(self, *, range_min, range_max, range_count, sound_celerity, pulse_duration,
+                     margin, pulse, flags=0) -> None:
+        p = np.ascontiguousarray(np.asarray(pulse, dtype=np.complex64))
+        s = Sensor1D(range_min, range_max, range_count, sound_celerity, pulse_duration, margin,
+                     p.ctypes.data, p.size, flags)
+        self._check(self._lib.rtacx_configure_1d(self._h, ctypes.byref(s)))
+        self.dims = 1
+
+    def configure_2d(self, *, range_min, range_max, range_count, sound_celerity, pulse_duration,
+                     margin, pulse, beam, beam_span, bearings, flags=0) -> None:
+        p = np.ascontiguousarray(np.asarray(pulse, dtype=np.complex64))
+        bm = np.ascontiguousarray(np.asarray(beam, dtype=np.float32))
+        br = np.ascontiguousarray(np.asarray(bearings, dtype=np.float32))
+        s = Sensor2D(range_min, range_max, range_count, sound_celerity, pulse_duration, margin,
+                     p.ctypes.data, p.size, bm.ctypes.data, bm.size, beam_span,
+                     br.ctypes.data, br.size, flags)
+        self._check(self._lib.rtacx_configure_2d(self._h, ctypes.byref(s)))
+        self.dims = 2
+
+    def reserve(self, max_samples: int) -> None:
+        self._check(self._lib.rtacx_reserve(self._h, max_samples))
+
+    def bin(self, samples, n: int, kind: int, keys=None, segments=None, windows=None,
+            counts=None, oor=None, stream=None) -> None:
+        self._check(self._lib.rtacx_bin(self._h, _ptr(samples), n, kind, _ptr(keys), _ptr(segments),
+                                        _ptr(windows), _ptr(counts), _ptr(oor), _stream(stream)))
+
+    def reduce(self, samples, n: int, out, stream=None) -> None:
+        self._check(self._lib.rtacx_reduce(self._h, _ptr(samples), n, _ptr(out), _stream(stream)))
+
+    def set_tracing(self, enable: bool) -> None:
+        self._check(self._lib.rtacx_set_tracing(self._h, 1 if enable else 0))
+
+    def stage_times(self) -> dict:
+        """Per-stage device milliseconds of the last traced rtacx_reduce."""
+        buf = (ctypes.c_float * len(STAGES))()
+        k = self._lib.rtacx_stage_times(self._h, buf, len(STAGES))
+        if k < 0:
+            raise RtacxError(-k, self.last_error())
+        return {STAGES[i]: float(buf[i]) for i in range(k)}
+
+    def stream_status(self, stream=None) -> None:
+        self._check(self._lib.rtacx_stream_status(self._h, _stream(stream)))

@@ -1,0 +1,74 @@
+"""Build recipe for librtacx.so (sm_103a) and the C++ host-mirror demo.
+
+Compiles every translation unit of ``csrc/`` in parallel with nvcc for
+``sm_103a`` only and links them into ``rtac_simulation_gb300/librtacx.so``
+(in-tree, git-ignored). ``python -m rtac_simulation_gb300.build`` runs it.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OBJ = PKG / "_build"
+LIB = PKG / "librtacx.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math",
+              "-I", str(ROOT / "include")]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+             "-I", str(ROOT / "include")]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"command failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
+
+
+def build_library(verbose: bool = False, ptxas_info: bool = False) -> Path:
+    nvcc = _nvcc()
+    OBJ.mkdir(exist_ok=True)
+    srcs = sources()
+    jobs = []
+    for src in srcs:
+        obj = OBJ / (src.name + ".o")
+        if src.suffix == ".cu":
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+            if ptxas_info:
+                cmd += ["-Xptxas", "-v"]
+        else:
+            cmd = ["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)]
+        jobs.append((cmd, obj))
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+        futs = [ex.submit(_run, cmd) for cmd, _ in jobs]
+        for f in futs:
+            f.result()
+    tmp = LIB.with_suffix(".so.tmp")
+    _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o in jobs]])
+    os.replace(tmp, LIB)
+    if verbose:
+        print(f"built {LIB}")
+    return LIB
+
+
+if __name__ == "__main__":
+    build_library(verbose=True, ptxas_info="--ptxas" in sys.argv)

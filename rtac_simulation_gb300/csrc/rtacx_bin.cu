@@ -1,0 +1,370 @@
+// Sort + bin: a counting sort of echo samples by (range bin, bearing bin).
+//
+// Replaces sort() (src/Receiver.cu:9-42: thrust merge sort of the AoS
+// samples by travel) and Binner::compute (src/Binner.cu:24-136: key
+// transform, segment search, window construction). Only the multiset of
+// samples per range bin matters downstream -- the reference's reduction sums
+// a window of consecutive bins in any order -- so a counting sort on the
+// integer key gives the reference's segments and windows exactly without a
+// comparison sort.
+//
+// Passes (persistent CTAs, each owning one contiguous chunk of the input):
+//   k_count      key of every sample, per-CTA histogram in shared memory
+//                (warp-aggregated atomics for hot bins), written as one row
+//                of the [cta][bin] matrix; out-of-range counts.
+//   k_colscan    per bin, exclusive prefix over CTAs (in place) + bin total.
+//   k_binscan    exclusive scan of bin totals -> bin offsets.
+//   k_scatter    re-reads the chunk, ranks each sample in shared memory and
+//                writes it as a float4 {re, im, travel, bearing} record to
+//                offsets[bin] + prefix[cta][bin] + rank.
+//   k_windows    reference windows (do_make_bins, src/Binner.cu:82-106) as
+//                range-bin intervals, intersected with each row's PSF support.
+#include "rtacx_internal.cuh"
+
+#include <algorithm>
+#include <climits>
+
+namespace rtacx {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// One warp-uniform pass over a CTA's chunk. f(valid, record, key, side) is
+// called by every lane of every warp the same number of times.
+template <typename F>
+__device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, const BinParams& p, F&& f)
+{
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t begin = (uint64_t)blockIdx.x * chunk;
+    const uint64_t end = min(begin + chunk, n);
+    for(uint64_t i0 = begin + (threadIdx.x & ~31u); i0 < end; i0 += blockDim.x) {
+        const uint64_t i = i0 + lane_id();
+        const bool valid = i < end;
+        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t key = kOutOfRange;
+        int side = 0;
+        if(valid) {
+            rec = load_record(samples, i, p);
+            key = sample_key(p, rec.z, rec.w, side);
+        }
+        f(valid, rec, key, side);
+    }
+}
+
+__global__ void k_count(const float* __restrict__ samples, uint64_t n, BinParams p,
+                        uint32_t* __restrict__ hist, unsigned long long* __restrict__ oor)
+{
+    extern __shared__ uint32_t sh[];
+    __shared__ unsigned long long s_oor[2];
+    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = 0u;
+    if(threadIdx.x < 2) s_oor[threadIdx.x] = 0ull;
+    __syncthreads();
+
+    uint32_t low = 0, high = 0;
+    for_chunk(samples, n, p, [&](bool valid, const float4&, uint32_t key, int side) {
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if(valid && key != kOutOfRange) {
+            if(lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&sh[key], (uint32_t)__popc(peers));
+        }
+        else if(valid) {
+            if(side < 0) low++; else high++;
+        }
+    });
+    for(int o = 16; o > 0; o >>= 1) {
+        low += __shfl_down_sync(0xffffffffu, low, o);
+        high += __shfl_down_sync(0xffffffffu, high, o);
+    }
+    if(lane_id() == 0 && (low | high)) {
+        atomicAdd(&s_oor[0], (unsigned long long)low);
+        atomicAdd(&s_oor[1], (unsigned long long)high);
+    }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        if(s_oor[0]) atomicAdd(&oor[0], s_oor[0]);
+        if(s_oor[1]) atomicAdd(&oor[1], s_oor[1]);
+    }
+    uint32_t* row = hist + (size_t)blockIdx.x * p.nBins;
+    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) row[b] = sh[b];
+}
+
+// Per bin: hist[c][b] <- sum_{c' < c} hist[c'][b]; totals[b] <- sum_c hist[c][b].
+__global__ void k_colscan(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t nBins,
+                          uint32_t* __restrict__ totals)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if(b >= nBins) return;
+    uint32_t run = 0;
+    uint32_t c = 0;
+    for(; c + 8 <= ctas; c += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for(int u = 0; u < 8; u++) v[u] = hist[(size_t)(c + u) * nBins + b];
+#pragma unroll
+        for(int u = 0; u < 8; u++) { hist[(size_t)(c + u) * nBins + b] = run; run += v[u]; }
+    }
+    for(; c < ctas; c++) {
+        uint32_t v = hist[(size_t)c * nBins + b];
+        hist[(size_t)c * nBins + b] = run;
+        run += v;
+    }
+    totals[b] = run;
+}
+
+// Exclusive block scan of one value per thread (blockDim.x == kScanThreads).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t& total)
+{
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for(int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if(lane >= (unsigned)o) x += y;
+    }
+    if(lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    const unsigned nw = blockDim.x >> 5;
+    if(warp == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0u;
+        for(int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if(lane >= (unsigned)o) w += y;
+        }
+        if(lane < nw) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[nw - 1];
+    const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __restrict__ totals, uint32_t nBins,
+                                                           uint32_t* __restrict__ offsets)
+{
+    __shared__ uint32_t s_warp[32];
+    const uint32_t per = (nBins + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    const uint32_t b1 = min(b0 + per, nBins);
+    uint32_t sum = 0;
+    for(uint32_t b = b0; b < b1; b++) sum += totals[b];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(sum, s_warp, total);
+    for(uint32_t b = b0; b < b1; b++) { offsets[b] = run; run += totals[b]; }
+    if(threadIdx.x == 0) offsets[nBins] = total;
+}
+
+__global__ void k_scatter(const float* __restrict__ samples, uint64_t n, BinParams p,
+                          const uint32_t* __restrict__ hist, const uint32_t* __restrict__ offsets,
+                          float4* __restrict__ sorted, uint32_t* __restrict__ err)
+{
+    extern __shared__ uint32_t sh[];
+    const uint32_t* row = hist + (size_t)blockIdx.x * p.nBins;
+    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = offsets[b] + row[b];
+    const uint32_t total = offsets[p.nBins];
+    __syncthreads();
+
+    const unsigned lt_mask = (1u << lane_id()) - 1u;
+    for_chunk(samples, n, p, [&](bool valid, const float4& rec, uint32_t key, int) {
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        const bool live = valid && key != kOutOfRange;
+        if(live && (int)lane_id() == leader) base = atomicAdd(&sh[key], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if(live) {
+            const uint32_t pos = base + (uint32_t)__popc(peers & lt_mask);
+            if(pos < total) sorted[pos] = rec;
+            else atomicOr(err, kErrScatterOverflow);
+        }
+    });
+}
+
+__device__ __forceinline__ uint32_t bin_count(const uint32_t* off, uint32_t nBB, int j)
+{
+    return off[(size_t)(j + 1) * nBB] - off[(size_t)j * nBB];
+}
+
+// First / last non-empty range bin of row r's reference window
+// [max(0, r - ov), min(nR - 1, r + ov)]; returns false for the empty view
+// (no non-empty bin, or istart >= iend: src/Binner.cu:95-104).
+__device__ __forceinline__ bool ref_window(const uint32_t* off, uint32_t nBB, uint32_t nR, int ov, int r,
+                                           int& f, int& l)
+{
+    const long long lo = max(0ll, (long long)r - ov);
+    const long long hi = min((long long)nR - 1, (long long)r + ov);
+    long long a = lo;
+    while(a <= hi && bin_count(off, nBB, (int)a) == 0u) a++;
+    if(a >= hi) return false;
+    long long z = hi;
+    while(z > a && bin_count(off, nBB, (int)z) == 0u) z--;
+    if(a >= z) return false;
+    f = (int)a; l = (int)z;
+    return true;
+}
+
+__global__ void k_windows(const uint32_t* __restrict__ off, uint32_t nBB, uint32_t nR, int ov,
+                          const int2* __restrict__ support, int2* __restrict__ win)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if(r >= (int)nR) return;
+    int f, l;
+    int2 w = make_int2(1, 0);
+    if(ref_window(off, nBB, nR, ov, r, f, l)) {
+        const int2 s = support[r];
+        w = make_int2(max(f, s.x), min(l, s.y));
+    }
+    win[r] = w;
+}
+
+// Reference-coordinate outputs of rtacx_bin: the reference's sorted array
+// puts the below-range out-of-range samples first, then the bins in order.
+__global__ void k_ref_outputs(const uint32_t* __restrict__ off, uint32_t nBB, uint32_t nR, int ov,
+                              const unsigned long long* __restrict__ oor,
+                              uint32_t* __restrict__ segments, uint32_t* __restrict__ windows,
+                              uint32_t* __restrict__ counts)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if(r >= (int)nR) return;
+    const uint32_t lowc = (uint32_t)oor[0];
+    const uint32_t cnt = bin_count(off, nBB, r);
+    if(counts) counts[r] = cnt;
+    if(segments) {
+        uint2 s = make_uint2(0u, 0u);
+        if(cnt) s = make_uint2(lowc + off[(size_t)r * nBB], lowc + off[(size_t)(r + 1) * nBB]);
+        reinterpret_cast<uint2*>(segments)[r] = s;
+    }
+    if(windows) {
+        int f, l;
+        uint2 w = make_uint2(0u, 0u);
+        if(ref_window(off, nBB, nR, ov, r, f, l))
+            w = make_uint2(lowc + off[(size_t)f * nBB], off[(size_t)(l + 1) * nBB] - off[(size_t)f * nBB]);
+        reinterpret_cast<uint2*>(windows)[r] = w;
+    }
+}
+
+__global__ void k_range_keys(const float* __restrict__ samples, uint64_t n, BinParams p, uint32_t* __restrict__ keys)
+{
+    for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float t = __ldg(samples + i * p.stride + 2);
+        int side;
+        keys[i] = range_key(p.key, t, side);
+    }
+}
+
+__global__ void k_oor_out(const unsigned long long* __restrict__ src, uint64_t* __restrict__ dst)
+{
+    if(threadIdx.x < 2) dst[threadIdx.x] = src[threadIdx.x];
+}
+
+uint32_t hist_grid(const Context& ctx, uint64_t n)
+{
+    // At least ~4096 samples per CTA so that the per-CTA histogram rows stay
+    // small relative to the data.
+    const uint64_t want = std::max<uint64_t>(1, (n + 4095) / 4096);
+    return (uint32_t)std::min<uint64_t>(ctx.hist_ctas, want);
+}
+
+#define RTACX_CUDA(call)                                                         \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if(e_ != cudaSuccess) {                                                  \
+            ctx.error = std::string(#call) + ": " + cudaGetErrorString(e_);      \
+            return RTACX_ERR_CUDA;                                               \
+        }                                                                        \
+    } while(0)
+
+} // namespace
+
+bool ensure_capacity(Context& ctx, uint64_t n)
+{
+    if(n <= ctx.capacity) return true;
+    uint64_t cap = std::max<uint64_t>(n, 1024);
+    float4* p = nullptr;
+    if(cudaMalloc(&p, cap * sizeof(float4)) != cudaSuccess) {
+        cudaGetLastError();
+        return ctx.fail("out of device memory for " + std::to_string(cap) + " sorted samples");
+    }
+    if(ctx.d_sorted) cudaFree(ctx.d_sorted);
+    ctx.d_sorted = p;
+    ctx.capacity = cap;
+    return true;
+}
+
+void configure_hist_launch(Context& ctx);
+
+rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream)
+{
+    const BinParams& p = ctx.bin;
+    RTACX_CUDA(cudaMemsetAsync(ctx.d_oor, 0, 2 * sizeof(unsigned long long), stream));
+    if(n == 0) {
+        RTACX_CUDA(cudaMemsetAsync(ctx.d_offsets, 0, (p.nBins + 1) * sizeof(uint32_t), stream));
+    }
+    else {
+        const uint32_t grid = hist_grid(ctx, n);
+        const size_t smem = (size_t)p.nBins * sizeof(uint32_t);
+        const float* s = static_cast<const float*>(samples);
+        ctx.mark(0, false, stream);
+        k_count<<<grid, ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist, ctx.d_oor);
+        RTACX_CUDA(cudaGetLastError());
+        ctx.mark(0, true, stream);
+        ctx.mark(1, false, stream);
+        k_colscan<<<(p.nBins + 255) / 256, 256, 0, stream>>>(ctx.d_hist, grid, p.nBins, ctx.d_totals);
+        RTACX_CUDA(cudaGetLastError());
+        ctx.mark(1, true, stream);
+        ctx.mark(2, false, stream);
+        k_binscan<<<1, kScanThreads, 0, stream>>>(ctx.d_totals, p.nBins, ctx.d_offsets);
+        RTACX_CUDA(cudaGetLastError());
+        ctx.mark(2, true, stream);
+        ctx.mark(3, false, stream);
+        k_scatter<<<grid, ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets,
+                                                             ctx.d_sorted, ctx.d_err);
+        RTACX_CUDA(cudaGetLastError());
+        ctx.mark(3, true, stream);
+    }
+    ctx.mark(4, false, stream);
+    k_windows<<<(ctx.nR + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, p.nBB, ctx.nR, ctx.overlap,
+                                                         ctx.d_support, ctx.d_win);
+    RTACX_CUDA(cudaGetLastError());
+    ctx.mark(4, true, stream);
+    return RTACX_OK;
+}
+
+rtacx_status run_bin_outputs(Context& ctx, const void* samples, uint64_t n,
+                             uint32_t* keys, uint32_t* segments, uint32_t* windows,
+                             uint32_t* counts, uint64_t* oor, cudaStream_t stream)
+{
+    const BinParams& p = ctx.bin;
+    if(keys && n) {
+        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx.sm_count * 16);
+        k_range_keys<<<blocks, 256, 0, stream>>>(static_cast<const float*>(samples), n, p, keys);
+        RTACX_CUDA(cudaGetLastError());
+    }
+    if(segments || windows || counts) {
+        k_ref_outputs<<<(ctx.nR + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, p.nBB, ctx.nR, ctx.overlap,
+                                                                 ctx.d_oor, segments, windows, counts);
+        RTACX_CUDA(cudaGetLastError());
+    }
+    if(oor) {
+        k_oor_out<<<1, 32, 0, stream>>>(ctx.d_oor, oor);
+        RTACX_CUDA(cudaGetLastError());
+    }
+    return RTACX_OK;
+}
+
+// Launch shape of the count / scatter passes for the configured bin count.
+void configure_hist_launch(Context& ctx)
+{
+    const size_t smem = (size_t)ctx.bin.nBins * sizeof(uint32_t);
+    cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
+    cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
+    ctx.hist_threads = 512;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter, (int)ctx.hist_threads, smem);
+    per_sm = std::max(1, std::min(per_sm, 4));
+    ctx.hist_ctas = (uint32_t)(ctx.sm_count * per_sm);
+    cudaGetLastError();
+}
+
+} // namespace rtacx

@@ -1,0 +1,313 @@
+// Plain sparse PSF reduction (FP32 SIMT).
+//
+// Replaces do_sparse_convolve_2d_f (src/SensorInstance2D.cu:44-119) and
+// do_sparse_convolve_1d_f (src/SensorInstance1D.cu:35-89):
+//   out(r, b) = sum_{s in window(r)} v_s * pulse(t_s - R_r) * beam(theta_s - theta_b)
+// where pulse / beam are the texture lookups of KernelView2D
+// (include/rtac_simulation/ReductionKernel.h:44-73): normalized coordinate
+// u = scale * delta + 0.5, linear filter, border addressing. The bilinear
+// fetch of the separable table PSF[h][w] = pulse[h] * beam[w]
+// (src/SensorInstance2D.cu:20-33) is the product of the two 1D lerps, which
+// this file evaluates in software from shared-memory copies of the 1D tables
+// with exact (not 9-bit fixed point) weights.
+//
+// 2D layout: one CTA per (TR range rows x TB bearings) tile. Samples of the
+// tile's range-bin span and bearing-bin span are streamed through shared
+// memory in chunks of K; for each chunk the CTA evaluates
+//   U[k][r] = v_k * pulse(t_k - R_r)   (zero unless bin_k is in row r's window)
+//   B[k][b] = beam(theta_k - theta_b)
+// once, then every thread accumulates its (rows x bearings) register block:
+// acc[r][b] += U[k][r] * B[k][b]. A warp skips a chunk whose range bins lie
+// outside its rows' windows.
+#include "rtacx_internal.cuh"
+
+#include <algorithm>
+
+namespace rtacx {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 64;
+
+// Lerp of a zero-padded table (tab[0] = tab[n + 1] = 0, tab[i + 1] = T[i]).
+// Returns 0 outside the support of the border-addressed linear filter.
+__device__ __forceinline__ float lerp_real(const float* tab, const AxisLerp& ax, float delta)
+{
+    const float x1 = fmaf(delta, ax.k_hi, ax.c);
+    const float fi = floorf(x1);
+    if(!(fi >= -1.0f && fi <= (float)(ax.n - 1))) return 0.0f;
+    const float alpha = fmaf(delta, ax.k_lo, fmaf(delta, ax.k_hi, ax.c - fi));
+    const int i = (int)fi + 1;
+    const float lo = tab[i], hi = tab[i + 1];
+    return fmaf(alpha, hi - lo, lo);
+}
+
+__device__ __forceinline__ float2 lerp_cplx(const float2* tab, const AxisLerp& ax, float delta)
+{
+    const float x1 = fmaf(delta, ax.k_hi, ax.c);
+    const float fi = floorf(x1);
+    if(!(fi >= -1.0f && fi <= (float)(ax.n - 1))) return make_float2(0.f, 0.f);
+    const float alpha = fmaf(delta, ax.k_lo, fmaf(delta, ax.k_hi, ax.c - fi));
+    const int i = (int)fi + 1;
+    const float2 lo = tab[i], hi = tab[i + 1];
+    return make_float2(fmaf(alpha, hi.x - lo.x, lo.x), fmaf(alpha, hi.y - lo.y, lo.y));
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+template <int TR, int TB>
+struct GatherSmem {
+    float2 U[kChunk][TR];
+    float B[kChunk][TB];
+    float4 smp[kChunk];
+    int bin[kChunk];
+    uint32_t seg_start[kThreads];
+    uint32_t seg_pre[kThreads + 1];
+    float R[TR];
+    float theta[TB];
+    int elo[TR], ehi[TR];
+    uint32_t warp_sums[kWarps];
+    int jmin, jmax;
+};
+
+template <int TR, int TB>
+__global__ void __launch_bounds__(kThreads)
+k_gather_2d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+            const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
+            const float* __restrict__ ranges, const float* __restrict__ bearings,
+            const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
+            ReduceParams rp, uint32_t nBB, float2* __restrict__ out)
+{
+    constexpr int RPW = TR / kWarps;   // rows per warp
+    constexpr int BPL = TB / 32;       // bearings per lane
+    static_assert(TR % kWarps == 0 && TB % 32 == 0, "tile shape");
+    using Smem = GatherSmem<TR, TB>;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+    float2* s_pulse = reinterpret_cast<float2*>(smem_raw + sizeof(Smem));
+    float* s_beam = reinterpret_cast<float*>(s_pulse + (rp.range_axis.n + 2));
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = blockIdx.y * TR, b0 = blockIdx.x * TB;
+    const int nR = (int)rp.nR, nB = (int)rp.nB;
+
+    for(int i = tid; i < rp.range_axis.n + 2; i += kThreads) s_pulse[i] = pulse_pad[i];
+    for(int i = tid; i < rp.beam_axis.n + 2; i += kThreads) s_beam[i] = beam_pad[i];
+    if(tid == 0) { S.jmin = INT_MAX; S.jmax = INT_MIN; }
+    __syncthreads();
+    if(tid < TR) {
+        const int r = r0 + tid;
+        int2 w = make_int2(1, 0);
+        float R = 0.0f;
+        if(r < nR) { w = win[r]; R = ranges[r]; }
+        S.elo[tid] = w.x; S.ehi[tid] = w.y; S.R[tid] = R;
+        if(w.x <= w.y) { atomicMin(&S.jmin, w.x); atomicMax(&S.jmax, w.y); }
+    }
+    for(int i = tid; i < TB; i += kThreads) {
+        const int b = b0 + i;
+        S.theta[i] = b < nB ? bearings[b] : 0.0f;
+    }
+    __syncthreads();
+
+    // Range-bin span of this warp's rows.
+    int wlo = INT_MAX, whi = INT_MIN;
+#pragma unroll
+    for(int q = 0; q < RPW; q++) {
+        const int rr = warp * RPW + q;
+        if(S.elo[rr] <= S.ehi[rr]) { wlo = min(wlo, S.elo[rr]); whi = max(whi, S.ehi[rr]); }
+    }
+
+    float2 acc[RPW][BPL];
+#pragma unroll
+    for(int q = 0; q < RPW; q++)
+#pragma unroll
+        for(int c = 0; c < BPL; c++) acc[q][c] = make_float2(0.f, 0.f);
+
+    const int jmin = S.jmin, jmax = S.jmax;
+    const int2 kb = bb_tiles[blockIdx.x];
+    for(int jg = jmin; jg <= jmax; jg += kThreads) {
+        // Segment of bin (jg + tid) restricted to this tile's bearing bins.
+        const int j = jg + tid;
+        uint32_t start = 0, len = 0;
+        if(j <= jmax) {
+            start = off[(size_t)j * nBB + kb.x];
+            len = off[(size_t)j * nBB + kb.y + 1] - start;
+        }
+        // Exclusive scan of the segment lengths.
+        uint32_t x = len;
+        for(int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if(lane >= o) x += y;
+        }
+        if(lane == 31) S.warp_sums[warp] = x;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for(int w = 0; w < kWarps; w++) {
+            const uint32_t v = S.warp_sums[w];
+            if(w < warp) before += v;
+            total += v;
+        }
+        S.seg_start[tid] = start;
+        S.seg_pre[tid] = before + x - len;
+        if(tid == 0) S.seg_pre[kThreads] = total;
+        __syncthreads();
+
+        for(uint32_t c0 = 0; c0 < total; c0 += kChunk) {
+            const int valid = (int)((total - c0) < (uint32_t)kChunk ? (total - c0) : (uint32_t)kChunk);
+            if(tid < kChunk) {
+                if(tid < valid) {
+                    const uint32_t g = c0 + tid;
+                    int lo = 0, hi = kThreads - 1;     // largest t with seg_pre[t] <= g
+                    while(lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if(S.seg_pre[mid] <= g) lo = mid; else hi = mid - 1;
+                    }
+                    S.smp[tid] = sorted[S.seg_start[lo] + (g - S.seg_pre[lo])];
+                    S.bin[tid] = jg + lo;
+                }
+                else {
+                    S.smp[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    S.bin[tid] = INT_MIN;
+                }
+            }
+            __syncthreads();
+            for(int e = tid; e < kChunk * TR; e += kThreads) {
+                const int k = e / TR, rr = e % TR;
+                const int bin = S.bin[k];
+                float2 u = make_float2(0.f, 0.f);
+                if(bin >= S.elo[rr] && bin <= S.ehi[rr]) {
+                    const float4 s = S.smp[k];
+                    const float2 w = lerp_cplx(s_pulse, rp.range_axis, s.z - S.R[rr]);
+                    u = cmul(make_float2(s.x, s.y), w);
+                }
+                S.U[k][rr] = u;
+            }
+            for(int e = tid; e < kChunk * TB; e += kThreads) {
+                const int k = e / TB, bb = e % TB;
+                float v = 0.0f;
+                if(k < valid && b0 + bb < nB) v = lerp_real(s_beam, rp.beam_axis, S.smp[k].w - S.theta[bb]);
+                S.B[k][bb] = v;
+            }
+            __syncthreads();
+            const int cb0 = S.bin[0], cb1 = S.bin[valid - 1];
+            if(cb1 >= wlo && cb0 <= whi) {
+                for(int k = 0; k < valid; k++) {
+                    float2 u[RPW];
+                    float bv[BPL];
+#pragma unroll
+                    for(int q = 0; q < RPW; q++) u[q] = S.U[k][warp * RPW + q];
+#pragma unroll
+                    for(int c = 0; c < BPL; c++) bv[c] = S.B[k][lane * BPL + c];
+#pragma unroll
+                    for(int q = 0; q < RPW; q++)
+#pragma unroll
+                        for(int c = 0; c < BPL; c++) {
+                            acc[q][c].x = fmaf(u[q].x, bv[c], acc[q][c].x);
+                            acc[q][c].y = fmaf(u[q].y, bv[c], acc[q][c].y);
+                        }
+                }
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for(int q = 0; q < RPW; q++) {
+        const int r = r0 + warp * RPW + q;
+        if(r >= nR) continue;
+#pragma unroll
+        for(int c = 0; c < BPL; c++) {
+            const int b = b0 + lane * BPL + c;
+            if(b < nB) out[(size_t)r * nB + b] = acc[q][c];
+        }
+    }
+}
+
+// 1D: one warp per output range bin.
+__global__ void __launch_bounds__(kThreads)
+k_gather_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+            const int2* __restrict__ win, const float* __restrict__ ranges,
+            const float2* __restrict__ pulse_pad, ReduceParams rp, float2* __restrict__ out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s_pulse = reinterpret_cast<float2*>(smem_raw);
+    for(int i = threadIdx.x; i < rp.range_axis.n + 2; i += kThreads) s_pulse[i] = pulse_pad[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    if(r >= (int)rp.nR) return;
+    const int2 w = win[r];
+    float2 acc = make_float2(0.f, 0.f);
+    if(w.x <= w.y) {
+        const float R = ranges[r];
+        const uint32_t p0 = off[w.x], p1 = off[w.y + 1];
+        for(uint32_t i = p0 + lane; i < p1; i += 32) {
+            const float4 s = sorted[i];
+            const float2 wv = lerp_cplx(s_pulse, rp.range_axis, s.z - R);
+            const float2 u = cmul(make_float2(s.x, s.y), wv);
+            acc.x += u.x; acc.y += u.y;
+        }
+    }
+    for(int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if(lane == 0) out[r] = acc;
+}
+
+template <int TR, int TB>
+rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
+{
+    const size_t smem = sizeof(GatherSmem<TR, TB>) + (ctx.H + 2) * sizeof(float2) + (ctx.W + 2) * sizeof(float);
+    static thread_local size_t configured = 0;
+    if(smem > configured) {
+        if(cudaFuncSetAttribute(k_gather_2d<TR, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            ctx.error = "PSF tables too large for shared memory (pulse " + std::to_string(ctx.H) +
+                        " taps, beam " + std::to_string(ctx.W) + " taps)";
+            return RTACX_ERR_UNSUPPORTED;
+        }
+        configured = smem;
+    }
+    dim3 grid((ctx.nB + TB - 1) / TB, (ctx.nR + TR - 1) / TR);
+    k_gather_2d<TR, TB><<<grid, kThreads, smem, stream>>>(ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles,
+                                                          ctx.d_ranges, ctx.d_bearings, ctx.d_pulse, ctx.d_beam,
+                                                          ctx.red, ctx.bin.nBB, out);
+    const cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) { ctx.error = std::string("k_gather_2d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    return RTACX_OK;
+}
+
+} // namespace
+
+size_t gather_smem_bytes(uint32_t range_tile, uint32_t bearing_tile, uint32_t H, uint32_t W)
+{
+    size_t base = range_tile == 32 ? sizeof(GatherSmem<32, 128>)
+                : bearing_tile == 128 ? sizeof(GatherSmem<16, 128>) : sizeof(GatherSmem<16, 64>);
+    return base + (H + 2) * sizeof(float2) + (W + 2) * sizeof(float);
+}
+
+rtacx_status run_reduce(Context& ctx, float* out_f, cudaStream_t stream)
+{
+    float2* out = reinterpret_cast<float2*>(out_f);
+    if(ctx.dims == 1) {
+        const size_t smem = (ctx.H + 2) * sizeof(float2);
+        if(smem > 48 * 1024)
+            cudaFuncSetAttribute(k_gather_1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_gather_1d<<<(ctx.nR + kWarps - 1) / kWarps, kThreads, smem, stream>>>(
+            ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_ranges, ctx.d_pulse, ctx.red, out);
+        const cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess) { ctx.error = std::string("k_gather_1d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+        return RTACX_OK;
+    }
+    if(ctx.range_tile == 32) return launch_2d<32, 128>(ctx, out, stream);
+    if(ctx.bearing_tile == 128) return launch_2d<16, 128>(ctx, out, stream);
+    return launch_2d<16, 64>(ctx, out, stream);
+}
+
+} // namespace rtacx

@@ -1,0 +1,82 @@
+"""The C-ABI library loads and exports every entry point include/rtacx.h
+declares, with the struct layouts the header defines. No GPU needed: no call
+here launches device work."""
+import ctypes
+import re
+import subprocess
+import tempfile
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "rtacx.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from rtac_simulation_gb300 import _lib, build
+    srcs = build.sources()
+    if not _lib.LIB_PATH.exists() or any(s.stat().st_mtime > _lib.LIB_PATH.stat().st_mtime for s in srcs):
+        build.build_library()
+    return _lib
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:rtacx_status|void|int|const char\*)\s+(rtacx_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert {"rtacx_create", "rtacx_destroy", "rtacx_configure_1d", "rtacx_configure_2d",
+            "rtacx_bin", "rtacx_reduce", "rtacx_stream_status"} <= set(names)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    so = ctypes.CDLL(str(lib.LIB_PATH))
+    for name in declared_functions():
+        assert hasattr(so, name), name
+        assert name in lib.SIGNATURES, f"{name} has no ctypes signature"
+    nm = subprocess.run(["nm", "-D", "--defined-only", str(lib.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(rtacx_\w+)\b", nm))
+    assert set(declared_functions()) <= exported
+
+
+def test_struct_layout_matches_header(lib):
+    fields = {"rtacx_sensor_1d": lib.Sensor1D, "rtacx_sensor_2d": lib.Sensor2D}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
+    for cname, py in fields.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = Path(d) / "probe.c", Path(d) / "probe"
+        src.write_text("\n".join(lines))
+        subprocess.run(["gcc", "-std=c99", str(src), "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            parts = line.split()
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, py in fields.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py)
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_version_string(lib):
+    so = lib.load()
+    assert b"sm_103a" in so.rtacx_version()
+
+
+def test_create_without_gpu_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    so = lib.load()
+    h = ctypes.c_void_p()
+    assert so.rtacx_create(ctypes.byref(h), 0) != lib.RTACX_OK
+    assert not h.value
