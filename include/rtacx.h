@@ -154,6 +154,29 @@ rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
 int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);
 
+/* Allocation-free ping. No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc -- sensor loops running under an
+ * allocation ban (no driver allocation locks in a real-time step) or
+ * processes whose device memory belongs to another allocator. It runs the
+ * same kernels as rtacx_reduce without a context: the sensor (a
+ * rtacx_sensor_1d* or rtacx_sensor_2d* matching sample_kind, host tables) is
+ * uploaded on every call into one fixed file-scope device array that also
+ * holds all scratch (about 8.3 MB, kept by every GPU that loads the library
+ * until exit). Runs on the current device and on `stream`; no cudaMalloc,
+ * cudaFree or other allocating call. Sizes above the limits below return
+ * RTACX_ERR_UNSUPPORTED. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress): make it before any stream capture.
+ * All calls share the array, so calls whose GPU work overlaps (other streams,
+ * other threads) race: serialise them. Status codes only (no context, so no
+ * rtacx_last_error message). */
+#define RTACX_NOALLOC_MAX_SAMPLES  (1u << 18)
+#define RTACX_NOALLOC_MAX_RANGES   4096u
+#define RTACX_NOALLOC_MAX_BEARINGS 1024u
+#define RTACX_NOALLOC_MAX_PULSE    4096u
+#define RTACX_NOALLOC_MAX_BEAM     8192u
+rtacx_status rtacx_reduce_noalloc(int sample_kind, const void* sensor, const void* samples,
+                                  uint64_t n, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

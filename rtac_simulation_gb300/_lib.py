@@ -70,6 +70,7 @@ SIGNATURES = {
     "rtacx_stream_status": (_I, [_P, _P]),
     "rtacx_set_tracing": (_I, [_P, _I]),
     "rtacx_stage_times": (_I, [_P, ctypes.POINTER(ctypes.c_float), _I]),
+    "rtacx_reduce_noalloc": (_I, [_I, _P, _P, _U64, _P, _P]),
 }
 
 STAGES = ("count", "colscan", "binscan", "scatter", "windows", "reduce")
