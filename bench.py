@@ -1,9 +1,14 @@
 #!/usr/bin/env python
 """Benchmark of the receiver-side ping reduction on GB300.
 
-A step is one ping: sort + bin + sparse PSF reduction of one synthetic sample
-buffer (rtacx_reduce). Default workload: the dense-directivity precision ping
-(2^24 samples, 512 bearings x 4096 ranges); --config selects another.
+A step is one ping of one synthetic sample buffer. Default workload: the
+dense-directivity precision ping (2^24 samples, 512 bearings x 4096 ranges,
+1.2 MHz carrier phase and spreading applied on the device); --config selects
+another. On 2D workloads with an echo model both forms are timed: the
+tensor-core precision form (rtacx_reduce_precision: bin first, BF16x3
+contraction over bearings, FP32 range filter) is the headline and the plain
+form (rtacx_reduce: sort + bin + per-sample sparse PSF gather) is reported
+beside it; otherwise the plain form is the headline.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--config NAME]
   python bench.py --impl reference ...   # the reference algorithm on the host cores
@@ -182,7 +187,12 @@ def cpu_model() -> str:
 def run_reference(args, world, rank):
     if rank != 0:
         return
+    from oracle import oracle
+    if args.config == "batched_mix":
+        return run_reference_batch(args)
     wk = workloads.CONFIGS[args.config]()
+    if wk.echo:   # the reference applies the echo epilogue in its ray generator, before this path
+        wk.samples = oracle.apply_echo(wk.samples, wk.sensor, wk.echo, mode=1)
     threads = os.cpu_count() or 1
     rows = 16 if wk.dims == 2 else max(64, wk.sensor["range_count"] // 8)
     for _ in range(args.warmup):
@@ -204,12 +214,93 @@ def run_reference(args, world, rank):
     }))
 
 
+def run_reference_batch(args):
+    """Reference algorithm on the host for the batched mix: every step
+    reduces 8 of the 64 pings completely (sort + bin + gather of all rows)."""
+    from oracle import oracle
+    pings = workloads.batched_mix()
+    sample = pings[::8]
+    threads = os.cpu_count() or 1
+    times = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for wk in sample:
+            oracle.reduce(wk.samples, wk.sensor, mode=1, threads=threads)
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    n = sum(wk.n for wk in sample)
+    value = n / t
+    print(json.dumps({
+        "impl": "reference", "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t, "pings_per_s": len(sample) / t,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "batched_mix (8 of 64 pings per step)", "form": "reference algorithm, host CPU"},
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
+                         "sample": f"8 of the 64 pings ({n} samples) fully reduced per step"},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
 def wk_desc(wk) -> str:
     s = wk.sensor
     if wk.dims == 1:
         return f"{wk.name}: {wk.n} samples, 1D {s['range_count']} ranges, {len(s['pulse'])}-tap pulse"
     return (f"{wk.name}: {wk.n} samples, {len(s['bearings'])} bearings x {s['range_count']} ranges, "
             f"{len(s['pulse'])}-tap pulse x {len(s['beam'])}-tap beam")
+
+
+def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, local, torch):
+    """Device time of `steps` pings (samples resident), per-stage event times
+    and the end-to-end time with pinned host buffers, for one form."""
+    from rtac_simulation_gb300 import _lib
+    call = ctx.reduce if form == "plain" else ctx.reduce_precision
+    stream = torch.cuda.current_stream()
+    for _ in range(max(warmup, 3)):
+        call(d_in, n, out, stream=stream)
+    ctx.stream_status(stream)
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        call(d_in, n, out, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ctx.stream_status(stream)
+    t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
+
+    ctx.set_tracing(True)
+    names = _lib.STAGES if form == "plain" else _lib.PRECISION_STAGES
+    stage = {k: 0.0 for k in names}
+    for _ in range(steps):
+        call(d_in, n, out, stream=stream)
+        for k, v in ctx.stage_times(precision=(form != "plain")).items():
+            stage[k] += v / steps
+    ctx.set_tracing(False)
+
+    call(d_in, n, out, stream=stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0.record(stream)
+    for _ in range(steps):
+        d_in.copy_(host_in, non_blocking=True)
+        call(d_in, n, out, stream=stream)
+        host_out.copy_(out, non_blocking=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ctx.stream_status(stream)
+    t_e2e = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
+    return dict(t_dev=t_dev, stage=stage, t_e2e=t_e2e, clocks=clk)
+
+
+def to_complex(t):
+    o = t.cpu().numpy()
+    return o[..., 0].astype(np.float64) + 1j * o[..., 1]
 
 
 def run_ours(args, world, rank, local):
@@ -225,120 +316,218 @@ def run_ours(args, world, rank, local):
         ctx.configure_1d(**wk.sensor)
     else:
         ctx.configure_2d(**wk.sensor)
+    if wk.echo:
+        ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    forms = ["plain"]
+    if wk.dims == 2 and wk.echo:
+        D, taps, center = workloads.precision_tables(wk.sensor)
+        ctx.configure_precision(D, taps, center)
+        forms = ["precision", "plain"]
     ctx.reserve(n)
     host_in = torch.from_numpy(wk.samples.reshape(-1)).pin_memory()
     d_in = host_in.to("cuda")
-    out = torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda")
-    host_out = torch.empty(out.shape, dtype=torch.float32).pin_memory()
+    outs = {f: torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda") for f in forms}
+    host_out = torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory()
+    res = {f: time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch)
+           for f in forms}
+    if rank != 0:
+        return
+    head = forms[0]
+    peaks = measured_peaks()
+    rec_in = 16 if wk.dims == 2 else 12
+
+    def form_line(f):
+        r = res[f]
+        return {"samples_per_s": world * n * args.steps / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / args.steps,
+                "e2e_samples_per_s": world * n * args.steps / r["t_e2e"],
+                "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()}}
+
+    line = {
+        "metric": "samples/s", "value": world * n * args.steps / res[head]["t_dev"], "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * res[head]["t_dev"] / args.steps,
+        "pings_per_s": world * args.steps / res[head]["t_dev"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wk_desc(wk),
+                   "form": ("precision: bin-first, BF16x3 tcgen05 complex contraction, FP32 range filter, FP64 carrier phase"
+                            if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
+                   "l2": "inputs larger than L2 (%.0f MB of samples)" % (n * rec_in / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "forms": {f: form_line(f) for f in forms},
+    }
+    if "precision" in forms:
+        line["precision_speedup_vs_plain"] = res["plain"]["t_dev"] / res["precision"]["t_dev"]
+
+    # Rooflines. Plain gather: 8 flop per useful (sample, cell) pair.
+    st = res["plain"]["stage"]
+    pairs = useful_pairs(wk)
+    gather_s = st["reduce"] / 1e3
+    fp32_peak = 152 * 128 * 2 * peaks["sm_max_mhz"] * 1e6 / 1e12
+    gather_tf = 8.0 * pairs / gather_s / 1e12 if gather_s > 0 else 0.0
+    roof_plain = {"bound": "fp32", "achieved": gather_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                  "frac": gather_tf / fp32_peak, "traffic": None,
+                  "kernel": "k_gather_2d" if wk.dims == 2 else "k_gather_1d",
+                  "peak_source": "nominal FP32 SIMT (152 SMs x 128 FMA x max clock); no measured FP32 peak",
+                  "algorithmic": "8 flop per useful (sample, output cell) pair, %.3e pairs" % pairs}
+    bin_bytes = n * (rec_in + 16)
+    bin_s = (st["count"] + st["colscan"] + st["binscan"] + st["scatter"] + st["windows"]) / 1e3
+    bin_gbs = bin_bytes / bin_s / 1e9 if bin_s > 0 else 0.0
+    line["roofline_sort_bin"] = {"bound": "hbm", "achieved": bin_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                 "frac": bin_gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
+                                 "algorithmic": f"{rec_in}+16 bytes per sample over count+colscan+binscan+scatter+windows"}
+    if "precision" in forms:
+        ps = res["precision"]["stage"]
+        nR, nB = wk.sensor["range_count"], len(wk.sensor["bearings"])
+        # Accumulate: one read of every sample (16 B) + the binned grid written once (8 B / cell).
+        acc_bytes = n * rec_in + nR * nB * 8
+        acc_gbs = acc_bytes / (ps["accumulate"] / 1e3) / 1e9
+        Mp, Np, Kp = -(-nR // 128) * 128, -(-2 * nB // 256) * 256, -(-6 * nB // 64) * 64
+        gemm_tf = 2.0 * Mp * Np * Kp / (ps["gemm"] / 1e3) / 1e12
+        roof_acc = {"bound": "hbm", "achieved": acc_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": acc_gbs / peaks["hbm_gbs"], "traffic": None, "kernel": "k_prec_accumulate",
+                    "peak_source": peaks["source"],
+                    "algorithmic": f"{rec_in} B per sample read + 8 B per binned cell"}
+        roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": gemm_tf / peaks["bf16_tflops"], "traffic": None, "kernel": "k_gemm_bf16_tn",
+                     "peak_source": peaks["source"],
+                     "algorithmic": f"2*M*N*K with M={Mp} N={Np} K={Kp} (three BF16 split products as one K)"}
+        dominant = max(("accumulate", "gemm", "filter"), key=lambda k: ps[k])
+        line["roofline"] = roof_gemm if dominant == "gemm" else roof_acc
+        line["roofline"]["dominant_stage"] = dominant
+        line["roofline_gemm"] = roof_gemm
+        line["roofline_accumulate"] = roof_acc
+        line["roofline_plain_gather"] = roof_plain
+    else:
+        line["roofline"] = roof_plain
+    r = res[head]
+    line["e2e"] = {"value": world * n * args.steps / r["t_e2e"], "unit": "samples/s",
+                   "h2d_bytes_per_step": n * rec_in, "d2h_bytes_per_step": int(np.prod(wk.out_shape)) * 8}
+    line["gpu_launches"] = (4 if head == "precision" else KERNELS_PER_PING) * args.steps
+    line["clocks"] = r["clocks"]
+
+    if world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle
+        threads = os.cpu_count() or 1
+        ref_wk = wk
+        if wk.echo:
+            ref_wk = workloads.Workload(wk.name, wk.dims, wk.sensor,
+                                        oracle.apply_echo(wk.samples, wk.sensor, wk.echo, mode=1), wk.meta)
+        rows = 32 if wk.dims == 2 else max(64, wk.sensor["range_count"] // 8)
+        t_cpu, rows = cpu_reference_step(ref_wk, rows, threads)
+        line["cpu_baseline"] = {
+            "value": n / t_cpu, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": (f"oracle FP32 reference arithmetic (per-sample PSF, float carrier phase as the reference): "
+                       f"sort+bin of all {n} samples plus the gather of {rows} of {wk.sensor['range_count']} rows, "
+                       f"extrapolated"),
+            "cpu": cpu_model()}
+        # Accuracy of this run's pings against their FP64 oracles on bands of rows.
+        nR = wk.sensor["range_count"]
+        exact = oracle.apply_echo(wk.samples, wk.sensor, wk.echo) if wk.echo else wk.samples
+        acc = {}
+        bands = [(0, 16), (nR // 3, nR // 3 + 16)] if wk.dims == 2 else [(0, nR)]
+        got_plain = to_complex(outs["plain"])
+        for b0, b1 in bands:
+            want = oracle.reduce(exact, wk.sensor, mode=0, rows=(b0, b1), threads=threads)
+            acc.setdefault("plain_rel_l2_vs_fp64", []).append(
+                float(np.linalg.norm(got_plain[b0:b1] - want) / np.linalg.norm(want)))
+            if "precision" in forms:
+                got_p = to_complex(outs["precision"])
+                want_b = oracle.reduce_binned(exact, wk.sensor, D, taps, center, rows=(b0, b1), threads=threads)
+                acc.setdefault("precision_rel_l2_vs_fp64_binned", []).append(
+                    float(np.linalg.norm(got_p[b0:b1] - want_b) / np.linalg.norm(want_b)))
+                acc.setdefault("binned_vs_per_sample_model_rel_l2", []).append(
+                    float(np.linalg.norm(want_b - want) / np.linalg.norm(want)))
+        acc["rows_checked"] = bands
+        line["accuracy"] = acc
+    print(json.dumps(line))
+
+
+def run_batch(args, world, rank, local):
+    """Batched mixed-sensor set: 64 heterogeneous pings in one CUDA graph
+    (rtacx_batch_*, autotuned); pings/s, per-ping device latency."""
+    import torch
+    from rtac_simulation_gb300 import _lib
+
+    dist = init_dist(world)
+    torch.cuda.set_device(local)
+    pings = workloads.batched_mix()
+    ctxs, host_in, d_in, outs, host_out = [], [], [], [], []
+    for wk in pings:
+        c = _lib.Context(local)
+        (c.configure_1d if wk.dims == 1 else c.configure_2d)(**wk.sensor)
+        c.reserve(wk.n)
+        ctxs.append(c)
+        h = torch.from_numpy(wk.samples.reshape(-1)).pin_memory()
+        host_in.append(h)
+        d_in.append(h.to("cuda"))
+        outs.append(torch.empty(wk.out_shape + (2,), device="cuda"))
+        host_out.append(torch.empty(wk.out_shape + (2,)).pin_memory())
+    batch = _lib.Batch(local)
+    batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, d_in, outs)], autotune=True)
     stream = torch.cuda.current_stream()
-
     for _ in range(max(args.warmup, 3)):
-        ctx.reduce(d_in, n, out, stream=stream)
-    ctx.stream_status(stream)
-
-    # Timed region: K pings, samples resident in HBM.
+        batch.run(stream)
+    torch.cuda.synchronize()
     clocks = ClockSampler(local)
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
-        ctx.reduce(d_in, n, out, stream=stream)
+        batch.run(stream)
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ctx.stream_status(stream)
     t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
-    if dist:
-        dist.barrier()
-
-    # Per-stage device times on the launching stream (separate pass).
-    ctx.set_tracing(True)
-    stage = {k: 0.0 for k in _lib.STAGES}
-    for _ in range(args.steps):
-        ctx.reduce(d_in, n, out, stream=stream)
-        for k, v in ctx.stage_times().items():
-            stage[k] += v / args.steps
-    ctx.set_tracing(False)
-
-    # End to end through the C ABI: pinned host samples in, ping out.
-    ctx.reduce(d_in, n, out, stream=stream)
+    # Per-ping device latency: each ping alone through rtacx_reduce.
+    lat = []
+    for wk, c, d, o in zip(pings, ctxs, d_in, outs):
+        c.reduce(d, wk.n, o, stream=stream)
+        ev0.record(stream)
+        c.reduce(d, wk.n, o, stream=stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        lat.append(ev0.elapsed_time(ev1))
+    batch.run(stream)
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
     ev0.record(stream)
     for _ in range(args.steps):
-        d_in.copy_(host_in, non_blocking=True)
-        ctx.reduce(d_in, n, out, stream=stream)
-        host_out.copy_(out, non_blocking=True)
+        for h, d in zip(host_in, d_in):
+            d.copy_(h, non_blocking=True)
+        batch.run(stream)
+        for o, h in zip(outs, host_out):
+            h.copy_(o, non_blocking=True)
     ev1.record(stream)
     torch.cuda.synchronize()
-    ctx.stream_status(stream)
     t_e2e = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
-
     if rank != 0:
         return
-    value = world * n * args.steps / t_dev
-    e2e_value = world * n * args.steps / t_e2e
+    total = sum(wk.n for wk in pings)
+    pairs = sum(useful_pairs(wk) for wk in pings)
     peaks = measured_peaks()
-
-    # Roofline of the dominant kernel (the PSF gather): algorithmic FP32 flops
-    # (8 per useful sample x output-cell pair) over its mean launch time.
-    pairs = useful_pairs(wk)
-    gather_s = stage["reduce"] / 1e3
     fp32_peak = 152 * 128 * 2 * peaks["sm_max_mhz"] * 1e6 / 1e12
-    achieved = 8.0 * pairs / gather_s / 1e12 if gather_s > 0 else 0.0
-    # Sort / bin: one read of every input record and one write of every sorted
-    # record (the survey's algorithmic bytes), over count + scatter + scans.
-    rec_in = 16 if wk.dims == 2 else 12
-    bin_bytes = n * (rec_in + 16)
-    bin_s = (stage["count"] + stage["colscan"] + stage["binscan"] + stage["scatter"] + stage["windows"]) / 1e3
-    bin_gbs = bin_bytes / bin_s / 1e9 if bin_s > 0 else 0.0
-
+    tf = 8.0 * pairs * args.steps / t_dev / 1e12
+    rec_bytes = sum(wk.n * (16 if wk.dims == 2 else 12) for wk in pings)
     line = {
-        "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": world,
+        "metric": "samples/s", "value": world * total * args.steps / t_dev, "unit": "samples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
-        "pings_per_s": world * args.steps / t_dev,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)",
-        "config": {"workload": wk_desc(wk), "form": "plain (FP32 SIMT sparse PSF gather)",
-                   "l2": "inputs larger than L2 (%.0f MB of samples)" % (n * rec_in / 1e6),
-                   "parallelism": f"replicas x{world}"},
-        "stage_ms": {k: round(v, 4) for k, v in stage.items()},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None, "kernel": "k_gather_2d" if wk.dims == 2 else "k_gather_1d",
-                     "peak_source": "nominal FP32 SIMT (152 SMs x 128 FMA x max clock); no measured FP32 peak",
-                     "algorithmic": "8 flop per useful (sample, output cell) pair, %.3e pairs" % pairs},
-        "roofline_bin": {"bound": "hbm", "achieved": bin_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": bin_gbs / peaks["hbm_gbs"], "traffic": None,
-                         "peak_source": peaks["source"],
-                         "algorithmic": f"{rec_in}+16 bytes per sample over count+colscan+binscan+scatter+windows"},
-        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": n * rec_in,
-                "d2h_bytes_per_step": int(np.prod(wk.out_shape)) * 8},
-        "gpu_launches": KERNELS_PER_PING * args.steps,
-        "clocks": clk,
+        "pings_per_s": world * len(pings) * args.steps / t_dev,
+        "per_ping_latency_ms": {"median": float(np.median(lat)), "p90": float(np.percentile(lat, 90)),
+                                "max": float(np.max(lat)), "batched_amortised": 1e3 * t_dev / args.steps / len(pings)},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"batched_mix: {len(pings)} pings, {total} samples (log-uniform 2^14..2^22), "
+                               "50% 512-bearing 2D, 25% 256-bearing 2D, 25% 1D 2048 ranges",
+                   "form": "plain, batched: stage-batched binning + persistent gather, one CUDA graph",
+                   "tuning": batch.tuning(), "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "fp32", "achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tf / fp32_peak,
+                     "traffic": None, "kernel": "whole batch (k_gather_batch dominant)",
+                     "peak_source": "nominal FP32 SIMT", "algorithmic": "8 flop per useful (sample, cell) pair, %.3e pairs" % pairs},
+        "e2e": {"value": world * total * args.steps / t_e2e, "unit": "samples/s",
+                "h2d_bytes_per_step": rec_bytes, "d2h_bytes_per_step": sum(int(np.prod(wk.out_shape)) * 8 for wk in pings)},
+        "gpu_launches": 7 * args.steps, "clocks": clk,
     }
-    if world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        rows = 32 if wk.dims == 2 else max(64, wk.sensor["range_count"] // 8)
-        t_cpu, rows = cpu_reference_step(wk, rows, threads)
-        line["cpu_baseline"] = {
-            "value": n / t_cpu, "unit": "samples/s", "cores": threads, "kind": "port",
-            "sample": (f"oracle FP32 reference arithmetic: sort+bin of all {n} samples plus the gather of "
-                       f"{rows} of {wk.sensor['range_count']} rows, extrapolated"),
-            "cpu": cpu_model()}
-        # Accuracy of this run's ping against the FP64 oracle on a band of rows.
-        from oracle import oracle
-        nR = wk.sensor["range_count"]
-        r0 = nR // 3
-        band = (r0, r0 + (8 if wk.dims == 2 else nR - r0))
-        ref = oracle.reduce(wk.samples, wk.sensor, mode=0, rows=band, threads=threads)
-        o = out.cpu().numpy()
-        got = (o[..., 0].astype(np.float64) + 1j * o[..., 1])[band[0]:band[1]]
-        line["accuracy"] = {"rel_l2_vs_fp64": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
-                            "rows_checked": list(band)}
     print(json.dumps(line))
 
 
@@ -347,6 +536,9 @@ def main():
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.config == "batched_mix":
+        run_batch(args, world, rank, local)
         return
     run_ours(args, world, rank, local)
 

@@ -139,6 +139,78 @@ rtacx_status rtacx_bin(rtacx_ctx* ctx, const void* samples, uint64_t n, int samp
 rtacx_status rtacx_reduce(rtacx_ctx* ctx, const void* samples, uint64_t n,
                           float* out, void* stream);
 
+/* Echo-sample model: the per-sample epilogue of the reference's ray
+ * generator, value *= exp(i 4 pi f travel / c) / travel^2
+ * (src/RayCaster.cu:37-39, 69-71), applied on the device to every sample
+ * before the reduction (both forms). The reference rounds the carrier phase
+ * to float (an error of up to 0.06 rad at 1.2 MHz and 120 m); here it is
+ * reduced modulo one cycle in FP64. NULL or flags = 0 turns it off (the
+ * default). Uses the configured sound_celerity; call after rtacx_configure_*. */
+#define RTACX_ECHO_PHASE     1u   /* value *= exp(i 4 pi f travel / c) */
+#define RTACX_ECHO_SPREADING 2u   /* value /= travel^2                */
+typedef struct {
+    double carrier_hz;
+    uint32_t flags;
+} rtacx_echo_model;
+rtacx_status rtacx_set_echo_model(rtacx_ctx* ctx, const rtacx_echo_model* model);
+
+/* Precision (tensor-core) form of a configured 2D sensor. Bins first, then
+ * contracts over bearings on the tensor cores, then filters in range:
+ *   G[j][k]  = sum over samples s in range bin j (Binner::Key) of v_s, split
+ *              linearly between the two table bearings k, k+1 around theta_s
+ *              (clamped to the first / last bearing outside the table);
+ *   G'[r][k] = sum_t taps[t] G[r + t - tap_center][k] over the bins j of
+ *              row r's reference window (do_make_bins rule, range bins whose
+ *              G row received a sample count as non-empty);
+ *   out      = G' x D, D the dense complex [bearing_count][bearing_count]
+ *              directivity (D[k][b]: response of beam b to bearing k).
+ * The contraction runs in BF16 with three split products (hi*hi + hi*lo +
+ * lo*hi) and FP32 accumulation on tcgen05 tensor cores; the rest is FP32.
+ * This is a binned model: samples sit on the table bearings and at their
+ * range-bin offsets, unlike the per-sample PSF of rtacx_reduce. Bearings
+ * must be strictly increasing. NULL tables are derived from the 2D sensor:
+ * D[k][b] = beam(theta_k - theta_b) and taps[t] = pulse((t - tap_center) *
+ * resolution) with the same texture-equivalent lerp as rtacx_reduce. */
+typedef struct {
+    const float* directivity;   /* host complex [bearing_count][bearing_count] or NULL */
+    const float* range_taps;    /* host complex [tap_count] or NULL                    */
+    uint32_t tap_count;
+    uint32_t tap_center;
+    uint32_t flags;             /* reserved, 0 */
+} rtacx_precision_desc;
+rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_desc* desc);
+rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n,
+                                    float* out, void* stream);
+
+/* Batched plain form: many pings from heterogeneous sensors (each bound to
+ * its own configured 1D or 2D context, whose scratch it uses) in one CUDA
+ * graph: one launch per binning stage covering every ping, then one
+ * persistent gather kernel that takes output tiles of all pings from an
+ * atomic work counter, heaviest first. The reference has no batching
+ * (one SensorInstance::compute_output per ping, each kernel followed by a
+ * device sync). rtacx_batch_plan binds the pings (samples, counts, outputs
+ * are baked into the graph: re-plan when any of them changes) and, with
+ * RTACX_BATCH_AUTOTUNE, times every candidate gather tile shape x samples
+ * per binning CTA on this batch and keeps the fastest. rtacx_batch_run
+ * replays the graph on `stream`. Results equal rtacx_reduce's per ping. */
+typedef struct rtacx_batch rtacx_batch;
+typedef struct {
+    rtacx_ctx* ctx;          /* configured context, one per ping          */
+    const void* samples;     /* device samples matching the context       */
+    uint64_t n;              /* sample count, >= 1                        */
+    float* out;              /* device ping (complex64)                   */
+} rtacx_ping_desc;
+#define RTACX_BATCH_AUTOTUNE 1u
+rtacx_status rtacx_batch_create(rtacx_batch** batch, int device);
+void rtacx_batch_destroy(rtacx_batch* batch);
+const char* rtacx_batch_last_error(const rtacx_batch* batch);
+rtacx_status rtacx_batch_plan(rtacx_batch* batch, const rtacx_ping_desc* pings, uint32_t count, uint32_t flags);
+rtacx_status rtacx_batch_run(rtacx_batch* batch, void* stream);
+/* The plan's choice: gather tile rows x bearings, samples per binning CTA,
+ * and the autotuned batch time in ms (0 without autotuning). */
+rtacx_status rtacx_batch_tuning(const rtacx_batch* batch, uint32_t* tile_rows, uint32_t* tile_bearings,
+                                uint32_t* samples_per_cta, float* tuned_ms);
+
 /* Wait for `stream` and report the device error word of this context
  * (RTACX_ERR_DEVICE if a kernel flagged an error since the last check).
  * Clears the word. */
@@ -147,12 +219,20 @@ rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
 /* Stage tracing (no counterpart in the reference, which has no timers):
  * when enabled, rtacx_reduce records a CUDA event pair around each stage on
  * the caller's stream. rtacx_stage_times waits for the last traced call and
- * writes up to `max` stage durations in milliseconds, in the order
- * count, column scan, bin scan, scatter, windows, reduce; returns the number
- * of stages written (negative on error). */
+ * writes up to `max` stage durations in milliseconds (0 for stages the last
+ * call did not run): for rtacx_reduce count, column scan, bin scan, scatter,
+ * windows, reduce; for rtacx_reduce_precision accumulate, windows, range
+ * filter, tensor-core GEMM, copy-out. Returns the number of stages written
+ * (negative on error). */
 #define RTACX_STAGE_COUNT 6
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
 int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);
+
+/* Diagnostic: synchronous C = A * B^T on the tensor cores (the GEMM of the
+ * precision form). A [M][K], B [N][K] bf16, C [M][N] fp32, row-major,
+ * device pointers 16-byte aligned; M % 128 == 0, N % 256 == 0, K % 64 == 0.
+ * No counterpart in the reference. */
+rtacx_status rtacx_gemm_bf16_tn(const void* A, const void* B, float* C, int M, int N, int K, void* stream);
 
 /* Allocation-free ping. No counterpart in the reference: it exists for
  * callers that cannot call cudaMalloc -- sensor loops running under an

@@ -56,6 +56,11 @@ def load() -> ctypes.CDLL:
     lib.rtacx_oracle_reduce.argtypes = [_U32, _P, _U64, _F, _F, _U32, _F, _F, _P, _U32, _F, _P, _U32,
                                         _P, _U32, _I, _U32, _U32, _I, _P]
     lib.rtacx_oracle_reduce.restype = None
+    lib.rtacx_oracle_apply_echo.argtypes = [_P, _U64, _U32, ctypes.c_double, _F, _U32, _I]
+    lib.rtacx_oracle_apply_echo.restype = None
+    lib.rtacx_oracle_reduce_binned.argtypes = [_P, _U64, _F, _F, _U32, _F, _P, _U32, _P, _P, _U32, _U32,
+                                               _U32, _U32, _I, _P]
+    lib.rtacx_oracle_reduce_binned.restype = None
     _lib = lib
     return lib
 
@@ -146,3 +151,34 @@ def reduce(samples: np.ndarray, sensor: dict, mode: int = 0, rows=None, threads:
                             bscale, beam.ctypes.data, beam.size, bearings.ctypes.data, nB,
                             mode, r0, r1, threads, out.ctypes.data)
     return out[:, 0] if dims == 1 else out
+
+
+def apply_echo(samples: np.ndarray, sensor: dict, echo: dict | None, mode: int = 0) -> np.ndarray:
+    """Copy of `samples` with the echo pre-step applied (mode 0 exact FP64,
+    mode 1 the reference's float arithmetic)."""
+    out = np.array(samples, dtype=np.float32, copy=True, order="C")
+    if not echo or not echo.get("flags"):
+        return out
+    n, stride = out.shape
+    load().rtacx_oracle_apply_echo(out.ctypes.data, n, stride, float(echo.get("carrier_hz", 0.0)),
+                                   sensor["sound_celerity"], int(echo["flags"]), mode)
+    return out
+
+
+def reduce_binned(samples: np.ndarray, sensor: dict, directivity: np.ndarray, taps: np.ndarray,
+                  tap_center: int, rows=None, threads: int = 0) -> np.ndarray:
+    """FP64 oracle of the binned precision model (complex128 [rows][nB])."""
+    lib = load()
+    s = np.ascontiguousarray(samples, dtype=np.float32)
+    n = s.shape[0]
+    nR = sensor["range_count"]
+    bear = np.ascontiguousarray(sensor["bearings"], dtype=np.float32)
+    D = np.ascontiguousarray(directivity, dtype=np.complex64)
+    t = np.ascontiguousarray(taps, dtype=np.complex64)
+    r0, r1 = rows if rows is not None else (0, nR)
+    out = np.zeros((r1 - r0, bear.size), dtype=np.complex128)
+    lib.rtacx_oracle_reduce_binned(s.ctypes.data, n, sensor["range_min"], sensor["range_max"], nR,
+                                   sensor["margin"], bear.ctypes.data, bear.size, D.ctypes.data,
+                                   t.ctypes.data, t.size, tap_center, r0, r1,
+                                   threads or (os.cpu_count() or 1), out.ctypes.data)
+    return out

@@ -404,4 +404,104 @@ void rtacx_oracle_reduce(uint32_t dims, const float* samples, uint64_t n,
     });
 }
 
+// Echo-sample epilogue of the ray generator (src/RayCaster.cu:37-39, 69-71):
+// value *= exp(i * 4 pi f d / c) / d^2, applied in place to AoS samples
+// (`stride` floats per sample, travel at offset 2). mode 0: exact (the phase
+// reduced in double, products in double, rounded to float once); mode 1: the
+// reference's own arithmetic (float phase = (float)((4 pi f / c) * d), float
+// cos/sin, float product and division). flags: 1 phase, 2 spreading.
+void rtacx_oracle_apply_echo(float* samples, uint64_t n, uint32_t stride, double carrier_hz, float c,
+                             uint32_t flags, int mode)
+{
+    const double pi = 3.14159265358979323846;
+    for(uint64_t i = 0; i < n; i++) {
+        float* s = samples + i * stride;
+        const float d = s[2];
+        if(mode == 0) {
+            std::complex<double> v(s[0], s[1]);
+            if(flags & 1u) {
+                const double cyc = (double)d * (2.0 * carrier_hz / (double)c);
+                const double ph = 2.0 * pi * (cyc - std::nearbyint(cyc));
+                v *= std::complex<double>(std::cos(ph), std::sin(ph));
+            }
+            if(flags & 2u) v /= (double)d * (double)d;
+            s[0] = (float)v.real(); s[1] = (float)v.imag();
+        }
+        else {
+            std::complex<float> v(s[0], s[1]);
+            if(flags & 1u) {
+                const float ph = (float)((4.0 * pi * (double)(float)carrier_hz / (double)c) * (double)d);
+                v *= std::complex<float>(std::cos(ph), std::sin(ph));
+            }
+            if(flags & 2u) { const float dd = d * d; v = std::complex<float>(v.real() / dd, v.imag() / dd); }
+            s[0] = v.real(); s[1] = v.imag();
+        }
+    }
+}
+
+// FP64 oracle of the binned (precision) model -- see rtacx_reduce_precision
+// in include/rtacx.h: G[j][k] by range key and linear bearing split, window
+// rule on non-empty bins, range taps within each row's window, then the dense
+// complex directivity. Rows [row_begin, row_end) into out (complex double).
+void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, float rmax, uint32_t nR,
+                                float margin, const float* bearings, uint32_t nB, const float* D,
+                                const float* taps, uint32_t ntaps, uint32_t center,
+                                uint32_t row_begin, uint32_t row_end, int nthreads, void* out)
+{
+    using cd = std::complex<double>;
+    KeyParams key = make_key(nR, rmin, rmax, margin);
+    std::vector<cd> G((size_t)nR * nB, cd(0.0, 0.0));
+    std::vector<uint8_t> nonempty(nR, 0);
+    for(uint64_t i = 0; i < n; i++) {
+        const float* s = samples + i * 4;
+        const uint32_t j = range_key(key, s[2]);
+        if(j == kOutOfRange) continue;
+        nonempty[j] = 1;
+        const cd v(s[0], s[1]);
+        cd* row = G.data() + (size_t)j * nB;
+        if(nB == 1) { row[0] += v; continue; }
+        const float th = s[3];
+        int lo = 0, hi = (int)nB - 2;
+        while(lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if(bearings[mid] <= th) lo = mid; else hi = mid - 1;
+        }
+        double w = ((double)th - (double)bearings[lo]) / ((double)bearings[lo + 1] - (double)bearings[lo]);
+        w = std::fmin(std::fmax(w, 0.0), 1.0);
+        row[lo] += (1.0 - w) * v;
+        row[lo + 1] += w * v;
+    }
+    const int ov = (nR > 1) ? bin_overlap(rmin, rmax, nR, margin) : 0;
+    const cd* tp = nullptr;
+    std::vector<cd> tv(ntaps);
+    for(uint32_t t = 0; t < ntaps; t++) tv[t] = cd(taps[2 * t], taps[2 * t + 1]);
+    tp = tv.data();
+    std::vector<cd> Dd((size_t)nB * nB);
+    for(size_t q = 0; q < Dd.size(); q++) Dd[q] = cd(D[2 * q], D[2 * q + 1]);
+    row_end = std::min(row_end, nR);
+    parallel_rows(row_begin, row_end, nthreads, [&](uint32_t r) {
+        cd* o = static_cast<cd*>(out) + (size_t)(r - row_begin) * nB;
+        for(uint32_t b = 0; b < nB; b++) o[b] = cd(0.0, 0.0);
+        const long long lo = std::max(0ll, (long long)r - ov), hi = std::min((long long)nR - 1, (long long)r + ov);
+        long long a = lo;
+        while(a <= hi && !nonempty[a]) a++;
+        if(a >= hi) return;
+        long long z = hi;
+        while(z > a && !nonempty[z]) z--;
+        if(a >= z) return;
+        std::vector<cd> g(nB, cd(0.0, 0.0));
+        for(uint32_t t = 0; t < ntaps; t++) {
+            const long long jj = (long long)r + t - (long long)center;
+            if(jj < a || jj > z) continue;
+            const cd* row = G.data() + (size_t)jj * nB;
+            for(uint32_t k = 0; k < nB; k++) g[k] += tp[t] * row[k];
+        }
+        for(uint32_t k = 0; k < nB; k++) {
+            if(g[k] == cd(0.0, 0.0)) continue;
+            const cd* dk = Dd.data() + (size_t)k * nB;
+            for(uint32_t b = 0; b < nB; b++) o[b] += g[k] * dk[b];
+        }
+    });
+}
+
 } // extern "C"

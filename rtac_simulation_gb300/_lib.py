@@ -71,7 +71,37 @@ SIGNATURES = {
     "rtacx_set_tracing": (_I, [_P, _I]),
     "rtacx_stage_times": (_I, [_P, ctypes.POINTER(ctypes.c_float), _I]),
     "rtacx_reduce_noalloc": (_I, [_I, _P, _P, _U64, _P, _P]),
+    "rtacx_gemm_bf16_tn": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "rtacx_set_echo_model": (_I, [_P, _P]),
+    "rtacx_configure_precision": (_I, [_P, _P]),
+    "rtacx_reduce_precision": (_I, [_P, _P, _U64, _P, _P]),
+    "rtacx_batch_create": (_I, [ctypes.POINTER(_P), _I]),
+    "rtacx_batch_destroy": (None, [_P]),
+    "rtacx_batch_last_error": (ctypes.c_char_p, [_P]),
+    "rtacx_batch_plan": (_I, [_P, _P, _U32, _U32]),
+    "rtacx_batch_run": (_I, [_P, _P]),
+    "rtacx_batch_tuning": (_I, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_U32), ctypes.POINTER(_U32),
+                                ctypes.POINTER(ctypes.c_float)]),
 }
+
+RTACX_BATCH_AUTOTUNE = 1
+
+
+class PingDesc(ctypes.Structure):
+    _fields_ = [("ctx", _P), ("samples", _P), ("n", _U64), ("out", _P)]
+
+RTACX_ECHO_PHASE = 1
+RTACX_ECHO_SPREADING = 2
+PRECISION_STAGES = ("accumulate", "windows", "filter", "gemm", "copy")
+
+
+class EchoModel(ctypes.Structure):
+    _fields_ = [("carrier_hz", ctypes.c_double), ("flags", _U32)]
+
+
+class PrecisionDesc(ctypes.Structure):
+    _fields_ = [("directivity", _P), ("range_taps", _P), ("tap_count", _U32), ("tap_center", _U32),
+                ("flags", _U32)]
 
 STAGES = ("count", "colscan", "binscan", "scatter", "windows", "reduce")
 
@@ -190,16 +220,76 @@ class Context:
     def reduce(self, samples, n: int, out, stream=None) -> None:
         self._check(self._lib.rtacx_reduce(self._h, _ptr(samples), n, _ptr(out), _stream(stream)))
 
+    def set_echo_model(self, carrier_hz: float = 0.0, flags: int = 0) -> None:
+        m = EchoModel(carrier_hz, flags)
+        self._check(self._lib.rtacx_set_echo_model(self._h, ctypes.byref(m)))
+
+    def configure_precision(self, directivity=None, range_taps=None, tap_center: int = 0) -> None:
+        d = None if directivity is None else np.ascontiguousarray(np.asarray(directivity, dtype=np.complex64))
+        t = None if range_taps is None else np.ascontiguousarray(np.asarray(range_taps, dtype=np.complex64))
+        desc = PrecisionDesc(None if d is None else d.ctypes.data, None if t is None else t.ctypes.data,
+                             0 if t is None else t.size, tap_center, 0)
+        self._check(self._lib.rtacx_configure_precision(self._h, ctypes.byref(desc)))
+
+    def reduce_precision(self, samples, n: int, out, stream=None) -> None:
+        self._check(self._lib.rtacx_reduce_precision(self._h, _ptr(samples), n, _ptr(out), _stream(stream)))
+
     def set_tracing(self, enable: bool) -> None:
         self._check(self._lib.rtacx_set_tracing(self._h, 1 if enable else 0))
 
-    def stage_times(self) -> dict:
-        """Per-stage device milliseconds of the last traced rtacx_reduce."""
+    def stage_times(self, precision: bool = False) -> dict:
+        """Per-stage device milliseconds of the last traced call."""
+        names = PRECISION_STAGES if precision else STAGES
         buf = (ctypes.c_float * len(STAGES))()
         k = self._lib.rtacx_stage_times(self._h, buf, len(STAGES))
         if k < 0:
             raise RtacxError(-k, self.last_error())
-        return {STAGES[i]: float(buf[i]) for i in range(k)}
+        return {names[i]: float(buf[i]) for i in range(min(k, len(names)))}
 
     def stream_status(self, stream=None) -> None:
         self._check(self._lib.rtacx_stream_status(self._h, _stream(stream)))
+
+
+class Batch:
+    """Batched plain form (rtacx_batch_*): many pings, one CUDA graph."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = _P()
+        st = self._lib.rtacx_batch_create(ctypes.byref(h), device)
+        if st != RTACX_OK:
+            raise RtacxError(st, "rtacx_batch_create failed")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.rtacx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        if st != RTACX_OK:
+            msg = self._lib.rtacx_batch_last_error(self._h)
+            raise RtacxError(st, msg.decode() if msg else "")
+
+    def plan(self, pings, autotune: bool = True) -> None:
+        """pings: sequence of (Context, samples tensor, n, out tensor)."""
+        arr = (PingDesc * len(pings))()
+        for i, (ctx, smp, n, out) in enumerate(pings):
+            arr[i] = PingDesc(ctx.handle, _ptr(smp), n, _ptr(out))
+        self._check(self._lib.rtacx_batch_plan(self._h, arr, len(pings), RTACX_BATCH_AUTOTUNE if autotune else 0))
+
+    def run(self, stream=None) -> None:
+        self._check(self._lib.rtacx_batch_run(self._h, _stream(stream)))
+
+    def tuning(self) -> dict:
+        r, b, p = _U32(), _U32(), _U32()
+        ms = ctypes.c_float()
+        self._check(self._lib.rtacx_batch_tuning(self._h, ctypes.byref(r), ctypes.byref(b), ctypes.byref(p),
+                                                 ctypes.byref(ms)))
+        return {"tile_rows": r.value, "tile_bearings": b.value, "samples_per_cta": p.value, "tuned_ms": ms.value}

@@ -10,6 +10,7 @@ namespace rtacx {
 
 void configure_hist_launch(Context& ctx);
 size_t gather_smem_bytes(uint32_t range_tile, uint32_t bearing_tile, uint32_t H, uint32_t W);
+rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d);
 
 namespace {
 
@@ -22,10 +23,19 @@ void free_dev(T*& p)
     p = nullptr;
 }
 
+// Copy the context's echo model into the binning parameters.
+void sync_echo(Context& c)
+{
+    c.bin.echo_flags = c.echo_flags;
+    c.bin.echo_cycles = (c.c > 0.0f) ? 2.0 * c.echo_hz / (double)c.c : 0.0;
+}
+
 void free_config(Context& c)
 {
+    free_precision(c);
     free_dev(c.d_pulse); free_dev(c.d_beam); free_dev(c.d_bearings); free_dev(c.d_ranges);
-    free_dev(c.d_support); free_dev(c.d_bb_tiles); free_dev(c.d_offsets); free_dev(c.d_totals);
+    free_dev(c.d_support); free_dev(c.d_bb_tiles64); free_dev(c.d_bb_tiles128); c.d_bb_tiles = nullptr;
+    free_dev(c.d_offsets); free_dev(c.d_totals);
     free_dev(c.d_win); free_dev(c.d_hist);
     c.hist_cols = 0;
     c.configured = false;
@@ -194,6 +204,7 @@ rtacx_status rtacx_configure_1d(rtacx_ctx* ctx, const rtacx_sensor_1d* s)
     c.red.dims = 1; c.red.nB = 1;
     c.red.beam_axis = AxisLerp{0.f, 0.f, 0.f, 0};
     c.bin = BinParams{c.key, 1u, 0.0f, 0.0f, c.nR, 3u, 0};
+    sync_echo(c);
     if(c.nR > kMaxSmemBins) { c.error = "range_count above the shared-memory histogram limit"; return RTACX_ERR_UNSUPPORTED; }
     std::vector<float> one(1, 0.0f);
     if(!upload(c, c.d_beam, one.data(), 1) || !upload(c, c.d_bearings, one.data(), 1) || !allocate_bins(c))
@@ -262,24 +273,32 @@ rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* s)
         return RTACX_ERR_UNSUPPORTED;
     }
     c.bin = BinParams{c.key, nBB, bb_scale, bb_offset, c.nR * nBB, 4u, 0};
+    sync_echo(c);
 
-    const uint32_t tiles = (c.nB + c.bearing_tile - 1) / c.bearing_tile;
-    std::vector<int2> bbt(tiles);
-    for(uint32_t t = 0; t < tiles; t++) {
-        if(nBB == 1) { bbt[t] = make_int2(0, 0); continue; }
-        const uint32_t b0 = t * c.bearing_tile, b1 = std::min(c.nB, b0 + c.bearing_tile);
-        float tmin = c.bearings[b0], tmax = c.bearings[b0];
-        for(uint32_t b = b0; b < b1; b++) { tmin = std::min(tmin, c.bearings[b]); tmax = std::max(tmax, c.bearings[b]); }
-        const float qlo = (float)((double)tmin - sb), qhi = (float)((double)tmax + sb);
-        bbt[t] = make_int2((int)host_bearing_bin(bb_scale, bb_offset, nBB, qlo),
-                           (int)host_bearing_bin(bb_scale, bb_offset, nBB, qhi));
-    }
+    // Bearing-bin range of every bearing tile, for 64- and 128-bearing tiles.
+    auto tile_ranges = [&](uint32_t width) {
+        const uint32_t tiles = (c.nB + width - 1) / width;
+        std::vector<int2> bbt(tiles);
+        for(uint32_t t = 0; t < tiles; t++) {
+            if(nBB == 1) { bbt[t] = make_int2(0, 0); continue; }
+            const uint32_t b0 = t * width, b1 = std::min(c.nB, b0 + width);
+            float tmin = c.bearings[b0], tmax = c.bearings[b0];
+            for(uint32_t b = b0; b < b1; b++) { tmin = std::min(tmin, c.bearings[b]); tmax = std::max(tmax, c.bearings[b]); }
+            const float qlo = (float)((double)tmin - sb), qhi = (float)((double)tmax + sb);
+            bbt[t] = make_int2((int)host_bearing_bin(bb_scale, bb_offset, nBB, qlo),
+                               (int)host_bearing_bin(bb_scale, bb_offset, nBB, qhi));
+        }
+        return bbt;
+    };
+    const std::vector<int2> bbt64 = tile_ranges(64), bbt128 = tile_ranges(128);
     std::vector<float> bpad(c.W + 2, 0.0f);
     std::memcpy(bpad.data() + 1, s->beam, sizeof(float) * c.W);
     if(!upload(c, c.d_beam, bpad.data(), bpad.size()) ||
        !upload(c, c.d_bearings, c.bearings.data(), c.bearings.size()) ||
-       !upload(c, c.d_bb_tiles, bbt.data(), bbt.size()) || !allocate_bins(c))
+       !upload(c, c.d_bb_tiles64, bbt64.data(), bbt64.size()) ||
+       !upload(c, c.d_bb_tiles128, bbt128.data(), bbt128.size()) || !allocate_bins(c))
         return RTACX_ERR_OUT_OF_MEMORY;
+    c.d_bb_tiles = (c.bearing_tile == 64) ? c.d_bb_tiles64 : c.d_bb_tiles128;
     c.configured = true;
     return RTACX_OK;
 }
@@ -336,6 +355,48 @@ rtacx_status rtacx_reduce(rtacx_ctx* ctx, const void* samples, uint64_t n, float
     st = run_reduce(c, out, s);
     c.mark(5, true, s);
     return st;
+}
+
+rtacx_status rtacx_set_echo_model(rtacx_ctx* ctx, const rtacx_echo_model* m)
+{
+    if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;
+    Context& c = ctx->impl;
+    if(!m || m->flags == 0) { c.echo_flags = 0; c.echo_hz = 0.0; sync_echo(c); return RTACX_OK; }
+    if(m->flags & ~(RTACX_ECHO_PHASE | RTACX_ECHO_SPREADING)) { c.error = "unknown echo flags"; return RTACX_ERR_INVALID_ARGUMENT; }
+    if((m->flags & RTACX_ECHO_PHASE) && !(std::isfinite(m->carrier_hz) && m->carrier_hz > 0.0)) {
+        c.error = "carrier_hz must be positive and finite";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
+    c.echo_flags = m->flags;
+    c.echo_hz = (m->flags & RTACX_ECHO_PHASE) ? m->carrier_hz : 0.0;
+    sync_echo(c);
+    return RTACX_OK;
+}
+
+rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_desc* desc)
+{
+    if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;
+    Context& c = ctx->impl;
+    if(set_device(c) != RTACX_OK) return RTACX_ERR_CUDA;
+    return configure_precision(c, desc);
+}
+
+rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n, float* out, void* stream)
+{
+    if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;
+    Context& c = ctx->impl;
+    if(!c.prec_configured) { c.error = "call rtacx_configure_precision first"; return RTACX_ERR_NOT_CONFIGURED; }
+    if(!out) { c.error = "null output buffer"; return RTACX_ERR_INVALID_ARGUMENT; }
+    if(n && !samples) { c.error = "null sample buffer"; return RTACX_ERR_INVALID_ARGUMENT; }
+    if(n >= (1ull << 32)) { c.error = "at most 2^32 - 1 samples per ping"; return RTACX_ERR_UNSUPPORTED; }
+    if(reinterpret_cast<uintptr_t>(samples) % 4 != 0 || reinterpret_cast<uintptr_t>(out) % 16 != 0) {
+        c.error = "samples must be 4-byte and the ping 16-byte aligned";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
+    if(set_device(c) != RTACX_OK) return RTACX_ERR_CUDA;
+    c.bin.vec4 = reinterpret_cast<uintptr_t>(samples) % 16 == 0 ? 1 : 0;
+    for(bool& t : c.traced) t = false;
+    return run_precision(c, samples, n, out, static_cast<cudaStream_t>(stream));
 }
 
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable)

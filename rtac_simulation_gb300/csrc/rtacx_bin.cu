@@ -9,8 +9,8 @@
 // comparison sort.
 //
 // Passes (persistent CTAs, each owning one contiguous chunk of the input):
-//   k_count      key of every sample, per-CTA histogram in shared memory
-//                (warp-aggregated atomics for hot bins), written as one row
+//   k_count      key of every sample, per-CTA histogram in shared memory,
+//                written as one row
 //                of the [cta][bin] matrix; out-of-range counts.
 //   k_colscan    per bin, exclusive prefix over CTAs (in place) + bin total.
 //   k_binscan    exclusive scan of bin totals -> bin offsets.
@@ -32,13 +32,15 @@ constexpr int kScanThreads = 1024;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
-// One warp-uniform pass over a CTA's chunk. f(valid, record, key, side) is
-// called by every lane of every warp the same number of times.
+// One warp-uniform pass over chunk `c` of `nc` equal chunks of the input.
+// f(valid, record, key, side) is called by every lane of every warp the same
+// number of times.
 template <typename F>
-__device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, const BinParams& p, F&& f)
+__device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, const BinParams& p,
+                                          uint32_t c, uint32_t nc, F&& f)
 {
-    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const uint64_t begin = (uint64_t)blockIdx.x * chunk;
+    const uint64_t chunk = (n + nc - 1) / nc;
+    const uint64_t begin = (uint64_t)c * chunk;
     const uint64_t end = min(begin + chunk, n);
     for(uint64_t i0 = begin + (threadIdx.x & ~31u); i0 < end; i0 += blockDim.x) {
         const uint64_t i = i0 + lane_id();
@@ -54,21 +56,20 @@ __device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, cons
     }
 }
 
-__global__ void k_count(const float* __restrict__ samples, uint64_t n, BinParams p,
-                        uint32_t* __restrict__ hist, unsigned long long* __restrict__ oor)
+} // namespace
+
+// Count pass of chunk c of nc (shared-memory histogram sh of p.nBins words).
+__device__ void count_chunk(const float* __restrict__ samples, uint64_t n, const BinParams& p, uint32_t c,
+                            uint32_t nc, uint32_t* __restrict__ hist, unsigned long long* __restrict__ oor,
+                            uint32_t* sh, unsigned long long* s_oor)
 {
-    extern __shared__ uint32_t sh[];
-    __shared__ unsigned long long s_oor[2];
     for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = 0u;
     if(threadIdx.x < 2) s_oor[threadIdx.x] = 0ull;
     __syncthreads();
 
     uint32_t low = 0, high = 0;
-    for_chunk(samples, n, p, [&](bool valid, const float4&, uint32_t key, int side) {
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        if(valid && key != kOutOfRange) {
-            if(lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&sh[key], (uint32_t)__popc(peers));
-        }
+    for_chunk(samples, n, p, c, nc, [&](bool valid, const float4&, uint32_t key, int side) {
+        if(valid && key != kOutOfRange) atomicAdd(&sh[key], 1u);
         else if(valid) {
             if(side < 0) low++; else high++;
         }
@@ -86,15 +87,26 @@ __global__ void k_count(const float* __restrict__ samples, uint64_t n, BinParams
         if(s_oor[0]) atomicAdd(&oor[0], s_oor[0]);
         if(s_oor[1]) atomicAdd(&oor[1], s_oor[1]);
     }
-    uint32_t* row = hist + (size_t)blockIdx.x * p.nBins;
+    uint32_t* row = hist + (size_t)c * p.nBins;
     for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) row[b] = sh[b];
 }
 
-// Per bin: hist[c][b] <- sum_{c' < c} hist[c'][b]; totals[b] <- sum_c hist[c][b].
-__global__ void k_colscan(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t nBins,
-                          uint32_t* __restrict__ totals)
+namespace {
+
+__global__ void k_count(const float* __restrict__ samples, uint64_t n, BinParams p,
+                        uint32_t* __restrict__ hist, unsigned long long* __restrict__ oor)
 {
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ uint32_t sh[];
+    __shared__ unsigned long long s_oor[2];
+    count_chunk(samples, n, p, blockIdx.x, gridDim.x, hist, oor, sh, s_oor);
+}
+
+} // namespace
+
+// Per bin: hist[c][b] <- sum_{c' < c} hist[c'][b]; totals[b] <- sum_c hist[c][b].
+__device__ void colscan_bin(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t nBins,
+                            uint32_t* __restrict__ totals, uint32_t b)
+{
     if(b >= nBins) return;
     uint32_t run = 0;
     uint32_t c = 0;
@@ -111,6 +123,14 @@ __global__ void k_colscan(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t n
         run += v;
     }
     totals[b] = run;
+}
+
+namespace {
+
+__global__ void k_colscan(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t nBins,
+                          uint32_t* __restrict__ totals)
+{
+    colscan_bin(hist, ctas, nBins, totals, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Exclusive block scan of one value per thread (blockDim.x == kScanThreads).
@@ -140,8 +160,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
     return before + x - v;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __restrict__ totals, uint32_t nBins,
-                                                           uint32_t* __restrict__ offsets)
+} // namespace
+
+// Exclusive scan of totals[0, nBins) into offsets[0, nBins] by one CTA of
+// kScanThreads threads.
+__device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins, uint32_t* __restrict__ offsets)
 {
     __shared__ uint32_t s_warp[32];
     const uint32_t per = (nBins + blockDim.x - 1) / blockDim.x;
@@ -155,30 +178,49 @@ __global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __rest
     if(threadIdx.x == 0) offsets[nBins] = total;
 }
 
+namespace {
+
+__global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __restrict__ totals, uint32_t nBins,
+                                                           uint32_t* __restrict__ offsets)
+{
+    binscan_cta(totals, nBins, offsets);
+}
+
+} // namespace
+
+// Scatter pass of chunk c of nc: rank each sample in the shared-memory
+// cursors sh (p.nBins words) and write its sorted record.
+__device__ void scatter_chunk(const float* __restrict__ samples, uint64_t n, const BinParams& p, uint32_t c,
+                              uint32_t nc, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ offsets,
+                              float4* __restrict__ sorted, uint32_t* __restrict__ err, uint32_t* sh)
+{
+    const uint32_t* row = hist + (size_t)c * p.nBins;
+    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = offsets[b] + row[b];
+    const uint32_t total = offsets[p.nBins];
+    __syncthreads();
+
+    for_chunk(samples, n, p, c, nc, [&](bool valid, const float4& rec, uint32_t key, int) {
+        if(valid && key != kOutOfRange) {
+            const uint32_t pos = atomicAdd(&sh[key], 1u);
+            float4 out = rec;
+            if(p.echo_flags) {
+                const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z);
+                out.x = v.x; out.y = v.y;
+            }
+            if(pos < total) sorted[pos] = out;
+            else atomicOr(err, kErrScatterOverflow);
+        }
+    });
+}
+
+namespace {
+
 __global__ void k_scatter(const float* __restrict__ samples, uint64_t n, BinParams p,
                           const uint32_t* __restrict__ hist, const uint32_t* __restrict__ offsets,
                           float4* __restrict__ sorted, uint32_t* __restrict__ err)
 {
     extern __shared__ uint32_t sh[];
-    const uint32_t* row = hist + (size_t)blockIdx.x * p.nBins;
-    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = offsets[b] + row[b];
-    const uint32_t total = offsets[p.nBins];
-    __syncthreads();
-
-    const unsigned lt_mask = (1u << lane_id()) - 1u;
-    for_chunk(samples, n, p, [&](bool valid, const float4& rec, uint32_t key, int) {
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        const bool live = valid && key != kOutOfRange;
-        if(live && (int)lane_id() == leader) base = atomicAdd(&sh[key], (uint32_t)__popc(peers));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if(live) {
-            const uint32_t pos = base + (uint32_t)__popc(peers & lt_mask);
-            if(pos < total) sorted[pos] = rec;
-            else atomicOr(err, kErrScatterOverflow);
-        }
-    });
+    scatter_chunk(samples, n, p, blockIdx.x, gridDim.x, hist, offsets, sorted, err, sh);
 }
 
 __device__ __forceinline__ uint32_t bin_count(const uint32_t* off, uint32_t nBB, int j)
@@ -204,10 +246,13 @@ __device__ __forceinline__ bool ref_window(const uint32_t* off, uint32_t nBB, ui
     return true;
 }
 
-__global__ void k_windows(const uint32_t* __restrict__ off, uint32_t nBB, uint32_t nR, int ov,
-                          const int2* __restrict__ support, int2* __restrict__ win)
+} // namespace
+
+// Effective window of output row r: the reference window's first / last
+// non-empty bins intersected with the row's PSF support.
+__device__ void window_row(const uint32_t* __restrict__ off, uint32_t nBB, uint32_t nR, int ov,
+                           const int2* __restrict__ support, int2* __restrict__ win, int r)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if(r >= (int)nR) return;
     int f, l;
     int2 w = make_int2(1, 0);
@@ -216,6 +261,14 @@ __global__ void k_windows(const uint32_t* __restrict__ off, uint32_t nBB, uint32
         w = make_int2(max(f, s.x), min(l, s.y));
     }
     win[r] = w;
+}
+
+namespace {
+
+__global__ void k_windows(const uint32_t* __restrict__ off, uint32_t nBB, uint32_t nR, int ov,
+                          const int2* __restrict__ support, int2* __restrict__ win)
+{
+    window_row(off, nBB, nR, ov, support, win, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Reference-coordinate outputs of rtacx_bin: the reference's sorted array
@@ -256,6 +309,51 @@ __global__ void k_range_keys(const float* __restrict__ samples, uint64_t n, BinP
 __global__ void k_oor_out(const unsigned long long* __restrict__ src, uint64_t* __restrict__ dst)
 {
     if(threadIdx.x < 2) dst[threadIdx.x] = src[threadIdx.x];
+}
+
+// ---- batched stages (one launch per stage over every ping of a batch) -----
+
+__global__ void k_count_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
+{
+    extern __shared__ uint32_t sh[];
+    __shared__ unsigned long long s_oor[2];
+    const uint2 m = map[blockIdx.x];
+    const PingDev& P = pings[m.x];
+    count_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.hist, P.oor, sh, s_oor);
+}
+
+__global__ void k_colscan_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
+{
+    const uint2 m = map[blockIdx.x];
+    const PingDev& P = pings[m.x];
+    colscan_bin(P.hist, P.chunks, P.bin.nBins, P.totals, m.y * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_binscan_batch(const PingDev* __restrict__ pings)
+{
+    const PingDev& P = pings[blockIdx.x];
+    binscan_cta(P.totals, P.bin.nBins, P.offsets);
+}
+
+__global__ void k_scatter_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
+{
+    extern __shared__ uint32_t sh[];
+    const uint2 m = map[blockIdx.x];
+    const PingDev& P = pings[m.x];
+    scatter_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.hist, P.offsets, P.sorted, P.err, sh);
+}
+
+__global__ void k_windows_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
+{
+    const uint2 m = map[blockIdx.x];
+    const PingDev& P = pings[m.x];
+    window_row(P.offsets, P.bin.nBB, P.nR, P.overlap, P.support, P.win, m.y * blockDim.x + threadIdx.x);
+}
+
+__global__ void k_reset_batch(const PingDev* __restrict__ pings, uint32_t n_pings)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if(i < n_pings) { pings[i].oor[0] = 0ull; pings[i].oor[1] = 0ull; }
 }
 
 uint32_t hist_grid(const Context& ctx, uint64_t n)
@@ -350,6 +448,34 @@ rtacx_status run_bin_outputs(Context& ctx, const void* samples, uint64_t n,
         k_oor_out<<<1, 32, 0, stream>>>(ctx.d_oor, oor);
         RTACX_CUDA(cudaGetLastError());
     }
+    return RTACX_OK;
+}
+
+rtacx_status prepare_bin_batch(std::string& error, uint32_t max_bins)
+{
+    const size_t smem = std::max<size_t>((size_t)max_bins * sizeof(uint32_t), 1);
+    if(cudaFuncSetAttribute(k_count_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+       cudaFuncSetAttribute(k_scatter_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        error = "cannot reserve shared memory for the batched histograms";
+        return RTACX_ERR_CUDA;
+    }
+    return RTACX_OK;
+}
+
+rtacx_status launch_bin_batch(std::string& error, const PingDev* pings, uint32_t n_pings,
+                              const uint2* chunk_map, uint32_t n_chunks, const uint2* col_map, uint32_t n_col,
+                              const uint2* win_map, uint32_t n_win, uint32_t max_bins, cudaStream_t stream)
+{
+    const size_t smem = (size_t)max_bins * sizeof(uint32_t);
+    k_reset_batch<<<(n_pings + 255) / 256, 256, 0, stream>>>(pings, n_pings);
+    k_count_batch<<<n_chunks, 512, smem, stream>>>(pings, chunk_map);
+    k_colscan_batch<<<n_col, 256, 0, stream>>>(pings, col_map);
+    k_binscan_batch<<<n_pings, kScanThreads, 0, stream>>>(pings);
+    k_scatter_batch<<<n_chunks, 512, smem, stream>>>(pings, chunk_map);
+    k_windows_batch<<<n_win, 256, 0, stream>>>(pings, win_map);
+    const cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) { error = std::string("batched binning: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;
 }
 

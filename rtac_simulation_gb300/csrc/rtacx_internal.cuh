@@ -17,6 +17,7 @@ constexpr uint32_t kOutOfRange = RTACX_KEY_OUT_OF_RANGE;
 // Device error word bits (OR-ed by kernels, read by rtacx_stream_status).
 constexpr uint32_t kErrScatterOverflow = 1u << 0;  // sorted position beyond the counted total
 constexpr uint32_t kErrBadWindow       = 1u << 1;  // window bounds outside the sorted array
+constexpr uint32_t kErrGemmTimeout     = 1u << 2;  // a bounded mbarrier wait of the tensor-core GEMM expired
 
 // Largest (range bin x bearing bin) histogram a CTA keeps in shared memory.
 constexpr uint32_t kMaxSmemBins = 49152;
@@ -30,7 +31,31 @@ struct BinParams {
     uint32_t nBins;        // nR * nBB
     uint32_t stride;       // floats per input record: 3 (SimSample1D) or 4 (SimSample2D)
     int vec4;              // 1 when records are 16-byte aligned float4s
+    uint32_t echo_flags;   // RTACX_ECHO_* pre-step applied to each sample value (0: none)
+    double echo_cycles;    // carrier cycles per metre of travel, 2 f / c
 };
+
+// Echo-sample epilogue of the reference's ray generator
+// (src/RayCaster.cu:37-39, 69-71): value *= exp(i 4 pi f d / c) / d^2. The
+// carrier phase is reduced modulo one cycle in FP64 (d * 2f/c, minus its
+// nearest integer: three FP64 operations); the reduced fraction is then
+// exact enough for float sincos.
+__device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel)
+{
+    if(p.echo_flags & RTACX_ECHO_PHASE) {
+        const double cyc = (double)travel * p.echo_cycles;
+        const double frac = cyc - rint(cyc);
+        const float ph = (float)frac * 6.28318530717958647692f;
+        float sn, cs;
+        sincosf(ph, &sn, &cs);
+        v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
+    }
+    if(p.echo_flags & RTACX_ECHO_SPREADING) {
+        const float inv = 1.0f / (travel * travel);
+        v = make_float2(v.x * inv, v.y * inv);
+    }
+    return v;
+}
 
 // Range key of one travel value: Binner::Key::operator()
 // (include/rtac_simulation/Binner.h:47-53) with CUDA float->int semantics.
@@ -86,6 +111,31 @@ struct ReduceParams {
     AxisLerp beam_axis;
 };
 
+// Everything one ping of a batch needs on the device (rtacx_batch_*).
+struct PingDev {
+    const float* samples;
+    uint64_t n;
+    BinParams bin;
+    uint32_t chunks;                 // CTAs of its count / scatter passes
+    uint32_t* hist;
+    uint32_t* totals;
+    uint32_t* offsets;
+    unsigned long long* oor;
+    uint32_t* err;
+    float4* sorted;
+    uint32_t nR;
+    int overlap;
+    const int2* support;
+    int2* win;
+    ReduceParams red;
+    const int2* bb_tiles;
+    const float* ranges;
+    const float* bearings;
+    const float2* pulse;
+    const float* beam;
+    float2* out;
+};
+
 // Scratch and configuration owned by one context.
 struct Context {
     int device = 0;
@@ -113,7 +163,9 @@ struct Context {
     float* d_bearings = nullptr;        // [nB]
     float* d_ranges = nullptr;          // [nR] Linspace values
     int2* d_support = nullptr;          // [nR] range bins that can hold PSF support of row r
-    int2* d_bb_tiles = nullptr;         // [bearing tiles] bearing-bin range of each tile
+    int2* d_bb_tiles = nullptr;         // bearing-bin range of each tile of width bearing_tile
+    int2* d_bb_tiles64 = nullptr;       // ... of each 64-bearing tile
+    int2* d_bb_tiles128 = nullptr;      // ... of each 128-bearing tile
     uint32_t* d_offsets = nullptr;      // [nBins + 1] exclusive scan of bin counts
     uint32_t* d_totals = nullptr;       // [nBins]
     int2* d_win = nullptr;              // [nR] effective bin range per row (lo > hi: empty)
@@ -127,6 +179,25 @@ struct Context {
     uint32_t hist_threads = 0;
     size_t hist_cols = 0;               // allocated CTA x bin entries
     uint32_t* d_hist = nullptr;         // [hist_ctas][nBins]
+
+    // Echo model (rtacx_set_echo_model).
+    uint32_t echo_flags = 0;
+    double echo_hz = 0.0;
+
+    // Precision form (rtacx_configure_precision).
+    bool prec_configured = false;
+    uint32_t taps = 0, tap_center = 0;
+    uint32_t Mpad = 0, Npad = 0, Kp = 0;
+    float4* d_G = nullptr;              // [nR][nB] binned pair cells {to bearing k, to bearing k+1}
+    uint32_t* d_flags = nullptr;        // [(nR + 31) / 32] bitmap of non-empty range bins
+    int* d_lut = nullptr;               // bearing lookup grid
+    uint32_t lut_cells = 0;
+    float lut_origin = 0.0f, lut_scale = 0.0f;
+    int2* d_pwin = nullptr;             // [nR] window bin interval per row (lo > hi: empty)
+    uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the filtered grid
+    uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity
+    float* d_C = nullptr;               // [Mpad][Npad] GEMM output when the ping shape is not tile-aligned
+    float2* d_taps = nullptr;           // [taps] range taps at bin offsets t - tap_center
 
     // Stage tracing: events[2 * i], events[2 * i + 1] bracket stage i.
     bool tracing = false;
@@ -151,6 +222,30 @@ bool ensure_capacity(Context& ctx, uint64_t n);
 
 // Sparse PSF reduction (rtacx_reduce.cu).
 rtacx_status run_reduce(Context& ctx, float* out, cudaStream_t stream);
+
+// Batched plain form. Maps are (ping, index) pairs: count / scatter chunks,
+// column-scan bin blocks of 256, window row blocks of 256; gather items are
+// {ping, tile_b, tile_r, 0} for 2D pings and {ping, row_group, 0, 1} for 1D.
+rtacx_status launch_bin_batch(std::string& error, const PingDev* pings, uint32_t n_pings,
+                              const uint2* chunk_map, uint32_t n_chunks, const uint2* col_map, uint32_t n_col,
+                              const uint2* win_map, uint32_t n_win, uint32_t max_bins, cudaStream_t stream);
+rtacx_status prepare_bin_batch(std::string& error, uint32_t max_bins);
+rtacx_status prepare_gather_batch(std::string& error, int shape, size_t smem);
+size_t gather_batch_smem(int shape, uint32_t H, uint32_t W);
+rtacx_status launch_gather_batch(std::string& error, int shape, const PingDev* pings, const uint4* items,
+                                 uint32_t n_items, uint32_t* counter, size_t smem, uint32_t grid,
+                                 cudaStream_t stream);
+int gather_shape_rows(int shape);
+int gather_shape_bearings(int shape);
+
+// Precision form (rtacx_precision.cu).
+rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float* out, cudaStream_t stream);
+void free_precision(Context& ctx);
+
+// Tensor-core GEMM (rtacx_umma.cu): C = A * B^T, bf16 K-major operands.
+rtacx_status gemm_bf16_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K,
+                          int ldc, cudaStream_t stream, uint32_t* err);
+size_t gemm_smem_bytes();
 
 } // namespace rtacx
 

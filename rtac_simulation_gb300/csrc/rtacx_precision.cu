@@ -1,0 +1,418 @@
+// Precision (tensor-core) form: bin first, contract over bearings on the
+// tensor cores, filter in range.
+//
+//   k_prec_accumulate  one pass over the samples (read once, 16 B each):
+//                      range key (Binner::Key, bit-exact), optional FP64
+//                      echo pre-step, linear split between the two table
+//                      bearings around the sample bearing, one 16-byte vector
+//                      float atomic (red.global.add.v4.f32) into the pair
+//                      cell P[j][k]; non-empty range bins in a bitmap. No sort.
+//   k_prec_windows     reference window rule (src/Binner.cu:95-104) on the
+//                      non-empty bitmap.
+//   k_prec_filter      G'[r][k] = sum_t taps[t] G[r + t - c][k] over row r's
+//                      window, written as the bf16 A operand [hi | hi | lo]
+//                      of the three-term split product.
+//   gemm_bf16_tn       out = A x B^T on tcgen05 (rtacx_umma.cu), B the
+//                      [hi | lo | hi] split of the complex directivity laid
+//                      out so that output column 2b is Re(out(r, b)) and
+//                      2b + 1 is Im(out(r, b)): the GEMM writes the
+//                      complex64 ping directly.
+#include "rtacx_internal.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace rtacx {
+
+namespace {
+
+constexpr int kMaxBearingsSmem = 2048;
+
+__device__ __forceinline__ void red_add_v4(float4* addr, float4 v)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+
+// Pair cells: P[j][k] = {contribution to bearing k, contribution to bearing
+// k + 1} of the samples of range bin j whose bearing lies in [theta_k,
+// theta_k+1). One 16-byte vector atomic per sample; the filter kernel forms
+// G[j][k] = P[j][k].xy + P[j][k - 1].zw. Non-empty range bins are collected
+// in a shared-memory bitmap per CTA and OR-ed into the global bitmap once.
+// The bearing cell comes from a uniform lookup grid (lut[c] = the table
+// index at or below the grid line c), corrected by exact comparisons with the
+// table, so it equals the largest k in [0, nB - 2] with theta_k <= theta.
+constexpr int kMaxRangeWords = 8192 / 32 * 4;   // bitmap words for up to 32768 range bins
+constexpr int kLutCells = 4 * kMaxBearingsSmem;
+
+__global__ void __launch_bounds__(256)
+k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
+                  const float* __restrict__ bearings, uint32_t nB, const int* __restrict__ lut,
+                  uint32_t lut_cells, float lut_origin, float lut_scale,
+                  float4* __restrict__ P, uint32_t* __restrict__ nonempty)
+{
+    __shared__ float s_th[kMaxBearingsSmem];
+    __shared__ int16_t s_lut[kLutCells];
+    __shared__ uint32_t s_bits[kMaxRangeWords];
+    const uint32_t words = (p.key.nR + 31) / 32;
+    for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) s_th[i] = bearings[i];
+    for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = (int16_t)lut[i];
+    for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
+    __syncthreads();
+    const int kmax = (int)nB - 2;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float4 rec = load_record(samples, i, p);
+        int side;
+        const uint32_t j = range_key(p.key, rec.z, side);
+        if(j == kOutOfRange) continue;
+        const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z);
+        atomicOr(&s_bits[j >> 5], 1u << (j & 31));
+        if(nB == 1) { red_add_v4(P + j, make_float4(v.x, v.y, 0.f, 0.f)); continue; }
+        const float th = rec.w;
+        const float q = fminf(fmaxf((th - lut_origin) * lut_scale, 0.0f), (float)(lut_cells - 1));
+        int k = s_lut[(int)q];                       // NaN bearings: q = 0
+        while(k < kmax && s_th[k + 1] <= th) k++;
+        while(k > 0 && !(s_th[k] <= th)) k--;
+        const float t0 = s_th[k], t1 = s_th[k + 1];
+        float w = (th - t0) / (t1 - t0);
+        w = fminf(fmaxf(w, 0.0f), 1.0f);          // NaN bearings -> 0
+        const float w0 = 1.0f - w;
+        red_add_v4(P + (size_t)j * nB + k, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y));
+    }
+    __syncthreads();
+    for(uint32_t i = threadIdx.x; i < words; i += blockDim.x)
+        if(s_bits[i]) atomicOr(&nonempty[i], s_bits[i]);
+}
+
+__device__ __forceinline__ bool bit_set(const uint32_t* bits, long long j)
+{
+    return (bits[j >> 5] >> (j & 31)) & 1u;
+}
+
+__global__ void k_prec_windows(const uint32_t* __restrict__ nonempty, uint32_t nR, int ov, int2* __restrict__ win)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if(r >= (int)nR) return;
+    const long long lo = max(0ll, (long long)r - ov);
+    const long long hi = min((long long)nR - 1, (long long)r + ov);
+    int2 w = make_int2(1, 0);
+    long long a = lo;
+    while(a <= hi && !bit_set(nonempty, a)) a++;
+    if(a < hi) {
+        long long z = hi;
+        while(z > a && !bit_set(nonempty, z)) z--;
+        if(a < z) w = make_int2((int)a, (int)z);
+    }
+    win[r] = w;
+}
+
+// Round-to-nearest-even fp32 -> bf16 (bit pattern).
+__device__ __forceinline__ uint16_t bf16_bits(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+__device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
+
+constexpr int kFiltRows = 32, kFiltCols = 64, kFiltTaps = 56;
+
+// Range filter + split. One CTA per 32 rows x 64 bearings; the binned grid
+// rows a chunk of taps needs are staged in shared memory once (formed from
+// the pair cells), then each thread filters its 4 rows x 2 bearings and
+// writes the bf16 A operand [hi | hi | lo] of its outputs.
+__global__ void __launch_bounds__(256)
+k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const float2* __restrict__ taps,
+              uint32_t ntaps, uint32_t center, uint32_t nR, uint32_t nB, uint32_t Kp, uint16_t* __restrict__ A)
+{
+    __shared__ float2 sG[kFiltRows + kFiltTaps - 1][kFiltCols];
+    __shared__ float2 sT[kFiltTaps];
+    __shared__ int2 sW[kFiltRows];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols;
+    if(tid < kFiltRows) sW[tid] = (r0 + tid < (int)nR) ? win[r0 + tid] : make_int2(1, 0);
+    float2 acc[4][2];
+#pragma unroll
+    for(int q = 0; q < 4; q++) { acc[q][0] = make_float2(0.f, 0.f); acc[q][1] = make_float2(0.f, 0.f); }
+
+    for(int tc = 0; tc < (int)ntaps; tc += kFiltTaps) {
+        const int nt = min(kFiltTaps, (int)ntaps - tc);
+        const int jlo = r0 + tc - (int)center;          // bin of sG row 0
+        __syncthreads();
+        if(tid < nt) sT[tid] = taps[tc + tid];
+        for(int idx = tid; idx < (kFiltRows + nt - 1) * kFiltCols; idx += 256) {
+            const int rr = idx / kFiltCols, kk = idx % kFiltCols;
+            const int j = jlo + rr, k = k0 + kk;
+            float2 g = make_float2(0.f, 0.f);
+            if(j >= 0 && j < (int)nR && k < (int)nB) {
+                const float4 a = P[(size_t)j * nB + k];
+                g = make_float2(a.x, a.y);
+                if(k > 0) {
+                    const float4 b = P[(size_t)j * nB + k - 1];
+                    g.x += b.z; g.y += b.w;
+                }
+            }
+            sG[rr][kk] = g;
+        }
+        __syncthreads();
+#pragma unroll
+        for(int q = 0; q < 4; q++) {
+            const int rr = warp * 4 + q, r = r0 + rr;
+            const int2 w = sW[rr];
+            if(w.x > w.y) continue;
+            // taps t (absolute) with bin j = r + t - center inside the window
+            const int tlo = max(tc, w.x - r + (int)center), thi = min(tc + nt - 1, w.y - r + (int)center);
+            for(int t = tlo; t <= thi; t++) {
+                const float2 c = sT[t - tc];
+#pragma unroll
+                for(int h = 0; h < 2; h++) {
+                    const float2 g = sG[rr + t - tc][lane + 32 * h];
+                    acc[q][h].x = fmaf(c.x, g.x, fmaf(-c.y, g.y, acc[q][h].x));
+                    acc[q][h].y = fmaf(c.x, g.y, fmaf(c.y, g.x, acc[q][h].y));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for(int q = 0; q < 4; q++) {
+        const int r = r0 + warp * 4 + q;
+        if(r >= (int)nR) continue;
+        uint16_t* row = A + (size_t)r * Kp;
+#pragma unroll
+        for(int h = 0; h < 2; h++) {
+            const int k = k0 + lane + 32 * h;
+            if(k >= (int)nB) continue;
+            const float2 v = acc[q][h];
+            const uint16_t hr = bf16_bits(v.x), hi = bf16_bits(v.y);
+            const uint16_t lr = bf16_bits(v.x - bf16_value(hr)), li = bf16_bits(v.y - bf16_value(hi));
+            row[k] = hr;               row[nB + k] = hi;
+            row[2 * nB + k] = hr;      row[3 * nB + k] = hi;
+            row[4 * nB + k] = lr;      row[5 * nB + k] = li;
+        }
+    }
+}
+
+uint16_t host_bf16_bits(float x)
+{
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+float host_bf16_value(uint16_t b)
+{
+    uint32_t u = (uint32_t)b << 16;
+    float x;
+    std::memcpy(&x, &u, 4);
+    return x;
+}
+
+double host_lerp(const float* tab, int n, int comps, int comp, double x)
+{
+    const double fl = std::floor(x);
+    if(!(fl >= -1.0 && fl <= (double)(n - 1))) return 0.0;
+    const int i = (int)fl;
+    const double a = x - fl;
+    const double lo = i >= 0 ? tab[(size_t)i * comps + comp] : 0.0;
+    const double hi = i + 1 < n ? tab[(size_t)(i + 1) * comps + comp] : 0.0;
+    return lo * (1.0 - a) + hi * a;
+}
+
+#define RTACX_CUDA(call)                                                         \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if(e_ != cudaSuccess) {                                                  \
+            ctx.error = std::string(#call) + ": " + cudaGetErrorString(e_);      \
+            return RTACX_ERR_CUDA;                                               \
+        }                                                                        \
+    } while(0)
+
+template <typename T>
+void free_dev(T*& p)
+{
+    if(p) cudaFree(p);
+    p = nullptr;
+}
+
+} // namespace
+
+void free_precision(Context& c)
+{
+    free_dev(c.d_G); free_dev(c.d_flags); free_dev(c.d_pwin); free_dev(c.d_A); free_dev(c.d_B);
+    free_dev(c.d_C); free_dev(c.d_taps); free_dev(c.d_lut);
+    c.prec_configured = false;
+}
+
+rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
+{
+    if(!ctx.configured || ctx.dims != 2) { ctx.error = "the precision form needs a configured 2D sensor"; return RTACX_ERR_NOT_CONFIGURED; }
+    if(!d) { ctx.error = "null precision descriptor"; return RTACX_ERR_INVALID_ARGUMENT; }
+    const uint32_t nB = ctx.nB, nR = ctx.nR;
+    if(nB > (uint32_t)kMaxBearingsSmem) { ctx.error = "too many bearings for the precision form"; return RTACX_ERR_UNSUPPORTED; }
+    for(uint32_t b = 1; b < nB; b++)
+        if(!(ctx.bearings[b] > ctx.bearings[b - 1])) {
+            ctx.error = "the precision form needs strictly increasing bearings";
+            return RTACX_ERR_INVALID_ARGUMENT;
+        }
+    free_precision(ctx);
+
+    // Directivity D[k][b] (complex), given or derived from the beam table.
+    std::vector<float> D((size_t)nB * nB * 2, 0.0f);
+    if(d->directivity) {
+        std::memcpy(D.data(), d->directivity, D.size() * sizeof(float));
+    }
+    else {
+        const double kx = (double)(1.0f / ctx.span) * ctx.W, cx = 0.5 * ctx.W - 0.5;
+        for(uint32_t k = 0; k < nB; k++)
+            for(uint32_t b = 0; b < nB; b++) {
+                const float e = ctx.bearings[k] - ctx.bearings[b];
+                D[((size_t)k * nB + b) * 2] = (float)host_lerp(ctx.beam.data(), (int)ctx.W, 1, 0, (double)e * kx + cx);
+            }
+    }
+    for(float v : D) if(!std::isfinite(v)) { ctx.error = "non-finite directivity"; return RTACX_ERR_INVALID_ARGUMENT; }
+
+    // Range taps, given or derived from the pulse table at bin offsets.
+    std::vector<float> taps;
+    uint32_t center;
+    if(d->range_taps) {
+        if(d->tap_count == 0 || d->tap_center >= d->tap_count) { ctx.error = "bad tap_count / tap_center"; return RTACX_ERR_INVALID_ARGUMENT; }
+        taps.assign(d->range_taps, d->range_taps + 2 * (size_t)d->tap_count);
+        center = d->tap_center;
+    }
+    else {
+        const int ov = std::max(0, ctx.overlap);
+        const double res = (nR > 1) ? (double)((ctx.rmax - ctx.rmin) / (float)(nR - 1u)) : 0.0;
+        const float pscale = host_pulse_scale(ctx.duration, ctx.c, false);
+        const double ky = (double)pscale * ctx.H, cy = 0.5 * ctx.H - 0.5;
+        int first = ov + 1, last = -ov - 1;
+        std::vector<float> full((size_t)(2 * ov + 1) * 2);
+        for(int t = -ov; t <= ov; t++) {
+            const double x = t * res * ky + cy;
+            const float re = (float)host_lerp(ctx.pulse.data(), (int)ctx.H, 2, 0, x);
+            const float im = (float)host_lerp(ctx.pulse.data(), (int)ctx.H, 2, 1, x);
+            full[(size_t)(t + ov) * 2] = re; full[(size_t)(t + ov) * 2 + 1] = im;
+            if(re != 0.0f || im != 0.0f) { first = std::min(first, t); last = std::max(last, t); }
+        }
+        if(first > last) { first = 0; last = 0; }
+        taps.assign(full.begin() + (size_t)(first + ov) * 2, full.begin() + (size_t)(last + ov + 1) * 2);
+        center = (uint32_t)(-first);
+    }
+    for(float v : taps) if(!std::isfinite(v)) { ctx.error = "non-finite range taps"; return RTACX_ERR_INVALID_ARGUMENT; }
+    ctx.taps = (uint32_t)(taps.size() / 2);
+    ctx.tap_center = center;
+    if(nR > (uint32_t)kMaxRangeWords * 32) { ctx.error = "too many range bins for the precision form"; return RTACX_ERR_UNSUPPORTED; }
+
+    // Bearing lookup grid: lut[c] = largest k in [0, nB - 2] whose bearing is
+    // at or below the grid line origin + c / scale (0 below the table).
+    const uint32_t cells = std::min<uint32_t>(4 * nB, (uint32_t)kLutCells);
+    const float origin = ctx.bearings[0];
+    const float width = (nB > 1) ? ctx.bearings[nB - 1] - ctx.bearings[0] : 1.0f;
+    const float lscale = (float)cells / width;
+    std::vector<int> lut(cells, 0);
+    for(uint32_t cidx = 0; cidx < cells; cidx++) {
+        const double line = (double)origin + (double)cidx / (double)lscale;
+        int k = 0;
+        while(k + 1 <= (int)nB - 2 && (double)ctx.bearings[k + 1] <= line) k++;
+        lut[cidx] = k;
+    }
+    ctx.lut_cells = cells;
+    ctx.lut_origin = origin;
+    ctx.lut_scale = lscale;
+
+    // GEMM operand shapes.
+    ctx.Mpad = (nR + 127) / 128 * 128;
+    ctx.Npad = (2 * nB + 255) / 256 * 256;
+    ctx.Kp = (6 * nB + 63) / 64 * 64;
+
+    // B operand: row n = 2b (real) / 2b + 1 (imag); K blocks [hi | lo | hi]
+    // of [real part of G pairs | imaginary part of G pairs].
+    std::vector<uint16_t> B((size_t)ctx.Npad * ctx.Kp, 0);
+    for(uint32_t b = 0; b < nB; b++)
+        for(uint32_t k = 0; k < nB; k++) {
+            const float dr = D[((size_t)k * nB + b) * 2], di = D[((size_t)k * nB + b) * 2 + 1];
+            const float vals[2][2] = {{dr, -di}, {di, dr}};     // [re/im output][G real / G imag]
+            for(int o = 0; o < 2; o++)
+                for(int h = 0; h < 2; h++) {
+                    const float v = vals[o][h];
+                    const uint16_t bh = host_bf16_bits(v);
+                    const uint16_t bl = host_bf16_bits(v - host_bf16_value(bh));
+                    uint16_t* row = B.data() + (size_t)(2 * b + o) * ctx.Kp;
+                    row[h * nB + k] = bh;
+                    row[2 * nB + h * nB + k] = bl;
+                    row[4 * nB + h * nB + k] = bh;
+                }
+        }
+
+    const bool direct = (ctx.Mpad == nR) && (ctx.Npad == 2 * nB);
+    auto alloc = [&](auto*& p, size_t bytes) {
+        if(cudaMalloc(&p, bytes) != cudaSuccess) { cudaGetLastError(); p = nullptr; return false; }
+        return true;
+    };
+    if(!alloc(ctx.d_G, (size_t)nR * nB * sizeof(float4)) || !alloc(ctx.d_flags, (size_t)(nR + 31) / 32 * 4) ||
+       !alloc(ctx.d_lut, (size_t)cells * sizeof(int)) ||
+       !alloc(ctx.d_pwin, (size_t)nR * sizeof(int2)) || !alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) ||
+       !alloc(ctx.d_B, B.size() * 2) || !alloc(ctx.d_taps, taps.size() * sizeof(float)) ||
+       (!direct && !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float)))) {
+        free_precision(ctx);
+        ctx.error = "out of device memory for the precision form";
+        return RTACX_ERR_OUT_OF_MEMORY;
+    }
+    if(cudaMemset(ctx.d_A, 0, (size_t)ctx.Mpad * ctx.Kp * 2) != cudaSuccess ||
+       cudaMemcpy(ctx.d_B, B.data(), B.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(ctx.d_taps, taps.data(), taps.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(ctx.d_lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        free_precision(ctx);
+        ctx.error = "uploading the precision tables failed";
+        return RTACX_ERR_CUDA;
+    }
+    if(gemm_smem_bytes() > 227 * 1024) { ctx.error = "GEMM tile exceeds shared memory"; return RTACX_ERR_UNSUPPORTED; }
+    ctx.prec_configured = true;
+    return RTACX_OK;
+}
+
+rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float* out, cudaStream_t stream)
+{
+    const uint32_t nR = ctx.nR, nB = ctx.nB;
+    ctx.mark(0, false, stream);
+    RTACX_CUDA(cudaMemsetAsync(ctx.d_G, 0, (size_t)nR * nB * sizeof(float4), stream));
+    RTACX_CUDA(cudaMemsetAsync(ctx.d_flags, 0, (size_t)(nR + 31) / 32 * 4, stream));
+    if(n) {
+        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx.sm_count * 4);
+        k_prec_accumulate<<<blocks, 256, 0, stream>>>(static_cast<const float*>(samples), n, ctx.bin,
+                                                      ctx.d_bearings, nB, ctx.d_lut, ctx.lut_cells, ctx.lut_origin,
+                                                      ctx.lut_scale, ctx.d_G, ctx.d_flags);
+        RTACX_CUDA(cudaGetLastError());
+    }
+    ctx.mark(0, true, stream);
+    ctx.mark(1, false, stream);
+    k_prec_windows<<<(nR + 255) / 256, 256, 0, stream>>>(ctx.d_flags, nR, ctx.overlap, ctx.d_pwin);
+    RTACX_CUDA(cudaGetLastError());
+    ctx.mark(1, true, stream);
+    ctx.mark(2, false, stream);
+    k_prec_filter<<<dim3((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows), 256, 0, stream>>>(
+        ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, ctx.d_A);
+    RTACX_CUDA(cudaGetLastError());
+    ctx.mark(2, true, stream);
+    ctx.mark(3, false, stream);
+    const bool direct = ctx.d_C == nullptr;
+    float* C = direct ? out : ctx.d_C;
+    rtacx_status st = gemm_bf16_tn(ctx.error, ctx.d_A, ctx.d_B, C, (int)ctx.Mpad, (int)ctx.Npad, (int)ctx.Kp,
+                                   (int)ctx.Npad, stream, ctx.d_err);
+    if(st != RTACX_OK) return st;
+    ctx.mark(3, true, stream);
+    ctx.mark(4, false, stream);
+    if(!direct)
+        RTACX_CUDA(cudaMemcpy2DAsync(out, (size_t)2 * nB * sizeof(float), ctx.d_C, (size_t)ctx.Npad * sizeof(float),
+                                     (size_t)2 * nB * sizeof(float), nR, cudaMemcpyDeviceToDevice, stream));
+    ctx.mark(4, true, stream);
+    return RTACX_OK;
+}
+
+} // namespace rtacx

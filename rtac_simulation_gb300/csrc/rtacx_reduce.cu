@@ -75,26 +75,27 @@ struct GatherSmem {
     int jmin, jmax;
 };
 
+// One (TR rows x TB bearings) output tile (tile_b, tile_r) of a 2D ping;
+// smem_raw holds GatherSmem<TR, TB> followed by the padded pulse and beam.
 template <int TR, int TB>
-__global__ void __launch_bounds__(kThreads)
-k_gather_2d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
-            const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
-            const float* __restrict__ ranges, const float* __restrict__ bearings,
-            const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
-            ReduceParams rp, uint32_t nBB, float2* __restrict__ out)
+__device__ __forceinline__ void gather_tile_2d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+                                               const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
+                                               const float* __restrict__ ranges, const float* __restrict__ bearings,
+                                               const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
+                                               const ReduceParams& rp, uint32_t nBB, float2* __restrict__ out,
+                                               int tile_b, int tile_r, unsigned char* smem_raw)
 {
     constexpr int RPW = TR / kWarps;   // rows per warp
     constexpr int BPL = TB / 32;       // bearings per lane
     static_assert(TR % kWarps == 0 && TB % 32 == 0, "tile shape");
     using Smem = GatherSmem<TR, TB>;
 
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
     float2* s_pulse = reinterpret_cast<float2*>(smem_raw + sizeof(Smem));
     float* s_beam = reinterpret_cast<float*>(s_pulse + (rp.range_axis.n + 2));
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r0 = blockIdx.y * TR, b0 = blockIdx.x * TB;
+    const int r0 = tile_r * TR, b0 = tile_b * TB;
     const int nR = (int)rp.nR, nB = (int)rp.nB;
 
     for(int i = tid; i < rp.range_axis.n + 2; i += kThreads) s_pulse[i] = pulse_pad[i];
@@ -130,7 +131,7 @@ k_gather_2d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
         for(int c = 0; c < BPL; c++) acc[q][c] = make_float2(0.f, 0.f);
 
     const int jmin = S.jmin, jmax = S.jmax;
-    const int2 kb = bb_tiles[blockIdx.x];
+    const int2 kb = bb_tiles[tile_b];
     for(int jg = jmin; jg <= jmax; jg += kThreads) {
         // Segment of bin (jg + tid) restricted to this tile's bearing bins.
         const int j = jg + tid;
@@ -228,18 +229,28 @@ k_gather_2d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
     }
 }
 
-// 1D: one warp per output range bin.
+template <int TR, int TB>
 __global__ void __launch_bounds__(kThreads)
-k_gather_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
-            const int2* __restrict__ win, const float* __restrict__ ranges,
-            const float2* __restrict__ pulse_pad, ReduceParams rp, float2* __restrict__ out)
+k_gather_2d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+            const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
+            const float* __restrict__ ranges, const float* __restrict__ bearings,
+            const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
+            ReduceParams rp, uint32_t nBB, float2* __restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* s_pulse = reinterpret_cast<float2*>(smem_raw);
-    for(int i = threadIdx.x; i < rp.range_axis.n + 2; i += kThreads) s_pulse[i] = pulse_pad[i];
-    __syncthreads();
+    gather_tile_2d<TR, TB>(sorted, off, win, bb_tiles, ranges, bearings, pulse_pad, beam_pad, rp, nBB, out,
+                           blockIdx.x, blockIdx.y, smem_raw);
+}
+
+// 1D: one warp per output range bin; rows [row0, row0 + kWarps). The pulse
+// table must already be in s_pulse.
+__device__ __forceinline__ void gather_rows_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+                                               const int2* __restrict__ win, const float* __restrict__ ranges,
+                                               const float2* s_pulse, const ReduceParams& rp,
+                                               float2* __restrict__ out, int row0)
+{
     const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int r = row0 + (threadIdx.x >> 5);
     if(r >= (int)rp.nR) return;
     const int2 w = win[r];
     float2 acc = make_float2(0.f, 0.f);
@@ -258,6 +269,49 @@ k_gather_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
         acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
     }
     if(lane == 0) out[r] = acc;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_gather_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+            const int2* __restrict__ win, const float* __restrict__ ranges,
+            const float2* __restrict__ pulse_pad, ReduceParams rp, float2* __restrict__ out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* s_pulse = reinterpret_cast<float2*>(smem_raw);
+    for(int i = threadIdx.x; i < rp.range_axis.n + 2; i += kThreads) s_pulse[i] = pulse_pad[i];
+    __syncthreads();
+    gather_rows_1d(sorted, off, win, ranges, s_pulse, rp, out, blockIdx.x * kWarps);
+}
+
+// Persistent batched gather: each CTA takes work items from a global counter
+// (one atomicAdd per item, no waiting) until the list is exhausted. Items are
+// 2D tiles {ping, tile_b, tile_r, 0} or 1D row groups {ping, group, 0, 1}.
+template <int TR, int TB>
+__global__ void __launch_bounds__(kThreads)
+k_gather_batch(const PingDev* __restrict__ pings, const uint4* __restrict__ items, uint32_t n_items,
+               uint32_t* __restrict__ counter)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_item;
+    for(;;) {
+        if(threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if(it >= n_items) break;
+        const uint4 item = items[it];
+        const PingDev& P = pings[item.x];
+        if(item.w == 0) {
+            gather_tile_2d<TR, TB>(P.sorted, P.offsets, P.win, P.bb_tiles, P.ranges, P.bearings, P.pulse, P.beam,
+                                   P.red, P.bin.nBB, P.out, (int)item.y, (int)item.z, smem_raw);
+        }
+        else {
+            float2* s_pulse = reinterpret_cast<float2*>(smem_raw);
+            for(int i = threadIdx.x; i < P.red.range_axis.n + 2; i += kThreads) s_pulse[i] = P.pulse[i];
+            __syncthreads();
+            gather_rows_1d(P.sorted, P.offsets, P.win, P.ranges, s_pulse, P.red, P.out, (int)item.y * kWarps);
+        }
+        __syncthreads();
+    }
 }
 
 template <int TR, int TB>
@@ -284,6 +338,53 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
 }
 
 } // namespace
+
+// Batched gather tile shapes: 0 = 16 x 64, 1 = 16 x 128, 2 = 32 x 128.
+int gather_shape_rows(int shape) { return shape == 2 ? 32 : 16; }
+int gather_shape_bearings(int shape) { return shape == 0 ? 64 : 128; }
+
+size_t gather_batch_smem(int shape, uint32_t H, uint32_t W)
+{
+    const size_t base = shape == 2 ? sizeof(GatherSmem<32, 128>)
+                      : shape == 1 ? sizeof(GatherSmem<16, 128>) : sizeof(GatherSmem<16, 64>);
+    return base + (H + 2) * sizeof(float2) + (W + 2) * sizeof(float);
+}
+
+template <int TR, int TB>
+rtacx_status prepare_batch_shape(std::string& error, size_t smem)
+{
+    if(cudaFuncSetAttribute(k_gather_batch<TR, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        error = "PSF tables too large for the batched gather";
+        return RTACX_ERR_UNSUPPORTED;
+    }
+    return RTACX_OK;
+}
+
+template <int TR, int TB>
+rtacx_status launch_batch_shape(std::string& error, const PingDev* pings, const uint4* items, uint32_t n_items,
+                                uint32_t* counter, size_t smem, uint32_t grid, cudaStream_t stream)
+{
+    k_gather_batch<TR, TB><<<grid, kThreads, smem, stream>>>(pings, items, n_items, counter);
+    const cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) { error = std::string("k_gather_batch: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    return RTACX_OK;
+}
+
+rtacx_status prepare_gather_batch(std::string& error, int shape, size_t smem)
+{
+    if(shape == 2) return prepare_batch_shape<32, 128>(error, smem);
+    if(shape == 1) return prepare_batch_shape<16, 128>(error, smem);
+    return prepare_batch_shape<16, 64>(error, smem);
+}
+
+rtacx_status launch_gather_batch(std::string& error, int shape, const PingDev* pings, const uint4* items,
+                                 uint32_t n_items, uint32_t* counter, size_t smem, uint32_t grid, cudaStream_t stream)
+{
+    if(shape == 2) return launch_batch_shape<32, 128>(error, pings, items, n_items, counter, smem, grid, stream);
+    if(shape == 1) return launch_batch_shape<16, 128>(error, pings, items, n_items, counter, smem, grid, stream);
+    return launch_batch_shape<16, 64>(error, pings, items, n_items, counter, smem, grid, stream);
+}
 
 size_t gather_smem_bytes(uint32_t range_tile, uint32_t bearing_tile, uint32_t H, uint32_t W)
 {

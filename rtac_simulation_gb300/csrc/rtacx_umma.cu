@@ -1,0 +1,322 @@
+// BF16 tensor-core GEMM on sm_103a: C[M][N] (fp32) = A[M][K] * B[N][K]^T.
+//
+// Used by the precision form for the dense complex bearing-directivity
+// contraction, written as one real GEMM (see rtacx_precision.cu). Both
+// operands are K-major bf16 ("TN"); M % 128 == 0, N % 256 == 0, K % 64 == 0
+// (callers pad).
+//
+// One CTA computes a 128 x 256 tile with four warps:
+//   warp 0, lane 0  TMA producer: cp.async.bulk.tensor 2D loads of a 128x64
+//                   A tile and a 256x64 B tile per stage (128-byte swizzle)
+//                   into a 4-stage shared-memory ring guarded by mbarriers;
+//   warp 1, lane 0  MMA issuer: four tcgen05.mma.kind::f16 (K = 16 each) per
+//                   stage into a 128-lane x 256-column fp32 TMEM accumulator,
+//                   tcgen05.commit frees the stage;
+//   warps 0-3       epilogue: tcgen05.ld 32x32b of their TMEM lane quadrant,
+//                   fp32 stores of whole 128-byte row segments.
+// Every mbarrier wait is bounded (about two seconds); a timeout sets an
+// error bit and the CTA skips its remaining work, still waiting (bounded) for
+// issued MMAs and freeing its TMEM.
+#include "rtacx_internal.cuh"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+namespace rtacx {
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int kThreads = 128;
+constexpr uint32_t A_BYTES = BM * BK * 2;
+constexpr uint32_t B_BYTES = BN * BK * 2;
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+constexpr long long kWaitCycles = 4000000000ll;
+
+// Instruction descriptor of tcgen05.mma.kind::f16: D = f32 (bits 4-5 = 1),
+// A = B = bf16 (bits 7-9 = 1, bits 10-12 = 1), both K-major (bits 15, 16 = 0),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false if the CTA aborted or the wait ran out of time.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag)
+{
+    const long long t0 = clock64();
+    while(!mbar_try_wait(bar, parity)) {
+        if(*abort_flag) return false;
+        if(clock64() - t0 > kWaitCycles) { *abort_flag = 1; return false; }
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+                 : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major operand in the 128-byte swizzle
+// layout written by TMA: start address >> 4 (bits 0-13), leading byte offset
+// 16 B (unused for this layout), stride byte offset 1024 B between 8-row
+// groups (bits 32-45), fixed version bits 46-48 = 0b001, swizzle mode 2
+// (128 B) at bits 61-63. The tile base is 1024-byte aligned (base offset 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+                 "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                   "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                   "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_gemm_bf16_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               float* __restrict__ C, int M, int N, int K, int ldc, uint32_t* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
+    const int nkb = K / BK;
+    auto full_bar = [&](int s) { return smem_u32(bars + s); };
+    auto empty_bar = [&](int s) { return smem_u32(bars + STAGES + s); };
+    const uint32_t accum_bar = smem_u32(bars + 2 * STAGES);
+
+    if(threadIdx.x == 0) {
+        for(int s = 0; s < STAGES; s++) { mbar_init(full_bar(s), 1); mbar_init(empty_bar(s), 1); }
+        mbar_init(accum_bar, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    }
+    if(warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if(warp == 0 && lane == 0) {
+        // TMA producer.
+        for(int kb = 0; kb < nkb; kb++) {
+            const int s = kb % STAGES;
+            if(kb >= STAGES && !mbar_wait(empty_bar(s), ((kb / STAGES) - 1) & 1, abort_flag)) break;
+            unsigned char* a = base + s * STAGE_BYTES;
+            mbar_expect_tx(full_bar(s), STAGE_BYTES);
+            tma_load_2d(smem_u32(a), &tmA, kb * BK, m0, full_bar(s));
+            tma_load_2d(smem_u32(a + A_BYTES), &tmB, kb * BK, n0, full_bar(s));
+        }
+    }
+    else if(warp == 1 && lane == 0) {
+        // MMA issuer.
+        for(int kb = 0; kb < nkb; kb++) {
+            const int s = kb % STAGES;
+            if(!mbar_wait(full_bar(s), (kb / STAGES) & 1, abort_flag)) break;
+            tc_fence_after();
+            const uint32_t a = smem_u32(base + s * STAGE_BYTES);
+            const uint64_t ad = smem_desc(a), bd = smem_desc(a + A_BYTES);
+#pragma unroll
+            for(int kk = 0; kk < BK / 16; kk++)   // 32 bytes of K per MMA: +2 in descriptor units
+                umma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
+            umma_commit(empty_bar(s));
+        }
+        umma_commit(accum_bar);   // arrives once every MMA issued above has completed
+    }
+    __syncwarp();
+
+    // Epilogue: TMEM lane quadrant of this warp -> rows m0 + 32 warp + lane.
+    const bool ok = mbar_wait(accum_bar, 0, abort_flag);
+    __syncwarp();
+    tc_fence_after();
+    if(__all_sync(0xffffffffu, ok ? 1 : 0)) {
+        const int row = m0 + warp * 32 + lane;
+        float* crow = C + (size_t)row * ldc + n0;
+#pragma unroll 1
+        for(int c = 0; c < BN / 32; c++) {
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
+            if(row < M && n0 + c * 32 < N) {
+                float4* dst = reinterpret_cast<float4*>(crow + c * 32);
+#pragma unroll
+                for(int q = 0; q < 8; q++)
+                    dst[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                                         __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+            }
+        }
+    }
+    else if(lane == 0 && err) {
+        atomicOr(err, kErrGemmTimeout);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if(warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if(!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+           q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k, uint32_t box_rows)
+{
+    EncodeTiledFn enc = encode_fn();
+    if(!enc) return false;
+    cuuint64_t dims[2] = {k, rows};
+    cuuint64_t strides[1] = {k * 2};
+    cuuint32_t box[2] = {(cuuint32_t)BK, box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+} // namespace
+
+size_t gemm_smem_bytes() { return SMEM_BYTES; }
+
+// C = A * B^T; A [M][K], B [N][K] bf16 (16-byte aligned, row stride K),
+// C [M][ldc] fp32. Shapes must be multiples of the tile (128, 256, 64).
+rtacx_status gemm_bf16_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K,
+                          int ldc, cudaStream_t stream, uint32_t* err)
+{
+    if(M <= 0 || N <= 0 || K <= 0 || M % BM || N % BN || K % BK || ldc < N || ldc % 4) {
+        error = "gemm shape must be multiples of 128 x 256 x 64";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
+    if((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16 || reinterpret_cast<uintptr_t>(C) % 16) {
+        error = "gemm operands must be 16-byte aligned";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
+    CUtensorMap ma, mb;
+    if(!make_map(&ma, A, (uint64_t)M, (uint64_t)K, BM) || !make_map(&mb, B, (uint64_t)N, (uint64_t)K, BN)) {
+        error = "cuTensorMapEncodeTiled failed";
+        return RTACX_ERR_CUDA;
+    }
+    static bool attr = false;
+    if(!attr) {
+        if(cudaFuncSetAttribute(k_gemm_bf16_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) != cudaSuccess) {
+            cudaGetLastError();
+            error = "cannot reserve shared memory for the tensor-core GEMM";
+            return RTACX_ERR_CUDA;
+        }
+        attr = true;
+    }
+    dim3 grid(N / BN, M / BM);
+    k_gemm_bf16_tn<<<grid, kThreads, SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, err);
+    const cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) { error = std::string("k_gemm_bf16_tn: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    return RTACX_OK;
+}
+
+} // namespace rtacx
+
+namespace {
+__device__ uint32_t g_gemm_check_err;
+}
+
+// Diagnostic entry point (include/rtacx.h): synchronous C = A * B^T.
+extern "C" rtacx_status rtacx_gemm_bf16_tn(const void* A, const void* B, float* C, int M, int N, int K, void* stream)
+{
+    std::string error;
+    uint32_t* err = nullptr;
+    if(cudaGetSymbolAddress(reinterpret_cast<void**>(&err), g_gemm_check_err) != cudaSuccess) {
+        cudaGetLastError();
+        return RTACX_ERR_CUDA;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if(cudaMemsetAsync(err, 0, sizeof(uint32_t), s) != cudaSuccess) { cudaGetLastError(); return RTACX_ERR_CUDA; }
+    rtacx_status st = rtacx::gemm_bf16_tn(error, A, B, C, M, N, K, N, s, err);
+    if(st != RTACX_OK) return st;
+    uint32_t word = 0;
+    if(cudaStreamSynchronize(s) != cudaSuccess ||
+       cudaMemcpyFromSymbol(&word, g_gemm_check_err, sizeof(word)) != cudaSuccess) {
+        cudaGetLastError();
+        return RTACX_ERR_CUDA;
+    }
+    return word ? RTACX_ERR_DEVICE : RTACX_OK;
+}

@@ -77,6 +77,13 @@ def pulse_at_bin_spacing(taps: int, res: float, frequency: float, c: float) -> n
     return w.astype(np.complex64)
 
 
+def baseband_pulse(taps: int) -> np.ndarray:
+    """Gaussian pulse envelope (complex baseband, sigma = taps / 6 taps), one
+    tap per range bin: the carrier is carried by each sample's phase."""
+    d = np.arange(taps, dtype=np.float64) - (taps - 1) / 2.0
+    return np.exp(-0.5 * (d / (taps / 6.0)) ** 2).astype(np.complex64)
+
+
 def beam_sinc2(taps: int, span: float, resolution: float, floor: float = 0.0) -> np.ndarray:
     """Sinc-squared beam table (first null at `resolution`), optionally floored."""
     x = texel_centers(taps, span)
@@ -94,6 +101,10 @@ def beam_sinc(span: float, resolution: float, oversampling: int = 8) -> np.ndarr
     return np.sinc(texel_centers(taps, span) / resolution).astype(F32)
 
 
+ECHO_PHASE = 1
+ECHO_SPREADING = 2
+
+
 @dataclass
 class Workload:
     name: str
@@ -101,6 +112,7 @@ class Workload:
     sensor: dict
     samples: np.ndarray               # (N, 3) SimSample1D or (N, 4) SimSample2D, float32
     meta: dict = field(default_factory=dict)
+    echo: dict | None = None          # echo pre-step: {"carrier_hz": f, "flags": ECHO_*}
 
     @property
     def n(self) -> int:
@@ -184,9 +196,11 @@ def oculus_2d(n_samples: int = 1 << 20, seed: int = 2, n_bearings: int = 512, n_
 def precision_2d(n_samples: int = 1 << 24, seed: int = 3, n_bearings: int = 512, n_ranges: int = 4096,
                  rmin: float = 0.3, rmax: float = 120.0, taps: int = 33) -> Workload:
     """Dense-directivity 512-bearing ping at 1.2 MHz: travel ~ U[rmin, rmax],
-    bearing ~ U over the fan, amplitude Rayleigh(1) * r^-2 * random phase;
-    sinc^2 beam floored at -40 dB over the whole fan (every sample reaches
-    every bearing), 33-tap pulse at bin spacing."""
+    bearing ~ U over the fan, reflectivity Rayleigh(1) * random phase; the
+    echo pre-step applies the carrier phase 4 pi f d / c (reduced in FP64)
+    and the r^-2 spreading on the device. Sinc^2 beam floored at -40 dB over
+    the whole fan (every sample reaches every bearing), 33-tap Gaussian
+    baseband pulse envelope at bin spacing (the carrier is in the samples)."""
     c, f = 1500.0, 1.2e6
     res = float(linspace_resolution(rmin, rmax, n_ranges))
     bearings = arcsin_bearings(n_bearings, 130.0)
@@ -194,15 +208,15 @@ def precision_2d(n_samples: int = 1 << 24, seed: int = 3, n_bearings: int = 512,
     beam_res = 0.6 * DEG
     beam_taps = int(math.ceil(span / (beam_res / 8.0))) | 1
     beam = beam_sinc2(beam_taps, span, beam_res, floor=0.01)
-    pulse = pulse_at_bin_spacing(taps, res, f, c)
+    pulse = baseband_pulse(taps)
     rng = np.random.Generator(np.random.PCG64(seed))
     t = rng.uniform(rmin, rmax, n_samples)
     th = rng.uniform(-65.0 * DEG, 65.0 * DEG, n_samples)
     re, im = _rayleigh_phasor(rng, n_samples)
-    re, im = re / t ** 2, im / t ** 2
     return Workload("precision_2d", 2,
                     sensor_2d(rmin, rmax, n_ranges, c, pulse, taps * res, beam, span, bearings),
-                    _pack(re, im, t, th), dict(frequency=f))
+                    _pack(re, im, t, th), dict(frequency=f),
+                    echo=dict(carrier_hz=f, flags=ECHO_PHASE | ECHO_SPREADING))
 
 
 def oculus_reference_2d(n_samples: int = 20000, seed: int = 4, n_bearings: int = 256) -> Workload:
@@ -240,10 +254,83 @@ def ea400_reference_1d(n_samples: int = 20000, seed: int = 5) -> Workload:
     return Workload("ea400_reference_1d", 1, sensor, _pack(re, im, t), dict(frequency=f))
 
 
+def batched_mix(n_pings: int = 64, seed: int = 7, log2_min: float = 14.0, log2_max: float = 22.0) -> list:
+    """Batched mixed-sensor set: `n_pings` pings with log-uniform sample counts
+    in [2^log2_min, 2^log2_max]; 50% 512-bearing 2D (1024 ranges over
+    [0.3, 40] m), 25% 256-bearing 2D (512 ranges over [0.5, 30] m), 25% 1D
+    with 2048 ranges over [0.5, 100] m; per-ping pulses of 17..65 range taps
+    and beams of +/-8..32 bearings."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    kinds = np.array([0] * (n_pings // 2) + [1] * (n_pings // 4) + [2] * (n_pings - n_pings // 2 - n_pings // 4))
+    rng.shuffle(kinds)
+    pings = []
+    for i, kind in enumerate(kinds):
+        n = int(round(2.0 ** rng.uniform(log2_min, log2_max)))
+        taps = int(rng.integers(17, 66))
+        half = int(rng.integers(8, 33))
+        if kind == 0:
+            wk = oculus_2d(n_samples=n, seed=1000 + i, n_bearings=512, n_ranges=1024, rmin=0.3, rmax=40.0,
+                           taps=taps, half_bearings=half)
+        elif kind == 1:
+            wk = oculus_2d(n_samples=n, seed=1000 + i, n_bearings=256, n_ranges=512, rmin=0.5, rmax=30.0,
+                           taps=taps, half_bearings=half, altitude=3.0)
+        else:
+            wk = echosounder_1d(n_samples=n, seed=1000 + i, n_ranges=2048, rmin=0.5, rmax=100.0, taps=taps)
+        wk.name = f"batch{i}_{['2d512', '2d256', '1d2048'][kind]}"
+        pings.append(wk)
+    return pings
+
+
 CONFIGS = {
     "echosounder_1d": echosounder_1d,
     "oculus_2d": oculus_2d,
     "precision_2d": precision_2d,
     "oculus_reference_2d": oculus_reference_2d,
     "ea400_reference_1d": ea400_reference_1d,
+    "batched_mix": batched_mix,
 }
+
+
+def _lerp(table: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """Texture-equivalent lerp with border addressing, exact weights."""
+    n = table.shape[0]
+    fl = np.floor(x)
+    ok = (fl >= -1) & (fl <= n - 1)
+    i = np.where(ok, fl, 0).astype(np.int64)
+    a = x - fl
+    pad = np.concatenate([np.zeros(1, table.dtype), table, np.zeros(1, table.dtype)])
+    lo = pad[np.clip(i + 1, 0, n + 1)]
+    hi = pad[np.clip(i + 2, 0, n + 1)]
+    return np.where(ok, lo * (1 - a) + hi * a, 0)
+
+
+def precision_tables(sensor: dict):
+    """Directivity matrix and range taps of the binned precision model,
+    derived from a 2D sensor's tables exactly as rtacx_configure_precision
+    derives them when given NULL tables: D[k][b] = beam(theta_k - theta_b)
+    (float bearing difference, exact lerp) and taps[t] = pulse(t * resolution)
+    for |t| <= overlap, trimmed to the non-zero span. Returns
+    (D complex64 [nB][nB], taps complex64, centre index)."""
+    bear = np.asarray(sensor["bearings"], np.float32)
+    beam = np.asarray(sensor["beam"], np.float32).astype(np.float64)
+    W = beam.size
+    kx = float(np.float32(1.0) / np.float32(sensor["beam_span"])) * W
+    e = (bear[:, None] - bear[None, :]).astype(np.float32).astype(np.float64)
+    D = _lerp(beam, e * kx + 0.5 * W - 0.5).astype(np.complex64)
+    nR = sensor["range_count"]
+    res = float(linspace_resolution(sensor["range_min"], sensor["range_max"], nR)) if nR > 1 else 0.0
+    mres = np.float32(np.float32(sensor["range_max"]) - np.float32(sensor["range_min"]))
+    margin = np.float32(sensor["margin"])
+    ov = int(np.float32(margin / np.float32(mres / np.float32(nR - 1)))) if nR > 1 else 0
+    ov = max(ov, 0)
+    pulse = np.asarray(sensor["pulse"], np.complex64).astype(np.complex128)
+    H = pulse.size
+    pscale = float(np.float32(1.0) / np.float32(np.float32(sensor["pulse_duration"]) * np.float32(sensor["sound_celerity"])))
+    t = np.arange(-ov, ov + 1)
+    x = t * res * (pscale * H) + 0.5 * H - 0.5
+    full = (_lerp(pulse.real, x) + 1j * _lerp(pulse.imag, x)).astype(np.complex64)
+    nz = np.nonzero(full)[0]
+    if nz.size == 0:
+        return D, np.zeros(1, np.complex64), 0
+    first, last = nz[0], nz[-1]
+    return D, full[first:last + 1], int(ov - first)

@@ -1,0 +1,71 @@
+"""Batched plain form (rtacx_batch_*): every ping of a heterogeneous batch
+equals the single-ping path, and the single-ping path equals the oracle."""
+import numpy as np
+import pytest
+
+from rtac_simulation_gb300 import _lib
+from rtac_simulation_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a GPU", allow_module_level=True)
+
+from helpers_gpu import gpu_reduce, make_context, rel_l2  # noqa: E402
+
+
+def _complex(t):
+    o = t.cpu().numpy()
+    return o[..., 0].astype(np.float64) + 1j * o[..., 1]
+
+
+@pytest.fixture(scope="module")
+def batch_setup():
+    pings = wl.batched_mix(n_pings=12, seed=11, log2_min=10, log2_max=15)
+    ctxs, devs, outs = [], [], []
+    for wk in pings:
+        ctxs.append(make_context(wk))
+        devs.append(torch.from_numpy(wk.samples.reshape(-1)).cuda())
+        outs.append(torch.full(wk.out_shape + (2,), float("nan"), device="cuda"))
+    return pings, ctxs, devs, outs
+
+
+@pytest.mark.parametrize("autotune", [False, True])
+def test_batch_equals_single_ping(batch_setup, autotune):
+    pings, ctxs, devs, outs = batch_setup
+    batch = _lib.Batch(0)
+    batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)], autotune=autotune)
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        for o in outs:
+            o.fill_(float("nan"))
+        batch.run(stream)
+        torch.cuda.synchronize()
+        for wk, o in zip(pings, outs):
+            got = _complex(o)
+            ref_ctx = make_context(wk)
+            want = gpu_reduce(ref_ctx, wk.samples, wk.out_shape)
+            assert np.isfinite(got).all()
+            assert rel_l2(got, want) <= 1e-6, wk.name
+    t = batch.tuning()
+    assert t["tile_rows"] in (16, 32) and t["tile_bearings"] in (64, 128)
+    if autotune:
+        assert t["tuned_ms"] > 0
+
+
+def test_batch_pings_match_oracle(batch_setup, oracle):
+    pings, ctxs, devs, outs = batch_setup
+    batch = _lib.Batch(0)
+    batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)], autotune=False)
+    batch.run(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    for wk, o in list(zip(pings, outs))[:4]:
+        assert rel_l2(_complex(o), oracle.reduce(wk.samples, wk.sensor)) <= 1e-5, wk.name
+
+
+def test_batch_rejects_shared_context(batch_setup):
+    pings, ctxs, devs, outs = batch_setup
+    batch = _lib.Batch(0)
+    with pytest.raises(_lib.RtacxError):
+        batch.plan([(ctxs[0], devs[0], pings[0].n, outs[0]), (ctxs[0], devs[0], pings[0].n, outs[0])])

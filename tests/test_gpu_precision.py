@@ -1,0 +1,108 @@
+"""Precision (tensor-core) form against the FP64 oracle of the binned model
+at <= 1e-4 relative L2, the FP64 echo pre-step of the plain form at 1e-5, and
+the model difference between the two forms (reported, not a parity bar)."""
+import numpy as np
+import pytest
+
+from rtac_simulation_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a GPU", allow_module_level=True)
+
+from helpers_gpu import gpu_reduce, make_context, rel_l2, to_device  # noqa: E402
+
+TOL = 1e-4
+
+
+def gpu_precision(ctx, samples, out_shape):
+    d = to_device(samples)
+    out = torch.full(tuple(out_shape) + (2,), float("nan"), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    ctx.reduce_precision(d, samples.shape[0], out, stream=stream)
+    ctx.stream_status(stream)
+    o = out.cpu().numpy()
+    return o[..., 0].astype(np.float64) + 1j * o[..., 1]
+
+
+def precision_context(wk, explicit=True):
+    ctx = make_context(wk)
+    if wk.echo:
+        ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    if explicit:
+        D, taps, c = wl.precision_tables(wk.sensor)
+        ctx.configure_precision(D, taps, c)
+    else:
+        ctx.configure_precision()
+    return ctx
+
+
+@pytest.mark.parametrize("maker", [
+    lambda: wl.precision_2d(n_samples=1 << 16, n_bearings=128, n_ranges=512),
+    lambda: wl.precision_2d(n_samples=1 << 18, n_ranges=1024),
+    lambda: wl.precision_2d(n_samples=1 << 14, n_bearings=100, n_ranges=300),
+    lambda: wl.oculus_2d(n_samples=1 << 16, n_ranges=256, n_bearings=256),
+])
+def test_precision_matches_binned_fp64_oracle(oracle, maker):
+    wk = maker()
+    ctx = precision_context(wk)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    smp = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
+    want = oracle.reduce_binned(smp, wk.sensor, D, taps, c)
+    assert np.isfinite(got).all()
+    err = rel_l2(got, want)
+    assert err <= TOL, err
+
+
+def test_precision_full_size_rows(oracle):
+    wk = wl.precision_2d()
+    ctx = precision_context(wk)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    smp = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
+    rows = (1000, 1064)
+    want = oracle.reduce_binned(smp, wk.sensor, D, taps, c, rows=rows)
+    assert rel_l2(got[rows[0]:rows[1]], want) <= TOL
+    assert rel_l2(got[:64], oracle.reduce_binned(smp, wk.sensor, D, taps, c, rows=(0, 64))) <= TOL
+
+
+def test_precision_derived_tables_match_explicit():
+    wk = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512)
+    a = gpu_precision(precision_context(wk, explicit=True), wk.samples, wk.out_shape)
+    b = gpu_precision(precision_context(wk, explicit=False), wk.samples, wk.out_shape)
+    assert rel_l2(b, a) <= 1e-6
+
+
+def test_precision_unaligned_shape_uses_copy_out(oracle):
+    wk = wl.precision_2d(n_samples=1 << 14, n_bearings=77, n_ranges=130)
+    ctx = precision_context(wk)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    assert rel_l2(got, want) <= TOL
+
+
+def test_plain_form_with_fp64_echo(oracle):
+    wk = wl.precision_2d(n_samples=1 << 14, n_ranges=1024)
+    ctx = make_context(wk)
+    ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    got = gpu_reduce(ctx, wk.samples, wk.out_shape)
+    want = oracle.reduce(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor)
+    assert rel_l2(got, want) <= 1e-5
+
+
+def test_precision_vs_plain_model_difference(oracle):
+    # The binned model is not the per-sample PSF: report how far apart the
+    # two forms are on the same ping (bounded loosely, not a parity bar).
+    wk = wl.precision_2d(n_samples=1 << 16, n_ranges=1024)
+    ctx = precision_context(wk)
+    prec = gpu_precision(ctx, wk.samples, wk.out_shape)
+    ctx2 = make_context(wk)
+    ctx2.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    plain = gpu_reduce(ctx2, wk.samples, wk.out_shape)
+    diff = rel_l2(prec, plain)
+    print(f"binned vs per-sample model: rel-L2 {diff:.3e}")
+    assert diff < 1.5
