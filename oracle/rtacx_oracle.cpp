@@ -258,19 +258,38 @@ void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void*
             float d = s.travel - R;
             u[i] = std::complex<double>(s.re, s.im) * lerp_border(pulse_d.data(), H, (double)d * ky + cy);
         }
-        for(uint32_t b = 0; b < nB; b++) {
-            std::complex<double> acc(0.0, 0.0);
-            if(S.dims == 2) {
-                const float th = S.bearings[b];
-                for(uint32_t i = 0; i < size; i++) {
-                    float e = B.sorted[off + i].bearing - th;
-                    acc += u[i] * lerp_border(beam_d.data(), W, (double)e * kx + cx);
+        bool sorted_bearings = S.dims == 2;
+        for(uint32_t b = 1; sorted_bearings && b < nB; b++) sorted_bearings = S.bearings[b] > S.bearings[b - 1];
+        if(S.dims == 2 && sorted_bearings) {
+            // Only bearings inside the beam support can receive a non-zero
+            // weight (|e| < span/2 (1 + 1/W)); visit a superset of them.
+            for(uint32_t b = 0; b < nB; b++) o[b] = std::complex<double>(0.0, 0.0);
+            const double hs = 0.5 / (double)S.beam_scale * (1.0 + 1.0 / W) * (1.0 + 1e-6) + 1e-9;
+            for(uint32_t i = 0; i < size; i++) {
+                const float th_s = B.sorted[off + i].bearing;
+                const float* lo = std::lower_bound(S.bearings, S.bearings + nB, (float)((double)th_s - hs));
+                const float* hi = std::upper_bound(S.bearings, S.bearings + nB, (float)((double)th_s + hs));
+                for(const float* q = lo; q < hi; q++) {
+                    const float e = th_s - *q;
+                    o[q - S.bearings] += u[i] * lerp_border(beam_d.data(), W, (double)e * kx + cx);
                 }
             }
-            else {
-                for(uint32_t i = 0; i < size; i++) acc += u[i];
+        }
+        else {
+            for(uint32_t b = 0; b < nB; b++) {
+                std::complex<double> acc(0.0, 0.0);
+                if(S.dims == 2) {
+                    const float th = S.bearings[b];
+                    for(uint32_t i = 0; i < size; i++) {
+                        float e = B.sorted[off + i].bearing - th;
+                        acc += u[i] * lerp_border(beam_d.data(), W, (double)e * kx + cx);
+                    }
+                }
+                else {
+                    for(uint32_t i = 0; i < size; i++) acc += u[i];
+                }
+                o[b] = acc;
             }
-            o[b] = acc;
         }
     }
     else {

@@ -37,6 +37,7 @@ void free_config(Context& c)
     free_dev(c.d_support); free_dev(c.d_bb_tiles64); free_dev(c.d_bb_tiles128); c.d_bb_tiles = nullptr;
     free_dev(c.d_offsets); free_dev(c.d_totals);
     free_dev(c.d_win); free_dev(c.d_hist);
+    free_dev(c.d_tile_parts); free_dev(c.d_tile_first); free_dev(c.d_items); free_dev(c.d_item_counter);
     c.hist_cols = 0;
     c.configured = false;
 }
@@ -299,6 +300,12 @@ rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* s)
        !upload(c, c.d_bb_tiles128, bbt128.data(), bbt128.size()) || !allocate_bins(c))
         return RTACX_ERR_OUT_OF_MEMORY;
     c.d_bb_tiles = (c.bearing_tile == 64) ? c.d_bb_tiles64 : c.d_bb_tiles128;
+    {
+        const uint64_t tiles = (uint64_t)((c.nB + c.bearing_tile - 1) / c.bearing_tile) * ((c.nR + c.range_tile - 1) / c.range_tile);
+        if(!upload<uint32_t>(c, c.d_tile_parts, nullptr, tiles) || !upload<uint32_t>(c, c.d_tile_first, nullptr, tiles + 1) ||
+           !upload<uint4>(c, c.d_items, nullptr, tiles * 256) || !upload<uint32_t>(c, c.d_item_counter, nullptr, 1))
+            return RTACX_ERR_OUT_OF_MEMORY;
+    }
     c.configured = true;
     return RTACX_OK;
 }

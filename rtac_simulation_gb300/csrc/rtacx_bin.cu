@@ -479,6 +479,12 @@ rtacx_status launch_bin_batch(std::string& error, const PingDev* pings, uint32_t
     return RTACX_OK;
 }
 
+// Exclusive scan of n u32 values into out[0, n] (out[n] = total), one CTA.
+void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t stream)
+{
+    k_binscan<<<1, kScanThreads, 0, stream>>>(in, n, out);
+}
+
 // Launch shape of the count / scatter passes for the configured bin count.
 void configure_hist_launch(Context& ctx)
 {

@@ -55,6 +55,11 @@ __device__ __forceinline__ float2 lerp_cplx(const float2* tab, const AxisLerp& a
     return make_float2(fmaf(alpha, hi.x - lo.x, lo.x), fmaf(alpha, hi.y - lo.y, lo.y));
 }
 
+__device__ __forceinline__ void red_add_v2(float2* addr, float2 v)
+{
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(v.x), "f"(v.y) : "memory");
+}
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
@@ -83,7 +88,9 @@ __device__ __forceinline__ void gather_tile_2d(const float4* __restrict__ sorted
                                                const float* __restrict__ ranges, const float* __restrict__ bearings,
                                                const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
                                                const ReduceParams& rp, uint32_t nBB, float2* __restrict__ out,
-                                               int tile_b, int tile_r, unsigned char* smem_raw)
+                                               int tile_b, int tile_r, unsigned char* smem_raw,
+                                               uint32_t g_begin = 0u, uint32_t g_end = 0xFFFFFFFFu,
+                                               bool atomic_out = false)
 {
     constexpr int RPW = TR / kWarps;   // rows per warp
     constexpr int BPL = TB / 32;       // bearings per lane
@@ -132,7 +139,11 @@ __device__ __forceinline__ void gather_tile_2d(const float4* __restrict__ sorted
 
     const int jmin = S.jmin, jmax = S.jmax;
     const int2 kb = bb_tiles[tile_b];
-    for(int jg = jmin; jg <= jmax; jg += kThreads) {
+    // The tile's samples form one stream: the bearing-bin segments of range
+    // bins jmin..jmax in order. This call reduces stream positions
+    // [g_begin, g_end); `base` is the stream position of the current group.
+    uint32_t base = 0;
+    for(int jg = jmin; jg <= jmax && base < g_end; jg += kThreads) {
         // Segment of bin (jg + tid) restricted to this tile's bearing bins.
         const int j = jg + tid;
         uint32_t start = 0, len = 0;
@@ -159,8 +170,11 @@ __device__ __forceinline__ void gather_tile_2d(const float4* __restrict__ sorted
         if(tid == 0) S.seg_pre[kThreads] = total;
         __syncthreads();
 
-        for(uint32_t c0 = 0; c0 < total; c0 += kChunk) {
-            const int valid = (int)((total - c0) < (uint32_t)kChunk ? (total - c0) : (uint32_t)kChunk);
+        const uint32_t lo = g_begin > base ? min(g_begin - base, total) : 0u;
+        const uint32_t hi = (g_end - base < total) ? g_end - base : total;
+        base += total;
+        for(uint32_t c0 = lo; c0 < hi; c0 += kChunk) {
+            const int valid = (int)((hi - c0) < (uint32_t)kChunk ? (hi - c0) : (uint32_t)kChunk);
             if(tid < kChunk) {
                 if(tid < valid) {
                     const uint32_t g = c0 + tid;
@@ -224,7 +238,9 @@ __device__ __forceinline__ void gather_tile_2d(const float4* __restrict__ sorted
 #pragma unroll
         for(int c = 0; c < BPL; c++) {
             const int b = b0 + lane * BPL + c;
-            if(b < nB) out[(size_t)r * nB + b] = acc[q][c];
+            if(b >= nB) continue;
+            if(atomic_out) red_add_v2(out + (size_t)r * nB + b, acc[q][c]);
+            else out[(size_t)r * nB + b] = acc[q][c];
         }
     }
 }
@@ -283,6 +299,95 @@ k_gather_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
     gather_rows_1d(sorted, off, win, ranges, s_pulse, rp, out, blockIdx.x * kWarps);
 }
 
+// ---- split persistent gather of one 2D ping -------------------------------
+// k_tile_parts counts each output tile's sample stream (same definition as
+// gather_tile_2d) and splits it into parts of at most kPartSamples samples
+// (at most kMaxParts); k_tile_items writes one work item per part; the
+// persistent kernel reduces the parts, accumulating into the zeroed ping with
+// vector atomics. Tiles whose windows hold hot bins are spread over many CTAs.
+constexpr uint32_t kPartSamples = 16384;
+constexpr uint32_t kMaxParts = 256;
+
+template <int TR>
+__global__ void k_tile_parts(const uint32_t* __restrict__ off, const int2* __restrict__ win,
+                             const int2* __restrict__ bb_tiles, uint32_t nR, uint32_t nBB, uint32_t tiles_b,
+                             uint32_t tiles, uint32_t* __restrict__ parts)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if(t >= tiles) return;
+    const uint32_t tb = t % tiles_b, tr = t / tiles_b;
+    int jmin = INT_MAX, jmax = INT_MIN;
+    for(int q = 0; q < TR; q++) {
+        const int r = (int)tr * TR + q;
+        if(r >= (int)nR) break;
+        const int2 w = win[r];
+        if(w.x <= w.y) { jmin = min(jmin, w.x); jmax = max(jmax, w.y); }
+    }
+    uint64_t count = 0;
+    const int2 kb = bb_tiles[tb];
+    for(int j = jmin; j <= jmax; j++)
+        count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
+    const uint64_t np = (count + kPartSamples - 1) / kPartSamples;
+    parts[t] = (uint32_t)(np < kMaxParts ? np : kMaxParts);
+}
+
+__global__ void k_tile_items(const uint32_t* __restrict__ parts, const uint32_t* __restrict__ first,
+                             uint32_t tiles_b, uint32_t tiles, uint4* __restrict__ items)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if(t >= tiles) return;
+    const uint32_t np = parts[t], f = first[t];
+    for(uint32_t p = 0; p < np; p++) items[f + p] = make_uint4(t % tiles_b, t / tiles_b, p, np);
+}
+
+template <int TR, int TB>
+__global__ void __launch_bounds__(kThreads)
+k_gather_split(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+               const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
+               const float* __restrict__ ranges, const float* __restrict__ bearings,
+               const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
+               ReduceParams rp, uint32_t nBB, float2* __restrict__ out,
+               const uint4* __restrict__ items, const uint32_t* __restrict__ n_items_ptr,
+               uint32_t* __restrict__ counter)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_item;
+    __shared__ uint64_t s_count;
+    const uint32_t n_items = *n_items_ptr;
+    for(;;) {
+        if(threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if(it >= n_items) break;
+        const uint4 item = items[it];
+        uint32_t g0 = 0, g1 = 0xFFFFFFFFu;
+        if(item.w > 1) {
+            // Stream length of this tile, then this part's share of it.
+            if(threadIdx.x == 0) {
+                int jmin = INT_MAX, jmax = INT_MIN;
+                for(int q = 0; q < TR; q++) {
+                    const int r = (int)item.y * TR + q;
+                    if(r >= (int)rp.nR) break;
+                    const int2 w = win[r];
+                    if(w.x <= w.y) { jmin = min(jmin, w.x); jmax = max(jmax, w.y); }
+                }
+                const int2 kb = bb_tiles[item.x];
+                uint64_t count = 0;
+                for(int j = jmin; j <= jmax; j++)
+                    count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
+                s_count = count;
+            }
+            __syncthreads();
+            const uint64_t count = s_count;
+            g0 = (uint32_t)(count * item.z / item.w);
+            g1 = (uint32_t)(count * (item.z + 1) / item.w);
+        }
+        gather_tile_2d<TR, TB>(sorted, off, win, bb_tiles, ranges, bearings, pulse_pad, beam_pad, rp, nBB, out,
+                               (int)item.x, (int)item.y, smem_raw, g0, g1, true);
+        __syncthreads();
+    }
+}
+
 // Persistent batched gather: each CTA takes work items from a global counter
 // (one atomicAdd per item, no waiting) until the list is exhausted. Items are
 // 2D tiles {ping, tile_b, tile_r, 0} or 1D row groups {ping, group, 0, 1}.
@@ -329,11 +434,40 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
         configured = smem;
     }
     dim3 grid((ctx.nB + TB - 1) / TB, (ctx.nR + TR - 1) / TR);
-    k_gather_2d<TR, TB><<<grid, kThreads, smem, stream>>>(ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles,
-                                                          ctx.d_ranges, ctx.d_bearings, ctx.d_pulse, ctx.d_beam,
-                                                          ctx.red, ctx.bin.nBB, out);
+    if(!ctx.d_tile_parts) {
+        // One CTA per tile (contexts without split scratch).
+        k_gather_2d<TR, TB><<<grid, kThreads, smem, stream>>>(ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles,
+                                                              ctx.d_ranges, ctx.d_bearings, ctx.d_pulse, ctx.d_beam,
+                                                              ctx.red, ctx.bin.nBB, out);
+        const cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess) { ctx.error = std::string("k_gather_2d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+        return RTACX_OK;
+    }
+    static thread_local size_t split_configured = 0;
+    if(smem > split_configured) {
+        if(cudaFuncSetAttribute(k_gather_split<TR, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            ctx.error = "PSF tables too large for shared memory";
+            return RTACX_ERR_UNSUPPORTED;
+        }
+        split_configured = smem;
+    }
+    const uint32_t tiles = grid.x * grid.y;
+    k_tile_parts<TR><<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles, ctx.nR,
+                                                               ctx.bin.nBB, grid.x, tiles, ctx.d_tile_parts);
+    scan_u32(ctx.d_tile_parts, tiles, ctx.d_tile_first, stream);   // d_tile_first[tiles] = item count
+    k_tile_items<<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_tile_parts, ctx.d_tile_first, grid.x, tiles,
+                                                          ctx.d_items);
+    cudaMemsetAsync(ctx.d_item_counter, 0, sizeof(uint32_t), stream);
+    cudaMemsetAsync(out, 0, (size_t)ctx.nR * ctx.nB * sizeof(float2), stream);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather_split<TR, TB>, kThreads, smem);
+    per_sm = std::max(1, per_sm);
+    k_gather_split<TR, TB><<<ctx.sm_count * per_sm, kThreads, smem, stream>>>(
+        ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles, ctx.d_ranges, ctx.d_bearings, ctx.d_pulse,
+        ctx.d_beam, ctx.red, ctx.bin.nBB, out, ctx.d_items, ctx.d_tile_first + tiles, ctx.d_item_counter);
     const cudaError_t e = cudaGetLastError();
-    if(e != cudaSuccess) { ctx.error = std::string("k_gather_2d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    if(e != cudaSuccess) { ctx.error = std::string("k_gather_split: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;
 }
 

@@ -254,6 +254,43 @@ def ea400_reference_1d(n_samples: int = 20000, seed: int = 5) -> Workload:
     return Workload("ea400_reference_1d", 1, sensor, _pack(re, im, t), dict(frequency=f))
 
 
+def stress_2d(n_samples: int = 1 << 27, seed: int = 5, n_bearings: int = 1024, n_ranges: int = 8192,
+              rmin: float = 0.5, rmax: float = 100.0, taps: int = 33, half_bearings: int = 16,
+              cluster_fraction: float = 0.5) -> Workload:
+    """Contention stress ping: 1024 arcsin bearings x 8192 ranges, 2^27
+    samples. `cluster_fraction` of them form a wreck-like target, Gaussian in
+    range (sigma 0.25 m at 40 m, so ~1% of the range bins hold it) and in
+    bearing (sigma 3 deg at +10 deg); the rest lie on a flat seafloor at 8 m
+    altitude. Rayleigh reflectivity with the 1.2 MHz echo pre-step; 33-tap
+    baseband pulse x sinc^2 beam truncated to +/-16 bearings."""
+    c, f = 1500.0, 1.2e6
+    bearings = arcsin_bearings(n_bearings, 130.0)
+    spacing = 130.0 * DEG / (n_bearings - 1)
+    span = (2 * half_bearings + 1) * spacing
+    beam = beam_sinc2(8 * (2 * half_bearings + 1) + 1, span, 0.6 * DEG)
+    res = float(linspace_resolution(rmin, rmax, n_ranges))
+    pulse = baseband_pulse(taps)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nc = int(n_samples * cluster_fraction)
+    out = np.empty((n_samples, 4), dtype=F32)
+    # cluster
+    out[:nc, 2] = rng.normal(40.0, 0.25, nc)
+    out[:nc, 3] = rng.normal(10.0 * DEG, 3.0 * DEG, nc)
+    # seafloor
+    ns = n_samples - nc
+    out[nc:, 3] = rng.uniform(-65.0 * DEG, 65.0 * DEG, ns)
+    out[nc:, 2] = 8.0 / rng.uniform(8.0 / rmax, 1.0, ns)
+    a = rng.rayleigh(1.0, n_samples).astype(F32)
+    ph = rng.uniform(0.0, 2.0 * math.pi, n_samples).astype(F32)
+    out[:, 0] = a * np.cos(ph)
+    out[:, 1] = a * np.sin(ph)
+    perm = rng.permutation(n_samples)
+    out = out[perm]
+    return Workload("stress_2d", 2, sensor_2d(rmin, rmax, n_ranges, c, pulse, taps * res, beam, span, bearings),
+                    out, dict(frequency=f, cluster_fraction=cluster_fraction),
+                    echo=dict(carrier_hz=f, flags=ECHO_PHASE | ECHO_SPREADING))
+
+
 def batched_mix(n_pings: int = 64, seed: int = 7, log2_min: float = 14.0, log2_max: float = 22.0) -> list:
     """Batched mixed-sensor set: `n_pings` pings with log-uniform sample counts
     in [2^log2_min, 2^log2_max]; 50% 512-bearing 2D (1024 ranges over
@@ -288,6 +325,7 @@ CONFIGS = {
     "oculus_reference_2d": oculus_reference_2d,
     "ea400_reference_1d": ea400_reference_1d,
     "batched_mix": batched_mix,
+    "stress_2d": stress_2d,
 }
 
 
