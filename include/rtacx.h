@@ -182,6 +182,44 @@ rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_des
 rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n,
                                     float* out, void* stream);
 
+/* Echo-sample epilogue (no counterpart in this path of the reference: it
+ * restates the ray generator's and receiver's per-hit arithmetic,
+ * src/RayCaster.cu:49-81 and include/rtac_simulation/Receiver.h:51-60, so
+ * that sample buffers can be produced on the device from hit lists without
+ * OptiX). Per hit: distance < 1e-4 gives a null sample (value 0, travel -1);
+ * otherwise value *= exp(i 4 pi f d / c) / d^2 (per `flags`, carrier phase
+ * reduced in FP64), localDir = R^T dir, value *= directivity(atan2(ly, lx) /
+ * pi, atan2(lz, lx) / pi) (float table, normalized coordinates, bilinear,
+ * mirror addressing, include/rtac_simulation/Directivity.h:30-34), bearing =
+ * atan2(-ly, lx) (Sample.h:150). Writes 12-byte or 16-byte sample records for
+ * the configured 1D / 2D sensor (its sound_celerity). */
+typedef struct {
+    float re, im;            /* complex value reaching the receiver          */
+    float distance;          /* travel (m)                                   */
+    float dir_x, dir_y, dir_z; /* ray direction, world frame                 */
+} rtacx_echo;
+typedef struct {
+    float rotation[9];       /* receiver pose rotation R, row-major           */
+    const float* directivity;/* host [height][width] table, NULL = uniform 1  */
+    uint32_t directivity_width;
+    uint32_t directivity_height;
+    double carrier_hz;
+    uint32_t flags;          /* RTACX_ECHO_PHASE | RTACX_ECHO_SPREADING        */
+} rtacx_receiver;
+rtacx_status rtacx_configure_receiver(rtacx_ctx* ctx, const rtacx_receiver* receiver);
+rtacx_status rtacx_make_samples(rtacx_ctx* ctx, const rtacx_echo* hits, uint64_t n, void* samples, void* stream);
+
+/* Receiver directivity tables of Directivity::rectangle_antenna and
+ * Directivity::disk_antenna (src/Directivity.cpp:147-254), built on the
+ * device. params: rectangle {width, height, wavelength, baffle, oversampling},
+ * disk {diameter, wavelength, baffle, oversampling} (baffle 0 none, 1
+ * single-sided; lengths in one unit). Writes the table size; with out != NULL
+ * also the row-major [height][width] float table (device). */
+#define RTACX_DIRECTIVITY_RECTANGLE 1
+#define RTACX_DIRECTIVITY_DISK      2
+rtacx_status rtacx_directivity_table(int kind, const float* params, float* out, uint32_t* width,
+                                     uint32_t* height, void* stream);
+
 /* Batched plain form: many pings from heterogeneous sensors (each bound to
  * its own configured 1D or 2D context, whose scratch it uses) in one CUDA
  * graph: one launch per binning stage covering every ping, then one

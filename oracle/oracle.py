@@ -61,6 +61,8 @@ def load() -> ctypes.CDLL:
     lib.rtacx_oracle_reduce_binned.argtypes = [_P, _U64, _F, _F, _U32, _F, _P, _U32, _P, _P, _U32, _U32,
                                                _U32, _U32, _I, _P]
     lib.rtacx_oracle_reduce_binned.restype = None
+    lib.rtacx_oracle_make_samples.argtypes = [_P, _U64, _P, _P, _U32, _U32, ctypes.c_double, _F, _U32, _U32, _P]
+    lib.rtacx_oracle_make_samples.restype = None
     _lib = lib
     return lib
 
@@ -181,4 +183,17 @@ def reduce_binned(samples: np.ndarray, sensor: dict, directivity: np.ndarray, ta
                                    sensor["margin"], bear.ctypes.data, bear.size, D.ctypes.data,
                                    t.ctypes.data, t.size, tap_center, r0, r1,
                                    threads or (os.cpu_count() or 1), out.ctypes.data)
+    return out
+
+
+def make_samples(hits: np.ndarray, rotation, table, carrier_hz: float, c: float, flags: int, dims: int) -> np.ndarray:
+    """Oracle of rtacx_make_samples: hits (n, 6) float32 -> samples (n, 3|4)."""
+    h = np.ascontiguousarray(hits, dtype=np.float32)
+    R = np.ascontiguousarray(np.asarray(rotation, np.float32).reshape(9))
+    tab = None if table is None else np.ascontiguousarray(table, dtype=np.float32)
+    out = np.zeros((h.shape[0], 4 if dims == 2 else 3), dtype=np.float32)
+    load().rtacx_oracle_make_samples(h.ctypes.data, h.shape[0], R.ctypes.data,
+                                     None if tab is None else tab.ctypes.data,
+                                     0 if tab is None else tab.shape[1], 0 if tab is None else tab.shape[0],
+                                     carrier_hz, c, flags, dims, out.ctypes.data)
     return out

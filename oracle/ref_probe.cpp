@@ -11,6 +11,9 @@
 //        conversion is undefined there, the device one saturates)
 //   WAVE frequency duration oversampling
 //     -> WAVE size re_0 im_0 .. re_{size-1} im_{size-1}
+//   RECT width height wavelength baffle oversampling   (Directivity::rectangle_antenna)
+//   DISK diameter wavelength baffle oversampling        (Directivity::disk_antenna)
+//     -> DIR width height v_0 .. v_{w*h-1}   (row-major [h][w]; baffle: none | single-sided)
 // Floats on input are parsed with strtof (hex or decimal); output uses %a.
 #include <cstdio>
 #include <cstdlib>
@@ -22,6 +25,7 @@
 
 #include <rtac_simulation/Binner.h>
 #include <rtac_simulation/Waveform.h>
+#include <rtac_simulation/Directivity.h>
 
 using rtac::simulation::Binner;
 using rtac::simulation::SimSample1D;
@@ -65,6 +69,27 @@ int main()
                 auto v = (*w)[i];
                 std::printf(" %a %a", v.real(), v.imag());
             }
+            std::printf("\n");
+        }
+        else if(cmd == "RECT" || cmd == "DISK") {
+            std::string tok, baffle;
+            rtac::simulation::Directivity::Ptr d;
+            if(cmd == "RECT") {
+                in >> tok; float w = parse_f(tok);
+                in >> tok; float h = parse_f(tok);
+                in >> tok; float l = parse_f(tok);
+                in >> baffle; unsigned int os; in >> os;
+                d = rtac::simulation::Directivity::rectangle_antenna(w, h, l, baffle, os);
+            }
+            else {
+                in >> tok; float dia = parse_f(tok);
+                in >> tok; float l = parse_f(tok);
+                in >> baffle; unsigned int os; in >> os;
+                d = rtac::simulation::Directivity::disk_antenna(dia, l, baffle, os);
+            }
+            const auto& t = d->texture();
+            std::printf("DIR %u %u", t.width, t.height);
+            for(float v : t.image) std::printf(" %a", v);
             std::printf("\n");
         }
         std::fflush(stdout);

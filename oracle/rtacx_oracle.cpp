@@ -523,4 +523,46 @@ void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, fl
     });
 }
 
+// Echo-sample epilogue (see rtacx_make_samples): hits are n x 6 floats
+// {re, im, distance, dir_x, dir_y, dir_z}; R row-major; table [h][w] (or
+// w = 0 for uniform); out: n x (dims == 2 ? 4 : 3). Exact arithmetic after
+// the float inputs: FP64 phase and exact bilinear weights with mirror
+// addressing on normalized coordinates.
+void rtacx_oracle_make_samples(const float* hits, uint64_t n, const float* R, const float* tab, uint32_t w,
+                               uint32_t h, double carrier_hz, float c, uint32_t flags, uint32_t dims, float* out)
+{
+    const double pi = 3.14159265358979323846;
+    auto mirror = [](double u) { double t = u - 2.0 * std::floor(0.5 * u); return t <= 1.0 ? t : 2.0 - t; };
+    auto midx = [](long long i, long long n_) { if(i < 0) return std::min(-i - 1, n_ - 1); if(i >= n_) return std::max(2 * n_ - i - 1, 0ll); return i; };
+    for(uint64_t i = 0; i < n; i++) {
+        const float* e = hits + 6 * i;
+        float* o = out + (dims == 2 ? 4 : 3) * i;
+        const double d = e[2];
+        if(!(e[2] >= 1.0e-4f)) {
+            o[0] = 0.0f; o[1] = 0.0f; o[2] = -1.0f; if(dims == 2) o[3] = 0.0f;
+            continue;
+        }
+        std::complex<double> v(e[0], e[1]);
+        if(flags & 1u) {
+            const double cyc = d * (2.0 * carrier_hz / (double)c);
+            const double ph = 2.0 * pi * (cyc - std::nearbyint(cyc));
+            v *= std::complex<double>(std::cos(ph), std::sin(ph));
+        }
+        if(flags & 2u) v /= d * d;
+        const double lx = (double)R[0] * e[3] + (double)R[3] * e[4] + (double)R[6] * e[5];
+        const double ly = (double)R[1] * e[3] + (double)R[4] * e[4] + (double)R[7] * e[5];
+        const double lz = (double)R[2] * e[3] + (double)R[5] * e[4] + (double)R[8] * e[5];
+        if(w > 0) {
+            const double x = mirror(std::atan2(ly, lx) / pi) * w - 0.5, y = mirror(std::atan2(lz, lx) / pi) * h - 0.5;
+            const double fx = std::floor(x), fy = std::floor(y), ax = x - fx, ay = y - fy;
+            const long long x0 = midx((long long)fx, w), x1 = midx((long long)fx + 1, w);
+            const long long y0 = midx((long long)fy, h), y1 = midx((long long)fy + 1, h);
+            const double t00 = tab[y0 * w + x0], t01 = tab[y0 * w + x1], t10 = tab[y1 * w + x0], t11 = tab[y1 * w + x1];
+            v *= (1 - ay) * ((1 - ax) * t00 + ax * t01) + ay * ((1 - ax) * t10 + ax * t11);
+        }
+        o[0] = (float)v.real(); o[1] = (float)v.imag(); o[2] = e[2];
+        if(dims == 2) o[3] = (float)std::atan2(-ly, lx);
+    }
+}
+
 } // extern "C"

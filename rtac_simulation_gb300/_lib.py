@@ -75,6 +75,10 @@ SIGNATURES = {
     "rtacx_set_echo_model": (_I, [_P, _P]),
     "rtacx_configure_precision": (_I, [_P, _P]),
     "rtacx_reduce_precision": (_I, [_P, _P, _U64, _P, _P]),
+    "rtacx_configure_receiver": (_I, [_P, _P]),
+    "rtacx_make_samples": (_I, [_P, _P, _U64, _P, _P]),
+    "rtacx_directivity_table": (_I, [_I, ctypes.POINTER(ctypes.c_float), _P, ctypes.POINTER(_U32),
+                                     ctypes.POINTER(_U32), _P]),
     "rtacx_batch_create": (_I, [ctypes.POINTER(_P), _I]),
     "rtacx_batch_destroy": (None, [_P]),
     "rtacx_batch_last_error": (ctypes.c_char_p, [_P]),
@@ -85,6 +89,30 @@ SIGNATURES = {
 }
 
 RTACX_BATCH_AUTOTUNE = 1
+RTACX_DIRECTIVITY_RECTANGLE = 1
+RTACX_DIRECTIVITY_DISK = 2
+
+
+class Receiver(ctypes.Structure):
+    _fields_ = [("rotation", ctypes.c_float * 9), ("directivity", _P), ("directivity_width", _U32),
+                ("directivity_height", _U32), ("carrier_hz", ctypes.c_double), ("flags", _U32)]
+
+
+def directivity_table(kind: int, params, stream=None):
+    """Device directivity table (torch tensor [height][width]) built by
+    rtacx_directivity_table."""
+    import torch
+    lib = load()
+    p = (ctypes.c_float * len(params))(*params)
+    w, h = _U32(), _U32()
+    st = lib.rtacx_directivity_table(kind, p, None, ctypes.byref(w), ctypes.byref(h), None)
+    if st != RTACX_OK:
+        raise RtacxError(st, "rtacx_directivity_table (size) failed")
+    out = torch.empty((h.value, w.value), dtype=torch.float32, device="cuda")
+    st = lib.rtacx_directivity_table(kind, p, out.data_ptr(), ctypes.byref(w), ctypes.byref(h), _stream(stream))
+    if st != RTACX_OK:
+        raise RtacxError(st, "rtacx_directivity_table failed")
+    return out
 
 
 class PingDesc(ctypes.Structure):
@@ -233,6 +261,16 @@ class Context:
 
     def reduce_precision(self, samples, n: int, out, stream=None) -> None:
         self._check(self._lib.rtacx_reduce_precision(self._h, _ptr(samples), n, _ptr(out), _stream(stream)))
+
+    def configure_receiver(self, rotation=None, directivity=None, carrier_hz: float = 0.0, flags: int = 0) -> None:
+        R = np.eye(3, dtype=np.float32) if rotation is None else np.asarray(rotation, np.float32).reshape(3, 3)
+        tab = None if directivity is None else np.ascontiguousarray(np.asarray(directivity, np.float32))
+        r = Receiver((ctypes.c_float * 9)(*R.reshape(-1).tolist()), None if tab is None else tab.ctypes.data,
+                     0 if tab is None else tab.shape[1], 0 if tab is None else tab.shape[0], carrier_hz, flags)
+        self._check(self._lib.rtacx_configure_receiver(self._h, ctypes.byref(r)))
+
+    def make_samples(self, hits, n: int, samples, stream=None) -> None:
+        self._check(self._lib.rtacx_make_samples(self._h, _ptr(hits), n, _ptr(samples), _stream(stream)))
 
     def set_tracing(self, enable: bool) -> None:
         self._check(self._lib.rtacx_set_tracing(self._h, 1 if enable else 0))

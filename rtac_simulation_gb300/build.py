@@ -70,5 +70,23 @@ def build_library(verbose: bool = False, ptxas_info: bool = False) -> Path:
     return LIB
 
 
+DEMO_SRC = ROOT / "tests" / "cpp" / "sensor_instance_demo.cpp"
+DEMO_BIN = OBJ / "sensor_instance_demo"
+
+
+def build_demo(verbose: bool = False) -> Path:
+    """C++ program written against include/rtacx/simulation.hpp (the host
+    mirror of the reference's SensorInstance API), linked to librtacx.so."""
+    cuda = Path(_nvcc()).resolve().parent.parent
+    OBJ.mkdir(exist_ok=True)
+    _run(["g++", "-std=c++17", "-O2", "-I", str(ROOT / "include"), "-I", str(cuda / "include"), str(DEMO_SRC),
+          "-L", str(PKG), "-lrtacx", f"-Wl,-rpath,{PKG}", "-L", str(cuda / "lib64"), "-lcudart",
+          f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(DEMO_BIN)])
+    if verbose:
+        print(f"built {DEMO_BIN}")
+    return DEMO_BIN
+
+
 if __name__ == "__main__":
     build_library(verbose=True, ptxas_info="--ptxas" in sys.argv)
+    build_demo(verbose=True)

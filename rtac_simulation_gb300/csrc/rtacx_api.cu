@@ -174,6 +174,7 @@ void rtacx_destroy(rtacx_ctx* ctx)
     cudaSetDevice(c.device);
     free_config(c);
     free_dev(c.d_sorted);
+    free_dev(c.d_dir);
     free_dev(c.d_err);
     free_dev(c.d_oor);
     for(cudaEvent_t& e : c.events) if(e) cudaEventDestroy(e);

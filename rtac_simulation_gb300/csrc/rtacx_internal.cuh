@@ -186,6 +186,14 @@ struct Context {
     uint4* d_items = nullptr;           // [tiles * 256] work items
     uint32_t* d_item_counter = nullptr; // work-queue counter
 
+    // Receiver model of rtacx_make_samples (rtacx_configure_receiver).
+    bool rx_configured = false;
+    float rx_rotation[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    uint32_t rx_flags = 0;
+    double rx_hz = 0.0;
+    float* d_dir = nullptr;             // [dir_h][dir_w] receiver directivity
+    uint32_t dir_w = 0, dir_h = 0;
+
     // Echo model (rtacx_set_echo_model).
     uint32_t echo_flags = 0;
     double echo_hz = 0.0;

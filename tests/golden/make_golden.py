@@ -3,7 +3,8 @@
 Builds oracle/_ref/ref_probe (oracle/ref_build.sh compiles the reference's
 header-only Binner::Key and Waveform_Sine against host stand-ins for the
 non-vendored rtac_base headers) and records its answers for a fixed, seeded
-set of inputs into tests/golden/ref_keys.json and tests/golden/ref_waveforms.json.
+set of inputs into tests/golden/ref_keys.json, ref_waveforms.json and
+ref_directivity.json (the receiver directivity builders of src/Directivity.cpp).
 Needs the reference tree (default /root/reference); the tests only read the
 committed JSON files.
 
@@ -108,7 +109,23 @@ def main():
     (HERE / "ref_waveforms.json").write_text(json.dumps(dict(
         source="rtac_simulation include/rtac_simulation/Waveform.h:96-138 compiled by oracle/ref_build.sh",
         cases=waves), indent=0))
-    print(f"wrote {len(key_cases)} key cases and {len(waves)} waveform cases")
+    # Directivity tables (src/Directivity.cpp): small parameter sets so that
+    # the fixtures stay small; lengths in metres.
+    dir_cases = [("RECT", (1.56e-3, 8.0e-3, 1.25e-3), "single-sided", 2),
+                 ("RECT", (1.56e-3, 4.0e-3, 1.25e-3), "none", 4),
+                 ("DISK", (0.15, 0.0395), "single-sided", 1),
+                 ("DISK", (0.05, 0.0395), "none", 2)]
+    lines = [" ".join([kind] + [f32hex(x) for x in par] + [baffle, str(os_)]) for kind, par, baffle, os_ in dir_cases]
+    out = run_probe(lines)
+    dirs = []
+    for (kind, par, baffle, os_), line in zip(dir_cases, out):
+        tok = line.split()
+        w, h = int(tok[1]), int(tok[2])
+        dirs.append(dict(kind=kind, params=[f32hex(x) for x in par], baffle=baffle, oversampling=os_,
+                         width=w, height=h, values=tok[3:]))
+    (HERE / "ref_directivity.json").write_text(json.dumps(dict(
+        source="rtac_simulation src/Directivity.cpp:147-254 compiled by oracle/ref_build.sh", cases=dirs)))
+    print(f"wrote {len(key_cases)} key cases, {len(waves)} waveform cases, {len(dirs)} directivity tables")
 
 
 if __name__ == "__main__":
