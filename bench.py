@@ -249,10 +249,15 @@ def wk_desc(wk) -> str:
             f"{len(s['pulse'])}-tap pulse x {len(s['beam'])}-tap beam")
 
 
-def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, local, torch):
+def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, local, torch, echo=None):
     """Device time of `steps` pings (samples resident), per-stage event times
-    and the end-to-end time with pinned host buffers, for one form."""
+    and the end-to-end time with pinned host buffers, for one form. The form
+    "precision_compensated" is the precision form with the carrier phase
+    reduced in compensated float arithmetic instead of FP64."""
     from rtac_simulation_gb300 import _lib
+    if echo:
+        extra = _lib.RTACX_ECHO_PHASE_COMPENSATED if form == "precision_compensated" else 0
+        ctx.set_echo_model(echo["carrier_hz"], echo["flags"] | extra)
     call = ctx.reduce if form == "plain" else ctx.reduce_precision
     stream = torch.cuda.current_stream()
     for _ in range(max(warmup, 3)):
@@ -322,14 +327,14 @@ def run_ours(args, world, rank, local):
     if wk.dims == 2 and wk.echo:
         D, taps, center = workloads.precision_tables(wk.sensor)
         ctx.configure_precision(D, taps, center)
-        forms = ["precision", "plain"]
+        forms = ["precision", "precision_compensated", "plain"]
     ctx.reserve(n)
     host_in = torch.from_numpy(wk.samples.reshape(-1)).pin_memory()
     d_in = host_in.to("cuda")
     outs = {f: torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda") for f in forms}
     host_out = torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory()
-    res = {f: time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch)
-           for f in forms}
+    res = {f: time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch,
+                        wk.echo) for f in forms}
     if rank != 0:
         return
     head = forms[0]
@@ -340,7 +345,8 @@ def run_ours(args, world, rank, local):
         r = res[f]
         return {"samples_per_s": world * n * args.steps / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / args.steps,
                 "e2e_samples_per_s": world * n * args.steps / r["t_e2e"],
-                "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()}}
+                "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()},
+                "clocks": r["clocks"]}
 
     line = {
         "metric": "samples/s", "value": world * n * args.steps / res[head]["t_dev"], "unit": "samples/s",
@@ -450,10 +456,11 @@ def run_ours(args, world, rank, local):
             acc.setdefault("plain_rel_l2_vs_fp64", []).append(
                 float(np.linalg.norm(got_plain[b0:b1] - want) / np.linalg.norm(want)))
             if "precision" in forms:
-                got_p = to_complex(outs["precision"])
                 want_b = oracle.reduce_binned(exact, wk.sensor, D, taps, center, rows=(b0, b1), threads=threads)
-                acc.setdefault("precision_rel_l2_vs_fp64_binned", []).append(
-                    float(np.linalg.norm(got_p[b0:b1] - want_b) / np.linalg.norm(want_b)))
+                for f in ("precision", "precision_compensated"):
+                    got_p = to_complex(outs[f])
+                    acc.setdefault(f"{f}_rel_l2_vs_fp64_binned", []).append(
+                        float(np.linalg.norm(got_p[b0:b1] - want_b) / np.linalg.norm(want_b)))
                 acc.setdefault("binned_vs_per_sample_model_rel_l2", []).append(
                     float(np.linalg.norm(want_b - want) / np.linalg.norm(want)))
         acc["rows_checked"] = bands

@@ -148,6 +148,10 @@ rtacx_status rtacx_reduce(rtacx_ctx* ctx, const void* samples, uint64_t n,
  * default). Uses the configured sound_celerity; call after rtacx_configure_*. */
 #define RTACX_ECHO_PHASE     1u   /* value *= exp(i 4 pi f travel / c) */
 #define RTACX_ECHO_SPREADING 2u   /* value /= travel^2                */
+/* Reduce the carrier phase with compensated float arithmetic (exact product
+ * split with fmaf) instead of FP64; same accuracy (~1e-7 cycle) without the
+ * FP64 pipe. */
+#define RTACX_ECHO_PHASE_COMPENSATED 4u
 typedef struct {
     double carrier_hz;
     uint32_t flags;

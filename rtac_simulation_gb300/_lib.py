@@ -120,6 +120,7 @@ class PingDesc(ctypes.Structure):
 
 RTACX_ECHO_PHASE = 1
 RTACX_ECHO_SPREADING = 2
+RTACX_ECHO_PHASE_COMPENSATED = 4
 PRECISION_STAGES = ("accumulate", "windows", "filter", "gemm", "copy")
 
 

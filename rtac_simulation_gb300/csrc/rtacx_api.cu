@@ -28,6 +28,8 @@ void sync_echo(Context& c)
 {
     c.bin.echo_flags = c.echo_flags;
     c.bin.echo_cycles = (c.c > 0.0f) ? 2.0 * c.echo_hz / (double)c.c : 0.0;
+    c.bin.echo_k_hi = (float)c.bin.echo_cycles;
+    c.bin.echo_k_lo = (float)(c.bin.echo_cycles - (double)c.bin.echo_k_hi);
 }
 
 void free_config(Context& c)
@@ -370,7 +372,10 @@ rtacx_status rtacx_set_echo_model(rtacx_ctx* ctx, const rtacx_echo_model* m)
     if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;
     Context& c = ctx->impl;
     if(!m || m->flags == 0) { c.echo_flags = 0; c.echo_hz = 0.0; sync_echo(c); return RTACX_OK; }
-    if(m->flags & ~(RTACX_ECHO_PHASE | RTACX_ECHO_SPREADING)) { c.error = "unknown echo flags"; return RTACX_ERR_INVALID_ARGUMENT; }
+    if(m->flags & ~(RTACX_ECHO_PHASE | RTACX_ECHO_SPREADING | RTACX_ECHO_PHASE_COMPENSATED)) {
+        c.error = "unknown echo flags";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
     if((m->flags & RTACX_ECHO_PHASE) && !(std::isfinite(m->carrier_hz) && m->carrier_hz > 0.0)) {
         c.error = "carrier_hz must be positive and finite";
         return RTACX_ERR_INVALID_ARGUMENT;

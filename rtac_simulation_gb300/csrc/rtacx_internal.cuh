@@ -33,6 +33,8 @@ struct BinParams {
     int vec4;              // 1 when records are 16-byte aligned float4s
     uint32_t echo_flags;   // RTACX_ECHO_* pre-step applied to each sample value (0: none)
     double echo_cycles;    // carrier cycles per metre of travel, 2 f / c
+    float echo_k_hi;       // echo_cycles split into two floats (compensated phase)
+    float echo_k_lo;
 };
 
 // Echo-sample epilogue of the reference's ray generator
@@ -40,18 +42,33 @@ struct BinParams {
 // carrier phase is reduced modulo one cycle in FP64 (d * 2f/c, minus its
 // nearest integer: three FP64 operations); the reduced fraction is then
 // exact enough for float sincos.
+// Carrier cycles of a travel reduced to [-0.5, 0.5]: in FP64 (three
+// operations), or with RTACX_ECHO_PHASE_COMPENSATED in float arithmetic
+// that is as exact for this range: t * k_hi split into its rounded product
+// and the exact rounding error (fmaf), the integer part removed from the
+// rounded product (exact below 2^23 cycles), the small terms added last.
+__device__ __forceinline__ float carrier_fraction(const BinParams& p, float travel)
+{
+    if(p.echo_flags & RTACX_ECHO_PHASE_COMPENSATED) {
+        const float prod = travel * p.echo_k_hi;
+        const float err = fmaf(travel, p.echo_k_hi, -prod);
+        const float whole = prod - rintf(prod);
+        return whole + fmaf(travel, p.echo_k_lo, err);
+    }
+    const double cyc = (double)travel * p.echo_cycles;
+    return (float)(cyc - rint(cyc));
+}
+
 __device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel)
 {
     if(p.echo_flags & RTACX_ECHO_PHASE) {
-        const double cyc = (double)travel * p.echo_cycles;
-        const double frac = cyc - rint(cyc);
-        const float ph = (float)frac * 6.28318530717958647692f;
+        // |phase| <= pi: the hardware sine / cosine are accurate to ~4e-7 here.
         float sn, cs;
-        sincosf(ph, &sn, &cs);
+        __sincosf(carrier_fraction(p, travel) * 6.28318530717958647692f, &sn, &cs);
         v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
     }
     if(p.echo_flags & RTACX_ECHO_SPREADING) {
-        const float inv = 1.0f / (travel * travel);
+        const float inv = __fdividef(1.0f, travel * travel);
         v = make_float2(v.x * inv, v.y * inv);
     }
     return v;

@@ -55,10 +55,14 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
                   float4* __restrict__ P, uint32_t* __restrict__ nonempty)
 {
     __shared__ float s_th[kMaxBearingsSmem];
+    __shared__ float s_inv[kMaxBearingsSmem];     // 1 / (theta_k+1 - theta_k)
     __shared__ int16_t s_lut[kLutCells];
     __shared__ uint32_t s_bits[kMaxRangeWords];
     const uint32_t words = (p.key.nR + 31) / 32;
-    for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) s_th[i] = bearings[i];
+    for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) {
+        s_th[i] = bearings[i];
+        s_inv[i] = (i + 1 < nB) ? 1.0f / (bearings[i + 1] - bearings[i]) : 0.0f;
+    }
     for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = (int16_t)lut[i];
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
     __syncthreads();
@@ -77,8 +81,7 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
         int k = s_lut[(int)q];                       // NaN bearings: q = 0
         while(k < kmax && s_th[k + 1] <= th) k++;
         while(k > 0 && !(s_th[k] <= th)) k--;
-        const float t0 = s_th[k], t1 = s_th[k + 1];
-        float w = (th - t0) / (t1 - t0);
+        float w = (th - s_th[k]) * s_inv[k];
         w = fminf(fmaxf(w, 0.0f), 1.0f);          // NaN bearings -> 0
         const float w0 = 1.0f - w;
         red_add_v4(P + (size_t)j * nB + k, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y));
@@ -384,7 +387,7 @@ rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float*
     RTACX_CUDA(cudaMemsetAsync(ctx.d_G, 0, (size_t)nR * nB * sizeof(float4), stream));
     RTACX_CUDA(cudaMemsetAsync(ctx.d_flags, 0, (size_t)(nR + 31) / 32 * 4, stream));
     if(n) {
-        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx.sm_count * 4);
+        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx.sm_count * 6);
         k_prec_accumulate<<<blocks, 256, 0, stream>>>(static_cast<const float*>(samples), n, ctx.bin,
                                                       ctx.d_bearings, nB, ctx.d_lut, ctx.lut_cells, ctx.lut_origin,
                                                       ctx.lut_scale, ctx.d_G, ctx.d_flags);

@@ -106,3 +106,24 @@ def test_precision_vs_plain_model_difference(oracle):
     diff = rel_l2(prec, plain)
     print(f"binned vs per-sample model: rel-L2 {diff:.3e}")
     assert diff < 1.5
+
+
+@pytest.mark.parametrize("form", ["plain", "precision"])
+def test_compensated_phase_matches_fp64_oracle(oracle, form):
+    # RTACX_ECHO_PHASE_COMPENSATED reduces the carrier phase without FP64;
+    # the FP64 oracle must not tell the difference.
+    wk = wl.precision_2d(n_samples=1 << 16, n_ranges=1024)
+    flags = wk.echo["flags"] | 4
+    exact = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
+    if form == "plain":
+        ctx = make_context(wk)
+        ctx.set_echo_model(wk.echo["carrier_hz"], flags)
+        got = gpu_reduce(ctx, wk.samples, wk.out_shape)
+        assert rel_l2(got, oracle.reduce(exact, wk.sensor)) <= 1e-5
+    else:
+        ctx = make_context(wk)
+        ctx.set_echo_model(wk.echo["carrier_hz"], flags)
+        D, taps, c = wl.precision_tables(wk.sensor)
+        ctx.configure_precision(D, taps, c)
+        got = gpu_precision(ctx, wk.samples, wk.out_shape)
+        assert rel_l2(got, oracle.reduce_binned(exact, wk.sensor, D, taps, c)) <= TOL
