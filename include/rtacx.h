@@ -224,6 +224,36 @@ rtacx_status rtacx_make_samples(rtacx_ctx* ctx, const rtacx_echo* hits, uint64_t
 rtacx_status rtacx_directivity_table(int kind, const float* params, float* out, uint32_t* width,
                                      uint32_t* height, void* stream);
 
+/* Rasterised echo samples: the OpenGL ray caster's vertex and fragment
+ * shader arithmetic (src/RayCasterGL.cpp:5-63) and its framebuffer readback
+ * into SimSample2D records (src/SimulationGL.cu:105-171), on CUDA, without a
+ * graphics stack. The mesh is drawn with a depth test (nearest fragment, the
+ * first triangle on ties); every pixel gets (a cos phase, a sin phase, range,
+ * bearing) with a = reflected / range^2 / cos(bearing) / cos(elevation),
+ * phase = range * 4 pi f / c + pi / 2 (reduced in FP64), or zeros where no
+ * triangle covers it; rows bottom-up (glReadPixels order), width x height
+ * records. Matrices are row-major (p' = M p). Triangles with a vertex behind
+ * the eye or outside a +/-64 NDC guard band are skipped (GL would clip them).
+ * Scratch grows on demand inside the context. */
+typedef struct {
+    const float* vertices;        /* device [n_vertices][3], world frame   */
+    const float* normals;         /* device [n_vertices][3]                */
+    const uint32_t* triangles;    /* device [n_triangles][3] vertex indices */
+    uint32_t n_vertices;
+    uint32_t n_triangles;
+} rtacx_mesh;
+typedef struct {
+    float world_to_local[16];     /* worldToLocal (receiver frame)         */
+    float world_to_screen[16];    /* worldToScreen (clip space)            */
+    float origin[3];              /* sensor position, world frame          */
+    uint32_t width;
+    uint32_t height;
+    double carrier_hz;            /* the reference's shader uses 1.2e6     */
+    float sound_celerity;         /* ... and 1500                          */
+} rtacx_raster_view;
+rtacx_status rtacx_rasterize(rtacx_ctx* ctx, const rtacx_mesh* mesh, const rtacx_raster_view* view,
+                             float* samples, void* stream);
+
 /* Batched plain form: many pings from heterogeneous sensors (each bound to
  * its own configured 1D or 2D context, whose scratch it uses) in one CUDA
  * graph: one launch per binning stage covering every ping, then one

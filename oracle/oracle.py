@@ -63,6 +63,8 @@ def load() -> ctypes.CDLL:
     lib.rtacx_oracle_reduce_binned.restype = None
     lib.rtacx_oracle_make_samples.argtypes = [_P, _U64, _P, _P, _U32, _U32, ctypes.c_double, _F, _U32, _U32, _P]
     lib.rtacx_oracle_make_samples.restype = None
+    lib.rtacx_oracle_rasterize.argtypes = [_P, _P, _P, _U32, _U32, _P, _P, _P, _U32, _U32, ctypes.c_double, _F, _P, _P]
+    lib.rtacx_oracle_rasterize.restype = None
     _lib = lib
     return lib
 
@@ -197,3 +199,20 @@ def make_samples(hits: np.ndarray, rotation, table, carrier_hz: float, c: float,
                                      0 if tab is None else tab.shape[1], 0 if tab is None else tab.shape[0],
                                      carrier_hz, c, flags, dims, out.ctypes.data)
     return out
+
+
+def rasterize(vertices, normals, triangles, world_to_local, world_to_screen, origin, width, height,
+              carrier_hz=1.2e6, c=1500.0):
+    """Oracle of rtacx_rasterize: (samples (H*W, 4) float32, winner (H*W,) int32)."""
+    v = np.ascontiguousarray(vertices, np.float32)
+    nrm = np.ascontiguousarray(normals, np.float32)
+    t = np.ascontiguousarray(triangles, np.uint32)
+    L = np.ascontiguousarray(np.asarray(world_to_local, np.float32).reshape(16))
+    S = np.ascontiguousarray(np.asarray(world_to_screen, np.float32).reshape(16))
+    o = np.ascontiguousarray(np.asarray(origin, np.float32))
+    out = np.zeros((height * width, 4), np.float32)
+    win = np.zeros(height * width, np.int32)
+    load().rtacx_oracle_rasterize(v.ctypes.data, nrm.ctypes.data, t.ctypes.data, v.shape[0], t.shape[0],
+                                  L.ctypes.data, S.ctypes.data, o.ctypes.data, width, height, carrier_hz, c,
+                                  out.ctypes.data, win.ctypes.data)
+    return out, win

@@ -565,4 +565,121 @@ void rtacx_oracle_make_samples(const float* hits, uint64_t n, const float* R, co
     }
 }
 
+// Rasteriser oracle (see rtacx_rasterize): identical integer coverage,
+// top-left rule, double depth rounded to float and (depth, triangle) ties as
+// the kernel; varyings and the fragment arithmetic in double. out: W*H*4
+// floats, rows bottom-up; winner (optional): triangle per pixel or -1.
+void rtacx_oracle_rasterize(const float* vtx, const float* nrm, const uint32_t* tris, uint32_t nv, uint32_t nt,
+                            const float* L, const float* S, const float* origin, uint32_t W, uint32_t H,
+                            double carrier_hz, float c, float* out, int32_t* winner)
+{
+    struct V { long long X, Y; float z, iw; double d[3]; double refl; bool ok; };
+    std::vector<V> vs(nv);
+    for(uint32_t i = 0; i < nv; i++) {
+        const float x = vtx[3 * i], y = vtx[3 * i + 1], z = vtx[3 * i + 2];
+        const float cx = std::fma(S[0], x, std::fma(S[1], y, std::fma(S[2], z, S[3])));
+        const float cy = std::fma(S[4], x, std::fma(S[5], y, std::fma(S[6], z, S[7])));
+        const float cz = std::fma(S[8], x, std::fma(S[9], y, std::fma(S[10], z, S[11])));
+        const float cw = std::fma(S[12], x, std::fma(S[13], y, std::fma(S[14], z, S[15])));
+        V& v = vs[i];
+        v.ok = false; v.X = v.Y = 0; v.z = 0.0f; v.iw = 0.0f;
+        if(cw > 1.0e-6f) {
+            const float iw = 1.0f / cw;
+            const float nx = cx * iw, ny = cy * iw;
+            if(std::fabs(nx) <= 64.0f && std::fabs(ny) <= 64.0f) {
+                float fx = nx + 1.0f; fx = fx * 0.5f; fx = fx * (float)W; fx = fx * 256.0f;
+                float fy = ny + 1.0f; fy = fy * 0.5f; fy = fy * (float)H; fy = fy * 256.0f;
+                v.X = (long long)std::nearbyint(fx); v.Y = (long long)std::nearbyint(fy);
+                v.z = cz * iw; v.iw = iw; v.ok = true;
+            }
+        }
+        const double o[3] = {(double)x - origin[0], (double)y - origin[1], (double)z - origin[2]};
+        double m[3];
+        for(int r = 0; r < 3; r++) {
+            v.d[r] = L[4 * r] * o[0] + L[4 * r + 1] * o[1] + L[4 * r + 2] * o[2];
+            m[r] = L[4 * r] * (double)nrm[3 * i] + L[4 * r + 1] * (double)nrm[3 * i + 1] + L[4 * r + 2] * (double)nrm[3 * i + 2];
+        }
+        v.refl = std::fabs(m[2] / std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]));
+    }
+    auto edge = [](long long ax, long long ay, long long bx, long long by, long long px, long long py) {
+        return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+    };
+    auto top_left = [](long long ax, long long ay, long long bx, long long by) {
+        const long long dx = bx - ax, dy = by - ay;
+        return (dy == 0 && dx < 0) || dy < 0;
+    };
+    std::vector<unsigned long long> vis((size_t)W * H, ~0ull);
+    for(uint32_t t = 0; t < nt; t++) {
+        const uint32_t id[3] = {tris[3 * t], tris[3 * t + 1], tris[3 * t + 2]};
+        if(id[0] >= nv || id[1] >= nv || id[2] >= nv) continue;
+        const V* p[3] = {&vs[id[0]], &vs[id[1]], &vs[id[2]]};
+        if(!p[0]->ok || !p[1]->ok || !p[2]->ok) continue;
+        const long long area = (p[1]->X - p[0]->X) * (p[2]->Y - p[0]->Y) - (p[1]->Y - p[0]->Y) * (p[2]->X - p[0]->X);
+        if(area == 0) continue;
+        const int o0 = 0, o1 = area > 0 ? 1 : 2, o2 = area > 0 ? 2 : 1;
+        long long minX = std::min({p[0]->X, p[1]->X, p[2]->X}), maxX = std::max({p[0]->X, p[1]->X, p[2]->X});
+        long long minY = std::min({p[0]->Y, p[1]->Y, p[2]->Y}), maxY = std::max({p[0]->Y, p[1]->Y, p[2]->Y});
+        const long long i0 = std::max(0ll, (minX - 128 + 255) / 256);
+        const long long i1 = std::min((long long)W - 1, (maxX - 128) >= 0 ? (maxX - 128) / 256 : -1ll);
+        const long long j0 = std::max(0ll, (minY - 128 + 255) / 256);
+        const long long j1 = std::min((long long)H - 1, (maxY - 128) >= 0 ? (maxY - 128) / 256 : -1ll);
+        for(long long j = j0; j <= j1; j++)
+            for(long long i = i0; i <= i1; i++) {
+                const long long px = i * 256 + 128, py = j * 256 + 128;
+                const long long e0 = edge(p[o1]->X, p[o1]->Y, p[o2]->X, p[o2]->Y, px, py);
+                const long long e1 = edge(p[o2]->X, p[o2]->Y, p[o0]->X, p[o0]->Y, px, py);
+                const long long e2 = edge(p[o0]->X, p[o0]->Y, p[o1]->X, p[o1]->Y, px, py);
+                if(e0 < 0 || e1 < 0 || e2 < 0) continue;
+                if(e0 == 0 && !top_left(p[o1]->X, p[o1]->Y, p[o2]->X, p[o2]->Y)) continue;
+                if(e1 == 0 && !top_left(p[o2]->X, p[o2]->Y, p[o0]->X, p[o0]->Y)) continue;
+                if(e2 == 0 && !top_left(p[o0]->X, p[o0]->Y, p[o1]->X, p[o1]->Y)) continue;
+                const double ar = (double)(e0 + e1 + e2);
+                double num = (double)e0 * (double)p[o0]->z;
+                num = num + (double)e1 * (double)p[o1]->z;
+                num = num + (double)e2 * (double)p[o2]->z;
+                const double zn = num / ar;
+                const double depth = 0.5 * zn + 0.5;
+                if(!(depth >= 0.0 && depth <= 1.0)) continue;
+                const float d = (float)depth;
+                uint32_t bits;
+                std::memcpy(&bits, &d, 4);
+                const unsigned long long w = ((unsigned long long)bits << 32) | t;
+                unsigned long long& slot = vis[(size_t)j * W + i];
+                if(w < slot) slot = w;
+            }
+    }
+    const double pi = 3.14159265358979323846;
+    for(size_t idx = 0; idx < (size_t)W * H; idx++) {
+        float* o = out + 4 * idx;
+        o[0] = o[1] = o[2] = o[3] = 0.0f;
+        if(winner) winner[idx] = -1;
+        if(vis[idx] == ~0ull) continue;
+        const uint32_t t = (uint32_t)(vis[idx] & 0xFFFFFFFFu);
+        if(winner) winner[idx] = (int32_t)t;
+        const V* p[3] = {&vs[tris[3 * t]], &vs[tris[3 * t + 1]], &vs[tris[3 * t + 2]]};
+        const long long i = (long long)(idx % W), j = (long long)(idx / W);
+        const long long px = i * 256 + 128, py = j * 256 + 128;
+        const double l[3] = {(double)edge(p[1]->X, p[1]->Y, p[2]->X, p[2]->Y, px, py),
+                             (double)edge(p[2]->X, p[2]->Y, p[0]->X, p[0]->Y, px, py),
+                             (double)edge(p[0]->X, p[0]->Y, p[1]->X, p[1]->Y, px, py)};
+        double wsum = 0.0, d[3] = {0, 0, 0}, refl = 0.0;
+        for(int k = 0; k < 3; k++) {
+            const double w = l[k] * (double)p[k]->iw;
+            wsum += w;
+            for(int r = 0; r < 3; r++) d[r] += w * p[k]->d[r];
+            refl += w * p[k]->refl;
+        }
+        for(int r = 0; r < 3; r++) d[r] /= wsum;
+        refl /= wsum;
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const double range = std::sqrt(r2);
+        const double bearing = std::atan2(d[0], -d[2]), elevation = std::atan2(d[1], -d[2]);
+        const double cyc = range * (2.0 * carrier_hz / (double)c) + 0.25;
+        const double ph = 2.0 * pi * (cyc - std::nearbyint(cyc));
+        const double a = refl / r2 / std::cos(bearing) / std::cos(elevation);
+        o[0] = (float)(a * std::cos(ph)); o[1] = (float)(a * std::sin(ph));
+        o[2] = (float)range; o[3] = (float)bearing;
+    }
+}
+
 } // extern "C"

@@ -79,6 +79,7 @@ SIGNATURES = {
     "rtacx_make_samples": (_I, [_P, _P, _U64, _P, _P]),
     "rtacx_directivity_table": (_I, [_I, ctypes.POINTER(ctypes.c_float), _P, ctypes.POINTER(_U32),
                                      ctypes.POINTER(_U32), _P]),
+    "rtacx_rasterize": (_I, [_P, _P, _P, _P, _P]),
     "rtacx_batch_create": (_I, [ctypes.POINTER(_P), _I]),
     "rtacx_batch_destroy": (None, [_P]),
     "rtacx_batch_last_error": (ctypes.c_char_p, [_P]),
@@ -91,6 +92,16 @@ SIGNATURES = {
 RTACX_BATCH_AUTOTUNE = 1
 RTACX_DIRECTIVITY_RECTANGLE = 1
 RTACX_DIRECTIVITY_DISK = 2
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("vertices", _P), ("normals", _P), ("triangles", _P), ("n_vertices", _U32), ("n_triangles", _U32)]
+
+
+class RasterView(ctypes.Structure):
+    _fields_ = [("world_to_local", ctypes.c_float * 16), ("world_to_screen", ctypes.c_float * 16),
+                ("origin", ctypes.c_float * 3), ("width", _U32), ("height", _U32),
+                ("carrier_hz", ctypes.c_double), ("sound_celerity", ctypes.c_float)]
 
 
 class Receiver(ctypes.Structure):
@@ -272,6 +283,19 @@ class Context:
 
     def make_samples(self, hits, n: int, samples, stream=None) -> None:
         self._check(self._lib.rtacx_make_samples(self._h, _ptr(hits), n, _ptr(samples), _stream(stream)))
+
+    def rasterize(self, vertices, normals, triangles, world_to_local, world_to_screen, origin, width: int,
+                  height: int, samples, carrier_hz: float = 1.2e6, sound_celerity: float = 1500.0,
+                  stream=None) -> None:
+        """vertices / normals / triangles: device tensors; matrices row-major 4x4."""
+        L = np.asarray(world_to_local, np.float32).reshape(16)
+        S = np.asarray(world_to_screen, np.float32).reshape(16)
+        m = Mesh(_ptr(vertices), _ptr(normals), _ptr(triangles), vertices.shape[0], triangles.shape[0])
+        v = RasterView((ctypes.c_float * 16)(*L.tolist()), (ctypes.c_float * 16)(*S.tolist()),
+                       (ctypes.c_float * 3)(*np.asarray(origin, np.float32).tolist()), width, height,
+                       carrier_hz, sound_celerity)
+        self._check(self._lib.rtacx_rasterize(self._h, ctypes.byref(m), ctypes.byref(v), _ptr(samples),
+                                              _stream(stream)))
 
     def set_tracing(self, enable: bool) -> None:
         self._check(self._lib.rtacx_set_tracing(self._h, 1 if enable else 0))

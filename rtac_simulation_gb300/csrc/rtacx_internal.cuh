@@ -211,6 +211,11 @@ struct Context {
     float* d_dir = nullptr;             // [dir_h][dir_w] receiver directivity
     uint32_t dir_w = 0, dir_h = 0;
 
+    // Rasteriser scratch (rtacx_rasterize), grown on demand.
+    unsigned char* d_rast_v = nullptr;  size_t rast_v_cap = 0;
+    unsigned long long* d_rast_vis = nullptr; size_t rast_vis_cap = 0;
+    uint32_t* d_rast_large = nullptr;   size_t rast_large_cap = 0;
+
     // Echo model (rtacx_set_echo_model).
     uint32_t echo_flags = 0;
     double echo_hz = 0.0;
