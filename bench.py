@@ -300,7 +300,19 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     ctx.stream_status(stream)
     t_e2e = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
-    return dict(t_dev=t_dev, stage=stage, t_e2e=t_e2e, clocks=clk)
+    # Breakdown of one end-to-end step: host->device copy, ping, device->host copy.
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    evs[0].record(stream)
+    d_in.copy_(host_in, non_blocking=True)
+    evs[1].record(stream)
+    call(d_in, n, out, stream=stream)
+    evs[2].record(stream)
+    host_out.copy_(out, non_blocking=True)
+    evs[3].record(stream)
+    torch.cuda.synchronize()
+    e2e_split = {"h2d_ms": evs[0].elapsed_time(evs[1]), "ping_ms": evs[1].elapsed_time(evs[2]),
+                 "d2h_ms": evs[2].elapsed_time(evs[3])}
+    return dict(t_dev=t_dev, stage=stage, t_e2e=t_e2e, clocks=clk, e2e_split=e2e_split)
 
 
 def to_complex(t):
@@ -346,6 +358,7 @@ def run_ours(args, world, rank, local):
         return {"samples_per_s": world * n * args.steps / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / args.steps,
                 "e2e_samples_per_s": world * n * args.steps / r["t_e2e"],
                 "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()},
+                "e2e_step_ms": {k: round(v, 4) for k, v in r["e2e_split"].items()},
                 "clocks": r["clocks"]}
 
     line = {

@@ -24,6 +24,8 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <fstream>
+#include <iostream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -342,6 +344,52 @@ public:
         check(rtacx_reduce(ctx_, receivedSamples_.data(), receivedSamples_.size(),
                            reinterpret_cast<float*>(sensorOutput_.data()), nullptr));
         check(rtacx_stream_status(ctx_, nullptr));
+    }
+};
+
+// Ping file sink (include/rtac_simulation/sinks/FileSink.h:12-31,
+// src/sinks/FileSink.cpp:14-42): appends one record per set_output() call.
+// The reference serialises rtac_base's CudaPing2D, whose wire format lives in
+// the non-vendored rtac_base serialization; this sink writes its own
+// documented little-endian record instead:
+//   char magic[8] = "RTACXPNG"; uint32 version = 1; uint32 range_count;
+//   uint32 bearing_count; float range_min, range_max;
+//   float bearings[bearing_count]; complex64 ping[range_count][bearing_count]
+// Like the reference, only 2D sensors are written.
+class FileSink {
+    std::string filename_;
+    std::ofstream* file_;
+    explicit FileSink(const std::string& filename)
+        : filename_(filename), file_(new std::ofstream(filename, std::ofstream::binary)) {}
+public:
+    using Ptr = std::shared_ptr<FileSink>;
+    ~FileSink() { delete file_; }
+    static Ptr Create(const std::string& filename, bool overwrite = false)
+    {
+        std::ifstream probe(filename);
+        if(probe.good() && !overwrite)
+            throw std::runtime_error("FileSink : could not prepare path for file '" + filename + "'");
+        Ptr p(new FileSink(filename));
+        if(!p->file_->good()) throw std::runtime_error("FileSink : cannot open '" + filename + "'");
+        return p;
+    }
+    const std::string& filename() const { return filename_; }
+    void set_output(const std::shared_ptr<SensorInstance2D_Complex>& sensor)
+    {
+        if(!sensor) { std::cerr << "FileSink : sensor type not handled" << std::endl; return; }
+        const std::vector<Complex> ping = sensor->output().to_host();
+        const uint32_t version = 1, nr = sensor->height(), nb = sensor->width();
+        const float rmin = sensor->ranges().lower(), rmax = sensor->ranges().upper();
+        file_->write("RTACXPNG", 8);
+        file_->write(reinterpret_cast<const char*>(&version), 4);
+        file_->write(reinterpret_cast<const char*>(&nr), 4);
+        file_->write(reinterpret_cast<const char*>(&nb), 4);
+        file_->write(reinterpret_cast<const char*>(&rmin), 4);
+        file_->write(reinterpret_cast<const char*>(&rmax), 4);
+        file_->write(reinterpret_cast<const char*>(sensor->bearings().data()), 4 * (std::streamsize)nb);
+        file_->write(reinterpret_cast<const char*>(ping.data()), (std::streamsize)(ping.size() * sizeof(Complex)));
+        file_->flush();
+        if(!file_->good()) throw std::runtime_error("FileSink : write failed on '" + filename_ + "'");
     }
 };
 

@@ -358,9 +358,9 @@ __global__ void k_reset_batch(const PingDev* __restrict__ pings, uint32_t n_ping
 
 uint32_t hist_grid(const Context& ctx, uint64_t n)
 {
-    // At least ~4096 samples per CTA so that the per-CTA histogram rows stay
+    // At least ~8192 samples per CTA so that the per-CTA histogram rows stay
     // small relative to the data.
-    const uint64_t want = std::max<uint64_t>(1, (n + 4095) / 4096);
+    const uint64_t want = std::max<uint64_t>(1, (n + 8191) / 8192);
     return (uint32_t)std::min<uint64_t>(ctx.hist_ctas, want);
 }
 
@@ -491,11 +491,12 @@ void configure_hist_launch(Context& ctx)
     const size_t smem = (size_t)ctx.bin.nBins * sizeof(uint32_t);
     cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
     cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
-    ctx.hist_threads = 512;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter, (int)ctx.hist_threads, smem);
-    per_sm = std::max(1, std::min(per_sm, 4));
-    ctx.hist_ctas = (uint32_t)(ctx.sm_count * per_sm);
+    // One 1024-thread CTA per SM: every (CTA, bin) pair keeps one partially
+    // written 128-byte line of the sorted array open in L2 while the scatter
+    // runs, so fewer CTAs keep that working set (CTAs x bins x 128 B) inside
+    // L2 and the scattered records merge into whole lines before eviction.
+    ctx.hist_threads = 1024;
+    ctx.hist_ctas = (uint32_t)ctx.sm_count;
     cudaGetLastError();
 }
 

@@ -3,7 +3,8 @@
 // would: SensorInfo + Waveform_Sine + BeamDirectivity -> SensorInstance,
 // set_sample_count, fill samples(), compute_output(), read output().
 //
-// usage: sensor_instance_demo <params.txt> <samples.bin> <out.bin>
+// usage: sensor_instance_demo <params.txt> <samples.bin> <out.bin> [sink]
+// With [sink], a 2D ping is computed twice and appended twice to a FileSink.
 // params.txt holds "key value" lines (dims, range_min, range_max,
 // range_count, celerity, frequency, duration, fixed, oversampling,
 // beam_span) and "key n v_0 .. v_n-1" lines (beam, bearings).
@@ -22,7 +23,7 @@ using namespace rtacx::simulation;
 
 int main(int argc, char** argv)
 {
-    if(argc != 4) { std::cerr << "usage: " << argv[0] << " params.txt samples.bin out.bin\n"; return 2; }
+    if(argc != 4 && argc != 5) { std::cerr << "usage: " << argv[0] << " params.txt samples.bin out.bin [sink]\n"; return 2; }
     std::map<std::string, double> scalars;
     std::map<std::string, std::vector<float>> arrays;
     std::ifstream pf(argv[1]);
@@ -54,6 +55,12 @@ int main(int argc, char** argv)
             sensor->samples().copy_from_host(reinterpret_cast<const SimSample2D*>(raw.data()), n);
             sensor->compute_output();
             out = sensor->output().to_host();
+            if(argc == 5) {
+                auto sink = FileSink::Create(argv[4], true);
+                sink->set_output(sensor);
+                sensor->compute_output();
+                sink->set_output(sensor);
+            }
         }
         else {
             auto info = SensorInfo::Create(ranges, waveform);

@@ -18,7 +18,7 @@ if not torch.cuda.is_available():
     pytest.skip("needs a GPU", allow_module_level=True)
 
 
-def run_demo(tmp_path, wk, frequency, duration, fixed):
+def run_demo(tmp_path, wk, frequency, duration, fixed, sink=None):
     if not build.DEMO_BIN.exists():
         build.build_demo()
     s = wk.sensor
@@ -32,7 +32,7 @@ def run_demo(tmp_path, wk, frequency, duration, fixed):
     (tmp_path / "params.txt").write_text("\n".join(lines) + "\n")
     wk.samples.astype(np.float32).tofile(tmp_path / "samples.bin")
     res = subprocess.run([str(build.DEMO_BIN), str(tmp_path / "params.txt"), str(tmp_path / "samples.bin"),
-                          str(tmp_path / "out.bin")], capture_output=True, text=True)
+                          str(tmp_path / "out.bin")] + ([str(sink)] if sink else []), capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
     return np.fromfile(tmp_path / "out.bin", dtype=np.complex64).reshape(wk.out_shape)
 
@@ -49,3 +49,16 @@ def test_cpp_mirror_1d_fixed_waveform(tmp_path, oracle):
     got = run_demo(tmp_path, wk, 38.0e3, 128.0e-6, fixed=True)
     want = oracle.reduce(wk.samples, wk.sensor)
     assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-5
+
+
+def test_cpp_file_sink_records(tmp_path):
+    from rtac_simulation_gb300.sink import read_pings
+    wk = wl.oculus_reference_2d(n_samples=20000)
+    got = run_demo(tmp_path, wk, 1.2e6, 1.0, fixed=False, sink=tmp_path / "pings.bin")
+    recs = read_pings(tmp_path / "pings.bin")
+    assert len(recs) == 2
+    for r in recs:
+        assert r["ping"].shape == wk.out_shape
+        np.testing.assert_array_equal(r["bearings"], np.asarray(wk.sensor["bearings"], np.float32))
+        assert np.linalg.norm(r["ping"] - got) <= 1e-6 * np.linalg.norm(got)
+        assert r["range_min"] == np.float32(wk.sensor["range_min"]) and r["range_max"] == np.float32(wk.sensor["range_max"])
