@@ -43,7 +43,7 @@ sys.path.insert(0, str(ROOT))
 from rtac_simulation_gb300 import workloads  # noqa: E402
 
 DEFAULT_CONFIG = "precision_2d"
-KERNELS_PER_PING = 6   # count, colscan, binscan, scatter, windows, gather
+KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
 
 
 def parse_args():
@@ -390,11 +390,11 @@ def run_ours(args, world, rank, local):
                   "peak_source": "nominal FP32 SIMT (152 SMs x 128 FMA x max clock); no measured FP32 peak",
                   "algorithmic": "8 flop per useful (sample, output cell) pair, %.3e pairs" % pairs}
     bin_bytes = n * (rec_in + 16)
-    bin_s = (st["count"] + st["colscan"] + st["binscan"] + st["scatter"] + st["windows"]) / 1e3
+    bin_s = (st["count"] + st["reset"] + st["binscan"] + st["scatter"] + st["windows"]) / 1e3
     bin_gbs = bin_bytes / bin_s / 1e9 if bin_s > 0 else 0.0
     line["roofline_sort_bin"] = {"bound": "hbm", "achieved": bin_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                  "frac": bin_gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
-                                 "algorithmic": f"{rec_in}+16 bytes per sample over count+colscan+binscan+scatter+windows"}
+                                 "algorithmic": f"{rec_in}+16 bytes per sample over count+reset+binscan+scatter+windows"}
     if "precision" in forms:
         ps = res["precision"]["stage"]
         nR, nB = wk.sensor["range_count"], len(wk.sensor["bearings"])

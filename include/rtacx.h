@@ -292,8 +292,8 @@ rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
  * when enabled, rtacx_reduce records a CUDA event pair around each stage on
  * the caller's stream. rtacx_stage_times waits for the last traced call and
  * writes up to `max` stage durations in milliseconds (0 for stages the last
- * call did not run): for rtacx_reduce count, column scan, bin scan, scatter,
- * windows, reduce; for rtacx_reduce_precision accumulate, windows, range
+ * call did not run): for rtacx_reduce count, reset of the bin totals, bin
+ * scan, scatter, windows, reduce; for rtacx_reduce_precision accumulate, windows, range
  * filter, tensor-core GEMM, copy-out. Returns the number of stages written
  * (negative on error). */
 #define RTACX_STAGE_COUNT 6

@@ -143,7 +143,7 @@ class PrecisionDesc(ctypes.Structure):
     _fields_ = [("directivity", _P), ("range_taps", _P), ("tap_count", _U32), ("tap_center", _U32),
                 ("flags", _U32)]
 
-STAGES = ("count", "colscan", "binscan", "scatter", "windows", "reduce")
+STAGES = ("count", "reset", "binscan", "scatter", "windows", "reduce")
 
 _lib = None
 

@@ -116,7 +116,7 @@ bool configure_common(Context& c, const Common& s, float pulse_scale)
 bool allocate_bins(Context& c)
 {
     configure_hist_launch(c);
-    const size_t cols = (size_t)c.hist_ctas * c.bin.nBins;
+    const size_t cols = (size_t)c.bin.nBins * kCursorStride;
     return upload<uint32_t>(c, c.d_offsets, nullptr, c.bin.nBins + 1) &&
            upload<uint32_t>(c, c.d_totals, nullptr, c.bin.nBins) &&
            upload<int2>(c, c.d_win, nullptr, c.nR) &&

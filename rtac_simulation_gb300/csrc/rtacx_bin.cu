@@ -8,17 +8,23 @@
 // integer key gives the reference's segments and windows exactly without a
 // comparison sort.
 //
-// Passes (persistent CTAs, each owning one contiguous chunk of the input):
+// Passes (persistent CTAs, each owning one contiguous chunk of the input,
+// processed in tiles of kTileLoads independent record loads per thread):
 //   k_count      key of every sample, per-CTA histogram in shared memory,
-//                written as one row
-//                of the [cta][bin] matrix; out-of-range counts.
-//   k_colscan    per bin, exclusive prefix over CTAs (in place) + bin total.
-//   k_binscan    exclusive scan of bin totals -> bin offsets.
-//   k_scatter    re-reads the chunk, ranks each sample in shared memory and
-//                writes it as a float4 {re, im, travel, bearing} record to
-//                offsets[bin] + prefix[cta][bin] + rank.
+//                added into the zeroed bin totals; out-of-range counts.
+//   k_binscan    exclusive scan of bin totals -> bin offsets, and one shared
+//                write cursor per bin initialised to its offset.
+//   k_scatter    re-reads the chunk; per tile, ranks each sample in a
+//                shared-memory histogram, reserves one run per (tile, bin)
+//                with a global atomicAdd on the bin's cursor and writes the
+//                float4 {re, im, travel, bearing} records of the run.
 //   k_windows    reference windows (do_make_bins, src/Binner.cu:82-106) as
 //                range-bin intervals, intersected with each row's PSF support.
+// Every bin has one write frontier shared by all CTAs, so the partially
+// written 128-byte lines of the sorted array number about one per bin and
+// complete in L2 before eviction (per-CTA sub-ranges inside each bin would
+// keep CTAs x bins lines open for the whole pass and turn the scattered
+// 16-byte stores into partial-line write-backs).
 #include "rtacx_internal.cuh"
 
 #include <algorithm>
@@ -32,9 +38,13 @@ constexpr int kScanThreads = 1024;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
-// One warp-uniform pass over chunk `c` of `nc` equal chunks of the input.
-// f(valid, record, key, side) is called by every lane of every warp the same
-// number of times.
+constexpr int kTileLoads = 4;        // independent record loads per thread and tile
+
+// Block-uniform pass over chunk `c` of `nc` equal chunks of the input in
+// tiles of blockDim.x * kTileLoads samples: the loads of tile t + 1 are
+// issued before tile t is processed, then the keys are computed and
+// f(valid[], record[], key[], side[]) is called -- the same number of times
+// in every thread, so f may synchronise the block.
 template <typename F>
 __device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, const BinParams& p,
                                           uint32_t c, uint32_t nc, F&& f)
@@ -42,15 +52,32 @@ __device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, cons
     const uint64_t chunk = (n + nc - 1) / nc;
     const uint64_t begin = (uint64_t)c * chunk;
     const uint64_t end = min(begin + chunk, n);
-    for(uint64_t i0 = begin + (threadIdx.x & ~31u); i0 < end; i0 += blockDim.x) {
-        const uint64_t i = i0 + lane_id();
-        const bool valid = i < end;
-        float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t key = kOutOfRange;
-        int side = 0;
-        if(valid) {
-            rec = load_record(samples, i, p);
-            key = sample_key(p, rec.z, rec.w, side);
+    const uint64_t tile = (uint64_t)blockDim.x * kTileLoads;
+    float4 next[kTileLoads];
+    auto load_tile = [&](uint64_t t0) {
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            const uint64_t i = t0 + (uint64_t)u * blockDim.x + threadIdx.x;
+            next[u] = i < end ? load_record(samples, i, p) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    if(begin < end) load_tile(begin);
+    for(uint64_t t0 = begin; t0 < end; t0 += tile) {
+        bool valid[kTileLoads];
+        float4 rec[kTileLoads];
+        uint32_t key[kTileLoads];
+        int side[kTileLoads];
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            valid[u] = t0 + (uint64_t)u * blockDim.x + threadIdx.x < end;
+            rec[u] = next[u];
+        }
+        if(t0 + tile < end) load_tile(t0 + tile);
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            key[u] = kOutOfRange;
+            side[u] = 0;
+            if(valid[u]) key[u] = sample_key(p, rec[u].z, rec[u].w, side[u]);
         }
         f(valid, rec, key, side);
     }
@@ -58,9 +85,10 @@ __device__ __forceinline__ void for_chunk(const float* samples, uint64_t n, cons
 
 } // namespace
 
-// Count pass of chunk c of nc (shared-memory histogram sh of p.nBins words).
+// Count pass of chunk c of nc (shared-memory histogram sh of p.nBins
+// words), added into totals[0, nBins) (zeroed by the caller).
 __device__ void count_chunk(const float* __restrict__ samples, uint64_t n, const BinParams& p, uint32_t c,
-                            uint32_t nc, uint32_t* __restrict__ hist, unsigned long long* __restrict__ oor,
+                            uint32_t nc, uint32_t* __restrict__ totals, unsigned long long* __restrict__ oor,
                             uint32_t* sh, unsigned long long* s_oor)
 {
     for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = 0u;
@@ -68,10 +96,13 @@ __device__ void count_chunk(const float* __restrict__ samples, uint64_t n, const
     __syncthreads();
 
     uint32_t low = 0, high = 0;
-    for_chunk(samples, n, p, c, nc, [&](bool valid, const float4&, uint32_t key, int side) {
-        if(valid && key != kOutOfRange) atomicAdd(&sh[key], 1u);
-        else if(valid) {
-            if(side < 0) low++; else high++;
+    for_chunk(samples, n, p, c, nc, [&](const bool* valid, const float4*, const uint32_t* key, const int* side) {
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            if(valid[u] && key[u] != kOutOfRange) atomicAdd(&sh[key[u]], 1u);
+            else if(valid[u]) {
+                if(side[u] < 0) low++; else high++;
+            }
         }
     });
     for(int o = 16; o > 0; o >>= 1) {
@@ -87,50 +118,18 @@ __device__ void count_chunk(const float* __restrict__ samples, uint64_t n, const
         if(s_oor[0]) atomicAdd(&oor[0], s_oor[0]);
         if(s_oor[1]) atomicAdd(&oor[1], s_oor[1]);
     }
-    uint32_t* row = hist + (size_t)c * p.nBins;
-    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) row[b] = sh[b];
+    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x)
+        if(sh[b]) atomicAdd(&totals[b], sh[b]);
 }
 
 namespace {
 
 __global__ void k_count(const float* __restrict__ samples, uint64_t n, BinParams p,
-                        uint32_t* __restrict__ hist, unsigned long long* __restrict__ oor)
+                        uint32_t* __restrict__ totals, unsigned long long* __restrict__ oor)
 {
     extern __shared__ uint32_t sh[];
     __shared__ unsigned long long s_oor[2];
-    count_chunk(samples, n, p, blockIdx.x, gridDim.x, hist, oor, sh, s_oor);
-}
-
-} // namespace
-
-// Per bin: hist[c][b] <- sum_{c' < c} hist[c'][b]; totals[b] <- sum_c hist[c][b].
-__device__ void colscan_bin(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t nBins,
-                            uint32_t* __restrict__ totals, uint32_t b)
-{
-    if(b >= nBins) return;
-    uint32_t run = 0;
-    uint32_t c = 0;
-    for(; c + 8 <= ctas; c += 8) {
-        uint32_t v[8];
-#pragma unroll
-        for(int u = 0; u < 8; u++) v[u] = hist[(size_t)(c + u) * nBins + b];
-#pragma unroll
-        for(int u = 0; u < 8; u++) { hist[(size_t)(c + u) * nBins + b] = run; run += v[u]; }
-    }
-    for(; c < ctas; c++) {
-        uint32_t v = hist[(size_t)c * nBins + b];
-        hist[(size_t)c * nBins + b] = run;
-        run += v;
-    }
-    totals[b] = run;
-}
-
-namespace {
-
-__global__ void k_colscan(uint32_t* __restrict__ hist, uint32_t ctas, uint32_t nBins,
-                          uint32_t* __restrict__ totals)
-{
-    colscan_bin(hist, ctas, nBins, totals, blockIdx.x * blockDim.x + threadIdx.x);
+    count_chunk(samples, n, p, blockIdx.x, gridDim.x, totals, oor, sh, s_oor);
 }
 
 // Exclusive block scan of one value per thread (blockDim.x == kScanThreads).
@@ -163,8 +162,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 } // namespace
 
 // Exclusive scan of totals[0, nBins) into offsets[0, nBins] by one CTA of
-// kScanThreads threads.
-__device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins, uint32_t* __restrict__ offsets)
+// kScanThreads threads; cursor (optional) receives offsets[0, nBins).
+__device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins, uint32_t* __restrict__ offsets,
+                            uint32_t* __restrict__ cursor)
 {
     __shared__ uint32_t s_warp[32];
     const uint32_t per = (nBins + blockDim.x - 1) / blockDim.x;
@@ -174,53 +174,75 @@ __device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins,
     for(uint32_t b = b0; b < b1; b++) sum += totals[b];
     uint32_t total;
     uint32_t run = block_exclusive_scan(sum, s_warp, total);
-    for(uint32_t b = b0; b < b1; b++) { offsets[b] = run; run += totals[b]; }
+    for(uint32_t b = b0; b < b1; b++) {
+        offsets[b] = run;
+        if(cursor) cursor[(size_t)b * kCursorStride] = run;
+        run += totals[b];
+    }
     if(threadIdx.x == 0) offsets[nBins] = total;
 }
 
 namespace {
 
 __global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __restrict__ totals, uint32_t nBins,
-                                                           uint32_t* __restrict__ offsets)
+                                                           uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursor)
 {
-    binscan_cta(totals, nBins, offsets);
+    binscan_cta(totals, nBins, offsets, cursor);
 }
 
 } // namespace
 
-// Scatter pass of chunk c of nc: rank each sample in the shared-memory
-// cursors sh (p.nBins words) and write its sorted record.
+// Scatter pass of chunk c of nc. Per tile: rank of each sample among the
+// tile's samples of its bin (shared-memory histogram sh of p.nBins words,
+// zero between tiles); the first sample of each (tile, bin) reserves the
+// bin's run with one atomicAdd on the shared cursor and leaves the run's
+// base in sh; every sample is written at base + rank.
 __device__ void scatter_chunk(const float* __restrict__ samples, uint64_t n, const BinParams& p, uint32_t c,
-                              uint32_t nc, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ offsets,
+                              uint32_t nc, uint32_t* __restrict__ cursor, const uint32_t* __restrict__ offsets,
                               float4* __restrict__ sorted, uint32_t* __restrict__ err, uint32_t* sh)
 {
-    const uint32_t* row = hist + (size_t)c * p.nBins;
-    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = offsets[b] + row[b];
+    for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x) sh[b] = 0u;
     const uint32_t total = offsets[p.nBins];
     __syncthreads();
 
-    for_chunk(samples, n, p, c, nc, [&](bool valid, const float4& rec, uint32_t key, int) {
-        if(valid && key != kOutOfRange) {
-            const uint32_t pos = atomicAdd(&sh[key], 1u);
-            float4 out = rec;
+    for_chunk(samples, n, p, c, nc, [&](const bool* valid, const float4* rec, const uint32_t* key, const int*) {
+        uint32_t rank[kTileLoads];
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++)
+            rank[u] = (valid[u] && key[u] != kOutOfRange) ? atomicAdd(&sh[key[u]], 1u) : UINT_MAX;
+        __syncthreads();
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++)
+            if(rank[u] == 0u) sh[key[u]] = atomicAdd(&cursor[(size_t)key[u] * kCursorStride], sh[key[u]]);
+        __syncthreads();
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            if(rank[u] == UINT_MAX) continue;
+            const uint32_t pos = sh[key[u]] + rank[u];
+            float4 out = rec[u];
             if(p.echo_flags) {
-                const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z);
+                const float2 v = apply_echo(p, make_float2(out.x, out.y), out.z);
                 out.x = v.x; out.y = v.y;
             }
             if(pos < total) sorted[pos] = out;
             else atomicOr(err, kErrScatterOverflow);
         }
+        __syncthreads();
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++)
+            if(rank[u] == 0u) sh[key[u]] = 0u;
+        __syncthreads();
     });
 }
 
 namespace {
 
 __global__ void k_scatter(const float* __restrict__ samples, uint64_t n, BinParams p,
-                          const uint32_t* __restrict__ hist, const uint32_t* __restrict__ offsets,
+                          uint32_t* __restrict__ cursor, const uint32_t* __restrict__ offsets,
                           float4* __restrict__ sorted, uint32_t* __restrict__ err)
 {
     extern __shared__ uint32_t sh[];
-    scatter_chunk(samples, n, p, blockIdx.x, gridDim.x, hist, offsets, sorted, err, sh);
+    scatter_chunk(samples, n, p, blockIdx.x, gridDim.x, cursor, offsets, sorted, err, sh);
 }
 
 __device__ __forceinline__ uint32_t bin_count(const uint32_t* off, uint32_t nBB, int j)
@@ -319,20 +341,22 @@ __global__ void k_count_batch(const PingDev* __restrict__ pings, const uint2* __
     __shared__ unsigned long long s_oor[2];
     const uint2 m = map[blockIdx.x];
     const PingDev& P = pings[m.x];
-    count_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.hist, P.oor, sh, s_oor);
+    count_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.totals, P.oor, sh, s_oor);
 }
 
-__global__ void k_colscan_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
+// Zeroes every ping's bin totals (one thread per (ping, bin)).
+__global__ void k_zero_totals_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
 {
     const uint2 m = map[blockIdx.x];
     const PingDev& P = pings[m.x];
-    colscan_bin(P.hist, P.chunks, P.bin.nBins, P.totals, m.y * blockDim.x + threadIdx.x);
+    const uint32_t b = m.y * blockDim.x + threadIdx.x;
+    if(b < P.bin.nBins) P.totals[b] = 0u;
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_binscan_batch(const PingDev* __restrict__ pings)
 {
     const PingDev& P = pings[blockIdx.x];
-    binscan_cta(P.totals, P.bin.nBins, P.offsets);
+    binscan_cta(P.totals, P.bin.nBins, P.offsets, P.hist);
 }
 
 __global__ void k_scatter_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
@@ -340,7 +364,7 @@ __global__ void k_scatter_batch(const PingDev* __restrict__ pings, const uint2* 
     extern __shared__ uint32_t sh[];
     const uint2 m = map[blockIdx.x];
     const PingDev& P = pings[m.x];
-    scatter_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.hist, P.offsets, P.sorted, P.err, sh);
+    scatter_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.hist, P.offsets, P.sorted, P.err, sh);   // hist = cursors
 }
 
 __global__ void k_windows_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
@@ -356,12 +380,12 @@ __global__ void k_reset_batch(const PingDev* __restrict__ pings, uint32_t n_ping
     if(i < n_pings) { pings[i].oor[0] = 0ull; pings[i].oor[1] = 0ull; }
 }
 
-uint32_t hist_grid(const Context& ctx, uint64_t n)
+uint32_t hist_grid(uint32_t ctas, uint64_t n)
 {
-    // At least ~8192 samples per CTA so that the per-CTA histogram rows stay
-    // small relative to the data.
+    // At least ~8192 samples per CTA so that the per-CTA histogram set-up
+    // stays small relative to the data.
     const uint64_t want = std::max<uint64_t>(1, (n + 8191) / 8192);
-    return (uint32_t)std::min<uint64_t>(ctx.hist_ctas, want);
+    return (uint32_t)std::min<uint64_t>(ctas, want);
 }
 
 #define RTACX_CUDA(call)                                                         \
@@ -400,24 +424,25 @@ rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStre
         RTACX_CUDA(cudaMemsetAsync(ctx.d_offsets, 0, (p.nBins + 1) * sizeof(uint32_t), stream));
     }
     else {
-        const uint32_t grid = hist_grid(ctx, n);
+        const uint32_t grid = hist_grid(ctx.hist_ctas, n);
         const size_t smem = (size_t)p.nBins * sizeof(uint32_t);
         const float* s = static_cast<const float*>(samples);
+        ctx.mark(1, false, stream);
+        RTACX_CUDA(cudaMemsetAsync(ctx.d_totals, 0, p.nBins * sizeof(uint32_t), stream));
+        ctx.mark(1, true, stream);
         ctx.mark(0, false, stream);
-        k_count<<<grid, ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist, ctx.d_oor);
+        k_count<<<grid, ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_totals, ctx.d_oor);
         RTACX_CUDA(cudaGetLastError());
         ctx.mark(0, true, stream);
-        ctx.mark(1, false, stream);
-        k_colscan<<<(p.nBins + 255) / 256, 256, 0, stream>>>(ctx.d_hist, grid, p.nBins, ctx.d_totals);
-        RTACX_CUDA(cudaGetLastError());
-        ctx.mark(1, true, stream);
         ctx.mark(2, false, stream);
-        k_binscan<<<1, kScanThreads, 0, stream>>>(ctx.d_totals, p.nBins, ctx.d_offsets);
+        // d_hist holds the per-bin write cursors of the scatter.
+        k_binscan<<<1, kScanThreads, 0, stream>>>(ctx.d_totals, p.nBins, ctx.d_offsets, ctx.d_hist);
         RTACX_CUDA(cudaGetLastError());
         ctx.mark(2, true, stream);
         ctx.mark(3, false, stream);
-        k_scatter<<<grid, ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets,
-                                                             ctx.d_sorted, ctx.d_err);
+        k_scatter<<<hist_grid(ctx.scatter_ctas, n), ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist,
+                                                                                       ctx.d_offsets, ctx.d_sorted,
+                                                                                       ctx.d_err);
         RTACX_CUDA(cudaGetLastError());
         ctx.mark(3, true, stream);
     }
@@ -469,8 +494,8 @@ rtacx_status launch_bin_batch(std::string& error, const PingDev* pings, uint32_t
 {
     const size_t smem = (size_t)max_bins * sizeof(uint32_t);
     k_reset_batch<<<(n_pings + 255) / 256, 256, 0, stream>>>(pings, n_pings);
+    k_zero_totals_batch<<<n_col, 256, 0, stream>>>(pings, col_map);
     k_count_batch<<<n_chunks, 512, smem, stream>>>(pings, chunk_map);
-    k_colscan_batch<<<n_col, 256, 0, stream>>>(pings, col_map);
     k_binscan_batch<<<n_pings, kScanThreads, 0, stream>>>(pings);
     k_scatter_batch<<<n_chunks, 512, smem, stream>>>(pings, chunk_map);
     k_windows_batch<<<n_win, 256, 0, stream>>>(pings, win_map);
@@ -482,7 +507,7 @@ rtacx_status launch_bin_batch(std::string& error, const PingDev* pings, uint32_t
 // Exclusive scan of n u32 values into out[0, n] (out[n] = total), one CTA.
 void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t stream)
 {
-    k_binscan<<<1, kScanThreads, 0, stream>>>(in, n, out);
+    k_binscan<<<1, kScanThreads, 0, stream>>>(in, n, out, nullptr);
 }
 
 // Launch shape of the count / scatter passes for the configured bin count.
@@ -491,12 +516,22 @@ void configure_hist_launch(Context& ctx)
     const size_t smem = (size_t)ctx.bin.nBins * sizeof(uint32_t);
     cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
     cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
-    // One 1024-thread CTA per SM: every (CTA, bin) pair keeps one partially
-    // written 128-byte line of the sorted array open in L2 while the scatter
-    // runs, so fewer CTAs keep that working set (CTAs x bins x 128 B) inside
-    // L2 and the scattered records merge into whole lines before eviction.
-    ctx.hist_threads = 1024;
-    ctx.hist_ctas = (uint32_t)ctx.sm_count;
+    // 512-thread CTAs when two histograms fit in one SM's shared memory, one
+    // 1024-thread CTA otherwise; each pass gets as many CTAs as are resident
+    // at once (registers and shared memory), so that the scatter's per-tile
+    // reservation phases of different CTAs overlap and no CTA waits for a
+    // second wave.
+    const size_t per_sm = 200u * 1024u;
+    ctx.hist_threads = per_sm / (smem + 1024) >= 2 ? 512 : 1024;
+    auto resident = [&](const void* fn) {
+        int nb = 0;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, (int)ctx.hist_threads, std::max<size_t>(smem, 1)) !=
+               cudaSuccess || nb < 1)
+            nb = 1;
+        return (uint32_t)ctx.sm_count * (uint32_t)std::min(nb, 4);
+    };
+    ctx.hist_ctas = resident((const void*)k_count);
+    ctx.scatter_ctas = resident((const void*)k_scatter);
     cudaGetLastError();
 }
 

@@ -12,6 +12,9 @@
 
 namespace rtacx {
 
+// Words between two bins' write cursors: one 128-byte L2 line per bin, so the
+// scatter's run reservations spread over all L2 slices.
+constexpr uint32_t kCursorStride = 32;
 constexpr uint32_t kOutOfRange = RTACX_KEY_OUT_OF_RANGE;
 
 // Device error word bits (OR-ed by kernels, read by rtacx_stream_status).
@@ -192,10 +195,11 @@ struct Context {
     // Sample-sized scratch.
     uint64_t capacity = 0;              // samples the sorted scratch holds
     float4* d_sorted = nullptr;
-    uint32_t hist_ctas = 0;             // CTAs of the count / scatter passes
+    uint32_t hist_ctas = 0;             // CTAs of the count pass (and of the batched passes)
+    uint32_t scatter_ctas = 0;          // CTAs of the scatter pass
     uint32_t hist_threads = 0;
     size_t hist_cols = 0;               // allocated CTA x bin entries
-    uint32_t* d_hist = nullptr;         // [hist_ctas][nBins]
+    uint32_t* d_hist = nullptr;         // [nBins][kCursorStride]: the scatter's per-bin write cursors
 
     // Split persistent gather of 2D pings (see rtacx_reduce.cu).
     uint32_t* d_tile_parts = nullptr;   // [tiles] parts per output tile

@@ -53,6 +53,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kOffSorted  = 0;
 constexpr size_t kOffHist    = align256(kOffSorted + kMaxSamples * sizeof(float4));
 constexpr size_t kOffOffsets = align256(kOffHist + (size_t)kMaxHistCtas * kMaxBins * 4);
+static_assert(kMaxHistCtas >= kCursorStride, "cursor region of the static scratch");
 constexpr size_t kOffTotals  = align256(kOffOffsets + (kMaxBins + 1) * 4);
 constexpr size_t kOffWin     = align256(kOffTotals + kMaxBins * 4);
 constexpr size_t kOffOor     = align256(kOffWin + kMaxRanges * sizeof(int2));
@@ -246,7 +247,7 @@ extern "C" rtacx_status rtacx_reduce_noalloc(int sample_kind, const void* sensor
     ctx.d_bb_tiles = reinterpret_cast<int2*>(base + kOffTiles);
     configure_hist_launch(ctx);
     ctx.hist_ctas = std::min(ctx.hist_ctas, kMaxHistCtas);
-    ctx.hist_cols = (size_t)ctx.hist_ctas * ctx.bin.nBins;
+    ctx.hist_cols = (size_t)ctx.bin.nBins * kCursorStride;
 
     // Upload this call's tables (pageable copies: the staging above may be
     // reused as soon as these return) and clear the error word.
