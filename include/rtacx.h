@@ -186,6 +186,19 @@ rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_des
 rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n,
                                     float* out, void* stream);
 
+/* The precision form from HOST memory, the end-to-end call of a host-side
+ * caller (the reference fills `samples()` from host vectors before
+ * SensorInstance::compute_output(), include/rtac_simulation/SensorInstance.h:67,
+ * and reads `output()` back). `samples` holds n host records (pinned memory
+ * lets the copies overlap); they are copied to the device in chunks of
+ * RTACX_STREAM_CHUNK records through two staging buffers on an internal copy
+ * stream, each copy overlapping the accumulation of the previous chunk, and
+ * the ping is copied to `out` (host, range_count x bearing_count complex64).
+ * Stream-ordered on `stream`: `out` is valid once the stream completes. */
+#define RTACX_STREAM_CHUNK (1u << 21)
+rtacx_status rtacx_reduce_precision_host(rtacx_ctx* ctx, const void* samples, uint64_t n,
+                                         float* out, void* stream);
+
 /* Echo-sample epilogue (no counterpart in this path of the reference: it
  * restates the ray generator's and receiver's per-hit arithmetic,
  * src/RayCaster.cu:49-81 and include/rtac_simulation/Receiver.h:51-60, so

@@ -75,6 +75,7 @@ SIGNATURES = {
     "rtacx_set_echo_model": (_I, [_P, _P]),
     "rtacx_configure_precision": (_I, [_P, _P]),
     "rtacx_reduce_precision": (_I, [_P, _P, _U64, _P, _P]),
+    "rtacx_reduce_precision_host": (_I, [_P, _P, _U64, _P, _P]),
     "rtacx_configure_receiver": (_I, [_P, _P]),
     "rtacx_make_samples": (_I, [_P, _P, _U64, _P, _P]),
     "rtacx_directivity_table": (_I, [_I, ctypes.POINTER(ctypes.c_float), _P, ctypes.POINTER(_U32),
@@ -273,6 +274,10 @@ class Context:
 
     def reduce_precision(self, samples, n: int, out, stream=None) -> None:
         self._check(self._lib.rtacx_reduce_precision(self._h, _ptr(samples), n, _ptr(out), _stream(stream)))
+
+    def reduce_precision_host(self, samples, n: int, out, stream=None) -> None:
+        """samples / out: host buffers (pinned for overlapped copies)."""
+        self._check(self._lib.rtacx_reduce_precision_host(self._h, _ptr(samples), n, _ptr(out), _stream(stream)))
 
     def configure_receiver(self, rotation=None, directivity=None, carrier_hz: float = 0.0, flags: int = 0) -> None:
         R = np.eye(3, dtype=np.float32) if rotation is None else np.asarray(rotation, np.float32).reshape(3, 3)

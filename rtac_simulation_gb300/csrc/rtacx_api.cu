@@ -178,6 +178,7 @@ void rtacx_destroy(rtacx_ctx* ctx)
     free_dev(c.d_sorted);
     free_dev(c.d_dir);
     free_dev(c.d_rast_v); free_dev(c.d_rast_vis); free_dev(c.d_rast_large);
+    free_streaming(c);
     free_dev(c.d_err);
     free_dev(c.d_oor);
     for(cudaEvent_t& e : c.events) if(e) cudaEventDestroy(e);

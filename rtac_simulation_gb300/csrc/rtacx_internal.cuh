@@ -50,16 +50,47 @@ struct BinParams {
 // that is as exact for this range: t * k_hi split into its rounded product
 // and the exact rounding error (fmaf), the integer part removed from the
 // rounded product (exact below 2^23 cycles), the small terms added last.
+// float -> double from the IEEE-754 bit fields (exact; the FP64 pipe is not
+// used). Zero and subnormal inputs give a signed zero; infinities and NaNs
+// do not reach the callers (their keys are out of range).
+__device__ __forceinline__ double f64_from_f32_fields(float x)
+{
+    const uint32_t u = __float_as_uint(x);
+    const uint32_t e = (u >> 23) & 0xffu;
+    if(e == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    const uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)((u & 7u) << 29));
+}
+
+// double -> float from the bit fields, mantissa truncated toward zero
+// (relative error below 2^-23); magnitudes under 2^-126 give a signed zero.
+// Valid for |x| < 2^128.
+__device__ __forceinline__ float f32_from_f64_fields(double x)
+{
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if(e <= 896u) return __uint_as_float(hi & 0x80000000u);
+    return __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
+// Carrier phase in cycles, reduced to about [-0.5, 0.5]: travel * 2 f / c
+// minus the nearest whole number of cycles.
+//   default      one FP64 fused multiply-add, travel * k - n, with n the
+//                float-rounded cycle count: the reduction itself is exact to
+//                2^-53 and it is the only FP64-pipe instruction per sample
+//                (the conversions are integer bit operations).
+//   compensated  no FP64: the float product's exact residual (fmaf) plus the
+//                low part of k.
 __device__ __forceinline__ float carrier_fraction(const BinParams& p, float travel)
 {
+    const float prod = travel * p.echo_k_hi;
     if(p.echo_flags & RTACX_ECHO_PHASE_COMPENSATED) {
-        const float prod = travel * p.echo_k_hi;
         const float err = fmaf(travel, p.echo_k_hi, -prod);
         const float whole = prod - rintf(prod);
         return whole + fmaf(travel, p.echo_k_lo, err);
     }
-    const double cyc = (double)travel * p.echo_cycles;
-    return (float)(cyc - rint(cyc));
+    const double r = fma(f64_from_f32_fields(travel), p.echo_cycles, -f64_from_f32_fields(rintf(prod)));
+    return f32_from_f64_fields(r);
 }
 
 __device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel)
@@ -197,6 +228,8 @@ struct Context {
     float4* d_sorted = nullptr;
     uint32_t hist_ctas = 0;             // CTAs of the count pass (and of the batched passes)
     uint32_t scatter_ctas = 0;          // CTAs of the scatter pass
+    size_t acc_smem = 0;                // dynamic shared memory of the precision accumulation
+    uint32_t acc_blocks_per_sm = 1;
     uint32_t hist_threads = 0;
     size_t hist_cols = 0;               // allocated CTA x bin entries
     uint32_t* d_hist = nullptr;         // [nBins][kCursorStride]: the scatter's per-bin write cursors
@@ -238,6 +271,16 @@ struct Context {
     uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity
     float* d_C = nullptr;               // [Mpad][Npad] GEMM output when the ping shape is not tile-aligned
     float2* d_taps = nullptr;           // [taps] range taps at bin offsets t - tap_center
+
+    // Host-buffer streaming (rtacx_reduce_precision_host): two device staging
+    // buffers of RTACX_STREAM_CHUNK records, a copy stream fork-joined to the
+    // caller's stream, and a device ping copied back to the host.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t stream_ev[5] = {};      // fork, copied[2], used[2]
+    unsigned char* d_stage[2] = {};
+    size_t stage_bytes = 0;
+    float* d_ping = nullptr;
+    size_t ping_floats = 0;
 
     // Stage tracing: events[2 * i], events[2 * i + 1] bracket stage i.
     bool tracing = false;
@@ -281,6 +324,10 @@ int gather_shape_bearings(int shape);
 
 // Precision form (rtacx_precision.cu).
 rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float* out, cudaStream_t stream);
+rtacx_status precision_begin(Context& ctx, cudaStream_t stream);
+rtacx_status precision_accumulate(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream);
+rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream);
+void free_streaming(Context& ctx);
 void free_precision(Context& ctx);
 
 // Tensor-core GEMM (rtacx_umma.cu): C = A * B^T, bf16 K-major operands.

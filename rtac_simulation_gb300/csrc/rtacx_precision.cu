@@ -45,46 +45,68 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float4 v)
 // The bearing cell comes from a uniform lookup grid (lut[c] = the table
 // index at or below the grid line c), corrected by exact comparisons with the
 // table, so it equals the largest k in [0, nB - 2] with theta_k <= theta.
+// Shared memory (dynamic, sized by nB and nR): per table bearing one 16-byte
+// cell {theta_k, 1 / (theta_k+1 - theta_k), theta_k+1, 0}, so the common case
+// (lookup already exact) costs one 16-byte shared load; the bitmap; the
+// lookup grid as int16.
 constexpr int kMaxRangeWords = 8192 / 32 * 4;   // bitmap words for up to 32768 range bins
 constexpr int kLutCells = 4 * kMaxBearingsSmem;
+constexpr int kAccThreads = 256;
+constexpr int kAccLoads = 4;                     // independent record loads per thread in flight
 
-__global__ void __launch_bounds__(256)
+size_t accumulate_smem_bytes(uint32_t nB, uint32_t nR, uint32_t lut_cells)
+{
+    return (size_t)nB * sizeof(float4) + (size_t)((nR + 31) / 32) * sizeof(uint32_t) + (size_t)lut_cells * sizeof(int16_t);
+}
+
+__global__ void __launch_bounds__(kAccThreads)
 k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
                   const float* __restrict__ bearings, uint32_t nB, const int* __restrict__ lut,
                   uint32_t lut_cells, float lut_origin, float lut_scale,
                   float4* __restrict__ P, uint32_t* __restrict__ nonempty)
 {
-    __shared__ float s_th[kMaxBearingsSmem];
-    __shared__ float s_inv[kMaxBearingsSmem];     // 1 / (theta_k+1 - theta_k)
-    __shared__ int16_t s_lut[kLutCells];
-    __shared__ uint32_t s_bits[kMaxRangeWords];
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    float4* s_cell = reinterpret_cast<float4*>(s_raw);
     const uint32_t words = (p.key.nR + 31) / 32;
+    uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_cell + nB);
+    int16_t* s_lut = reinterpret_cast<int16_t*>(s_bits + words);
     for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) {
-        s_th[i] = bearings[i];
-        s_inv[i] = (i + 1 < nB) ? 1.0f / (bearings[i + 1] - bearings[i]) : 0.0f;
+        const float th = bearings[i];
+        const bool last = i + 1 >= nB;
+        s_cell[i] = make_float4(th, last ? 0.0f : 1.0f / (bearings[i + 1] - th), last ? INFINITY : bearings[i + 1], 0.0f);
     }
     for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = (int16_t)lut[i];
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
     __syncthreads();
     const int kmax = (int)nB - 2;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float4 rec = load_record(samples, i, p);
-        int side;
-        const uint32_t j = range_key(p.key, rec.z, side);
-        if(j == kOutOfRange) continue;
-        const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z);
-        atomicOr(&s_bits[j >> 5], 1u << (j & 31));
-        if(nB == 1) { red_add_v4(P + j, make_float4(v.x, v.y, 0.f, 0.f)); continue; }
-        const float th = rec.w;
-        const float q = fminf(fmaxf((th - lut_origin) * lut_scale, 0.0f), (float)(lut_cells - 1));
-        int k = s_lut[(int)q];                       // NaN bearings: q = 0
-        while(k < kmax && s_th[k + 1] <= th) k++;
-        while(k > 0 && !(s_th[k] <= th)) k--;
-        float w = (th - s_th[k]) * s_inv[k];
-        w = fminf(fmaxf(w, 0.0f), 1.0f);          // NaN bearings -> 0
-        const float w0 = 1.0f - w;
-        red_add_v4(P + (size_t)j * nB + k, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y));
+    for(uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < n; i0 += stride * kAccLoads) {
+        float4 rec[kAccLoads];
+#pragma unroll
+        for(int u = 0; u < kAccLoads; u++) {
+            const uint64_t i = i0 + (uint64_t)u * stride;
+            rec[u] = i < n ? load_record(samples, i, p) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for(int u = 0; u < kAccLoads; u++) {
+            if(i0 + (uint64_t)u * stride >= n) continue;
+            int side;
+            const uint32_t j = range_key(p.key, rec[u].z, side);
+            if(j == kOutOfRange) continue;
+            const float2 v = apply_echo(p, make_float2(rec[u].x, rec[u].y), rec[u].z);
+            atomicOr(&s_bits[j >> 5], 1u << (j & 31));
+            if(nB == 1) { red_add_v4(P + j, make_float4(v.x, v.y, 0.f, 0.f)); continue; }
+            const float th = rec[u].w;
+            const float q = fminf(fmaxf((th - lut_origin) * lut_scale, 0.0f), (float)(lut_cells - 1));
+            int k = s_lut[(int)q];                       // NaN bearings: q = 0
+            float4 c = s_cell[k];
+            while(k < kmax && c.z <= th) c = s_cell[++k];
+            while(k > 0 && !(c.x <= th)) c = s_cell[--k];
+            float w = (th - c.x) * c.y;
+            w = fminf(fmaxf(w, 0.0f), 1.0f);          // NaN bearings -> 0
+            const float w0 = 1.0f - w;
+            red_add_v4(P + (size_t)j * nB + k, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y));
+        }
     }
     __syncthreads();
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x)
@@ -123,79 +145,115 @@ __device__ __forceinline__ uint16_t bf16_bits(float x)
 
 __device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
 
-constexpr int kFiltRows = 32, kFiltCols = 64, kFiltTaps = 56;
+constexpr int kFiltRows = 64, kFiltCols = 64, kFiltTapsMax = 64, kFiltThreads = 256;
 
-// Range filter + split. One CTA per 32 rows x 64 bearings; the binned grid
-// rows a chunk of taps needs are staged in shared memory once (formed from
-// the pair cells), then each thread filters its 4 rows x 2 bearings and
-// writes the bf16 A operand [hi | hi | lo] of its outputs.
-__global__ void __launch_bounds__(256)
+size_t filter_smem_bytes(uint32_t ntaps)
+{
+    const size_t nt = std::min<uint32_t>(std::max<uint32_t>(ntaps, 1u), (uint32_t)kFiltTapsMax);
+    return (kFiltRows + nt - 1) * kFiltCols * sizeof(float2) + kFiltTapsMax * sizeof(float2) + kFiltRows * sizeof(int2);
+}
+
+// Range filter + split. One CTA per 64 rows x 64 bearings. Per chunk of up
+// to 64 taps, the binned grid rows the chunk needs are staged in shared
+// memory once: each warp reads a row's pair cells with one 16-byte load per
+// cell and forms G[j][k] = P[j][k].xy + P[j][k - 1].zw with the neighbour
+// lane's cell (lane 0 loads its left neighbour). Each thread then filters 8
+// rows x 2 adjacent bearings and writes the bf16 A operand [hi | hi | lo],
+// two bearings per 4-byte store.
+__global__ void __launch_bounds__(kFiltThreads, 4)
 k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const float2* __restrict__ taps,
               uint32_t ntaps, uint32_t center, uint32_t nR, uint32_t nB, uint32_t Kp, uint16_t* __restrict__ A)
 {
-    __shared__ float2 sG[kFiltRows + kFiltTaps - 1][kFiltCols];
-    __shared__ float2 sT[kFiltTaps];
-    __shared__ int2 sW[kFiltRows];
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int ntc = min((int)max(ntaps, 1u), kFiltTapsMax);
+    float2* sG = reinterpret_cast<float2*>(s_raw);                    // [kFiltRows + ntc - 1][kFiltCols]
+    float2* sT = sG + (size_t)(kFiltRows + ntc - 1) * kFiltCols;       // [kFiltTapsMax]
+    int2* sW = reinterpret_cast<int2*>(sT + kFiltTapsMax);              // [kFiltRows]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols;
     if(tid < kFiltRows) sW[tid] = (r0 + tid < (int)nR) ? win[r0 + tid] : make_int2(1, 0);
-    float2 acc[4][2];
+    float2 acc[8][2];
 #pragma unroll
-    for(int q = 0; q < 4; q++) { acc[q][0] = make_float2(0.f, 0.f); acc[q][1] = make_float2(0.f, 0.f); }
+    for(int q = 0; q < 8; q++) { acc[q][0] = make_float2(0.f, 0.f); acc[q][1] = make_float2(0.f, 0.f); }
 
-    for(int tc = 0; tc < (int)ntaps; tc += kFiltTaps) {
-        const int nt = min(kFiltTaps, (int)ntaps - tc);
+    for(int tc = 0; tc < (int)ntaps; tc += ntc) {
+        const int nt = min(ntc, (int)ntaps - tc);
         const int jlo = r0 + tc - (int)center;          // bin of sG row 0
+        const int rows_s = kFiltRows + nt - 1;
         __syncthreads();
         if(tid < nt) sT[tid] = taps[tc + tid];
-        for(int idx = tid; idx < (kFiltRows + nt - 1) * kFiltCols; idx += 256) {
-            const int rr = idx / kFiltCols, kk = idx % kFiltCols;
-            const int j = jlo + rr, k = k0 + kk;
-            float2 g = make_float2(0.f, 0.f);
-            if(j >= 0 && j < (int)nR && k < (int)nB) {
-                const float4 a = P[(size_t)j * nB + k];
-                g = make_float2(a.x, a.y);
-                if(k > 0) {
-                    const float4 b = P[(size_t)j * nB + k - 1];
-                    g.x += b.z; g.y += b.w;
-                }
+#pragma unroll 2
+        for(int rr = warp; rr < rows_s; rr += kFiltThreads / 32) {
+            const int j = jlo + rr;
+            const bool jok = j >= 0 && j < (int)nR;
+            const float4* row = P + (size_t)(jok ? j : 0) * nB;
+            float4 c[2];
+#pragma unroll
+            for(int h = 0; h < 2; h++) {
+                const int k = k0 + 32 * h + lane;
+                c[h] = (jok && k < (int)nB) ? row[k] : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            sG[rr][kk] = g;
+            const float4 lead = (jok && lane == 0 && k0 > 0) ? row[k0 - 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for(int h = 0; h < 2; h++) {
+                float zx = __shfl_up_sync(0xffffffffu, c[h].z, 1), zy = __shfl_up_sync(0xffffffffu, c[h].w, 1);
+                const float ex = __shfl_sync(0xffffffffu, c[0].z, 31), ey = __shfl_sync(0xffffffffu, c[0].w, 31);
+                if(lane == 0) {
+                    zx = h == 0 ? lead.z : ex;
+                    zy = h == 0 ? lead.w : ey;
+                }
+                const int k = k0 + 32 * h + lane;
+                float2 g = make_float2(c[h].x, c[h].y);
+                if(k > 0) { g.x += zx; g.y += zy; }
+                sG[rr * kFiltCols + 32 * h + lane] = g;
+            }
         }
         __syncthreads();
 #pragma unroll
-        for(int q = 0; q < 4; q++) {
-            const int rr = warp * 4 + q, r = r0 + rr;
+        for(int q = 0; q < 8; q++) {
+            const int rr = warp * 8 + q, r = r0 + rr;
             const int2 w = sW[rr];
             if(w.x > w.y) continue;
             // taps t (absolute) with bin j = r + t - center inside the window
             const int tlo = max(tc, w.x - r + (int)center), thi = min(tc + nt - 1, w.y - r + (int)center);
             for(int t = tlo; t <= thi; t++) {
                 const float2 c = sT[t - tc];
-#pragma unroll
-                for(int h = 0; h < 2; h++) {
-                    const float2 g = sG[rr + t - tc][lane + 32 * h];
-                    acc[q][h].x = fmaf(c.x, g.x, fmaf(-c.y, g.y, acc[q][h].x));
-                    acc[q][h].y = fmaf(c.x, g.y, fmaf(c.y, g.x, acc[q][h].y));
-                }
+                const float4 g2 = *reinterpret_cast<const float4*>(&sG[(rr + t - tc) * kFiltCols + 2 * lane]);
+                acc[q][0].x = fmaf(c.x, g2.x, fmaf(-c.y, g2.y, acc[q][0].x));
+                acc[q][0].y = fmaf(c.x, g2.y, fmaf(c.y, g2.x, acc[q][0].y));
+                acc[q][1].x = fmaf(c.x, g2.z, fmaf(-c.y, g2.w, acc[q][1].x));
+                acc[q][1].y = fmaf(c.x, g2.w, fmaf(c.y, g2.z, acc[q][1].y));
             }
         }
     }
+    const int k = k0 + 2 * lane;
+    const bool packed = (nB & 1u) == 0u && k + 1 < (int)nB;
 #pragma unroll
-    for(int q = 0; q < 4; q++) {
-        const int r = r0 + warp * 4 + q;
-        if(r >= (int)nR) continue;
+    for(int q = 0; q < 8; q++) {
+        const int r = r0 + warp * 8 + q;
+        if(r >= (int)nR || k >= (int)nB) continue;
         uint16_t* row = A + (size_t)r * Kp;
+        uint16_t hr[2], hi[2], lr[2], li[2];
 #pragma unroll
         for(int h = 0; h < 2; h++) {
-            const int k = k0 + lane + 32 * h;
-            if(k >= (int)nB) continue;
             const float2 v = acc[q][h];
-            const uint16_t hr = bf16_bits(v.x), hi = bf16_bits(v.y);
-            const uint16_t lr = bf16_bits(v.x - bf16_value(hr)), li = bf16_bits(v.y - bf16_value(hi));
-            row[k] = hr;               row[nB + k] = hi;
-            row[2 * nB + k] = hr;      row[3 * nB + k] = hi;
-            row[4 * nB + k] = lr;      row[5 * nB + k] = li;
+            hr[h] = bf16_bits(v.x); hi[h] = bf16_bits(v.y);
+            lr[h] = bf16_bits(v.x - bf16_value(hr[h])); li[h] = bf16_bits(v.y - bf16_value(hi[h]));
+        }
+        if(packed) {
+            auto put = [&](uint32_t off, const uint16_t* v2) {
+                *reinterpret_cast<uint32_t*>(row + off + k) = (uint32_t)v2[0] | ((uint32_t)v2[1] << 16);
+            };
+            put(0, hr); put(nB, hi); put(2 * nB, hr); put(3 * nB, hi); put(4 * nB, lr); put(5 * nB, li);
+        }
+        else {
+#pragma unroll
+            for(int h = 0; h < 2; h++) {
+                if(k + h >= (int)nB) continue;
+                row[k + h] = hr[h];            row[nB + k + h] = hi[h];
+                row[2 * nB + k + h] = hr[h];   row[3 * nB + k + h] = hi[h];
+                row[4 * nB + k + h] = lr[h];   row[5 * nB + k + h] = li[h];
+            }
         }
     }
 }
@@ -327,6 +385,24 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     ctx.lut_cells = cells;
     ctx.lut_origin = origin;
     ctx.lut_scale = lscale;
+    ctx.acc_smem = accumulate_smem_bytes(nB, nR, cells);
+    int acc_blocks = 0;
+    if(cudaFuncSetAttribute(k_prec_accumulate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.acc_smem) !=
+           cudaSuccess ||
+       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&acc_blocks, k_prec_accumulate, kAccThreads, ctx.acc_smem) !=
+           cudaSuccess ||
+       acc_blocks < 1) {
+        cudaGetLastError();
+        ctx.error = "cannot reserve shared memory for the accumulation tables";
+        return RTACX_ERR_CUDA;
+    }
+    ctx.acc_blocks_per_sm = (uint32_t)acc_blocks;
+    if(cudaFuncSetAttribute(k_prec_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
+        cudaGetLastError();
+        ctx.error = "cannot reserve shared memory for the range filter";
+        return RTACX_ERR_CUDA;
+    }
 
     // GEMM operand shapes.
     ctx.Mpad = (nR + 127) / 128 * 128;
@@ -380,26 +456,51 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     return RTACX_OK;
 }
 
+// Zeroes the pair cells and the non-empty bitmap of a new ping.
+rtacx_status precision_begin(Context& ctx, cudaStream_t stream)
+{
+    RTACX_CUDA(cudaMemsetAsync(ctx.d_G, 0, (size_t)ctx.nR * ctx.nB * sizeof(float4), stream));
+    RTACX_CUDA(cudaMemsetAsync(ctx.d_flags, 0, (size_t)(ctx.nR + 31) / 32 * 4, stream));
+    return RTACX_OK;
+}
+
+// Adds n samples to the ping's pair cells (order-independent, so a ping may
+// be accumulated in any number of chunks).
+rtacx_status precision_accumulate(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream)
+{
+    if(!n) return RTACX_OK;
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + kAccThreads * kAccLoads - 1) / (kAccThreads * kAccLoads),
+                                                         (uint64_t)ctx.sm_count * ctx.acc_blocks_per_sm);
+    k_prec_accumulate<<<blocks, kAccThreads, ctx.acc_smem, stream>>>(static_cast<const float*>(samples), n, ctx.bin,
+                                                                     ctx.d_bearings, ctx.nB, ctx.d_lut, ctx.lut_cells,
+                                                                     ctx.lut_origin, ctx.lut_scale, ctx.d_G, ctx.d_flags);
+    RTACX_CUDA(cudaGetLastError());
+    return RTACX_OK;
+}
+
+rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream);
+
 rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float* out, cudaStream_t stream)
 {
-    const uint32_t nR = ctx.nR, nB = ctx.nB;
     ctx.mark(0, false, stream);
-    RTACX_CUDA(cudaMemsetAsync(ctx.d_G, 0, (size_t)nR * nB * sizeof(float4), stream));
-    RTACX_CUDA(cudaMemsetAsync(ctx.d_flags, 0, (size_t)(nR + 31) / 32 * 4, stream));
-    if(n) {
-        const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx.sm_count * 6);
-        k_prec_accumulate<<<blocks, 256, 0, stream>>>(static_cast<const float*>(samples), n, ctx.bin,
-                                                      ctx.d_bearings, nB, ctx.d_lut, ctx.lut_cells, ctx.lut_origin,
-                                                      ctx.lut_scale, ctx.d_G, ctx.d_flags);
-        RTACX_CUDA(cudaGetLastError());
-    }
+    rtacx_status st = precision_begin(ctx, stream);
+    if(st == RTACX_OK) st = precision_accumulate(ctx, samples, n, stream);
+    if(st != RTACX_OK) return st;
     ctx.mark(0, true, stream);
+    return precision_finish(ctx, out, stream);
+}
+
+// Windows, range filter + split, tensor-core contraction into `out`.
+rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
+{
+    const uint32_t nR = ctx.nR, nB = ctx.nB;
     ctx.mark(1, false, stream);
     k_prec_windows<<<(nR + 255) / 256, 256, 0, stream>>>(ctx.d_flags, nR, ctx.overlap, ctx.d_pwin);
     RTACX_CUDA(cudaGetLastError());
     ctx.mark(1, true, stream);
     ctx.mark(2, false, stream);
-    k_prec_filter<<<dim3((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows), 256, 0, stream>>>(
+    k_prec_filter<<<dim3((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows), kFiltThreads,
+                    filter_smem_bytes(ctx.taps), stream>>>(
         ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, ctx.d_A);
     RTACX_CUDA(cudaGetLastError());
     ctx.mark(2, true, stream);

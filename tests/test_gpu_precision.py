@@ -127,3 +127,46 @@ def test_compensated_phase_matches_fp64_oracle(oracle, form):
         ctx.configure_precision(D, taps, c)
         got = gpu_precision(ctx, wk.samples, wk.out_shape)
         assert rel_l2(got, oracle.reduce_binned(exact, wk.sensor, D, taps, c)) <= TOL
+
+
+def gpu_precision_host(ctx, samples, out_shape, pinned=True):
+    """The host-buffer entry point: pinned host samples in, host ping out."""
+    h = torch.from_numpy(np.ascontiguousarray(samples, dtype=np.float32))
+    if pinned:
+        h = h.pin_memory()
+    out = torch.full(tuple(out_shape) + (2,), float("nan"), dtype=torch.float32)
+    if pinned:
+        out = out.pin_memory()
+    stream = torch.cuda.current_stream()
+    ctx.reduce_precision_host(h, samples.shape[0], out, stream=stream)
+    ctx.stream_status(stream)
+    o = out.numpy()
+    return o[..., 0].astype(np.float64) + 1j * o[..., 1]
+
+
+@pytest.mark.parametrize("n", [0, 1000, (1 << 21) + 17, 5 * (1 << 20) + 3])
+def test_precision_host_entry_matches_device_entry(oracle, n):
+    """Chunked, copy-overlapped host entry point (1 to 3 staging chunks and
+    the empty ping) gives the device entry point's ping."""
+    wk = wl.precision_2d(n_samples=max(n, 1), n_bearings=128, n_ranges=512)
+    smp = wk.samples[:n]
+    ctx = precision_context(wk)
+    dev = gpu_precision(ctx, smp, wk.out_shape)
+    host = gpu_precision_host(ctx, smp, wk.out_shape)
+    assert np.isfinite(host).all()
+    if n == 0:
+        assert np.all(host == 0) and np.all(dev == 0)
+        return
+    assert rel_l2(host, dev) <= 1e-6
+    if n <= 1 << 21:
+        D, taps, c = wl.precision_tables(wk.sensor)
+        want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+        assert rel_l2(host, want) <= TOL
+
+
+def test_precision_host_entry_pageable_memory():
+    wk = wl.precision_2d(n_samples=1 << 16, n_bearings=128, n_ranges=512)
+    ctx = precision_context(wk)
+    a = gpu_precision(ctx, wk.samples, wk.out_shape)
+    b = gpu_precision_host(ctx, wk.samples, wk.out_shape, pinned=False)
+    assert rel_l2(b, a) <= 1e-6
