@@ -351,14 +351,20 @@ def run_ours(args, world, rank, local):
     if wk.dims == 2 and wk.echo:
         D, taps, center = workloads.precision_tables(wk.sensor)
         ctx.configure_precision(D, taps, center)
-        forms = ["precision", "precision_compensated", "plain"]
+        forms = ["precision", "precision_compensated", "precision_fp16", "plain"]
     ctx.reserve(n)
     host_in = torch.from_numpy(wk.samples.reshape(-1)).pin_memory()
     d_in = host_in.to("cuda")
     outs = {f: torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda") for f in forms}
     host_out = torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory()
-    res = {f: time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch,
-                        wk.echo) for f in forms}
+    res = {}
+    for f in forms:
+        if f == "precision_fp16":   # FP16 per-row-scaled contraction, FP64 carrier phase
+            ctx.configure_precision(D, taps, center, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE)
+        res[f] = time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch,
+                           wk.echo)
+        if f == "precision_fp16":
+            ctx.configure_precision(D, taps, center)
     if rank != 0:
         return
     head = forms[0]
@@ -482,7 +488,7 @@ def run_ours(args, world, rank, local):
                 float(np.linalg.norm(got_plain[b0:b1] - want) / np.linalg.norm(want)))
             if "precision" in forms:
                 want_b = oracle.reduce_binned(exact, wk.sensor, D, taps, center, rows=(b0, b1), threads=threads)
-                for f in ("precision", "precision_compensated"):
+                for f in ("precision", "precision_compensated", "precision_fp16"):
                     got_p = to_complex(outs[f])
                     acc.setdefault(f"{f}_rel_l2_vs_fp64_binned", []).append(
                         float(np.linalg.norm(got_p[b0:b1] - want_b) / np.linalg.norm(want_b)))

@@ -180,8 +180,14 @@ typedef struct {
     const float* range_taps;    /* host complex [tap_count] or NULL                    */
     uint32_t tap_count;
     uint32_t tap_center;
-    uint32_t flags;             /* reserved, 0 */
+    uint32_t flags;             /* 0 or RTACX_PRECISION_FP16_ROWSCALE */
 } rtacx_precision_desc;
+/* Contract in FP16 instead of BF16: each row of the filtered grid and each
+ * column of the directivity is scaled by a power of two to [2^14, 2^15)
+ * before the fp16 [hi | hi | lo] x [hi | lo | hi] split (11-bit halves,
+ * products exact in the FP32 accumulator) and the scales are undone exactly
+ * in the GEMM epilogue. */
+#define RTACX_PRECISION_FP16_ROWSCALE 1u
 rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_desc* desc);
 rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n,
                                     float* out, void* stream);

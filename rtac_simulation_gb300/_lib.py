@@ -133,6 +133,7 @@ class PingDesc(ctypes.Structure):
 RTACX_ECHO_PHASE = 1
 RTACX_ECHO_SPREADING = 2
 RTACX_ECHO_PHASE_COMPENSATED = 4
+RTACX_PRECISION_FP16_ROWSCALE = 1
 PRECISION_STAGES = ("accumulate", "windows", "filter", "gemm", "copy")
 
 
@@ -265,11 +266,11 @@ class Context:
         m = EchoModel(carrier_hz, flags)
         self._check(self._lib.rtacx_set_echo_model(self._h, ctypes.byref(m)))
 
-    def configure_precision(self, directivity=None, range_taps=None, tap_center: int = 0) -> None:
+    def configure_precision(self, directivity=None, range_taps=None, tap_center: int = 0, flags: int = 0) -> None:
         d = None if directivity is None else np.ascontiguousarray(np.asarray(directivity, dtype=np.complex64))
         t = None if range_taps is None else np.ascontiguousarray(np.asarray(range_taps, dtype=np.complex64))
         desc = PrecisionDesc(None if d is None else d.ctypes.data, None if t is None else t.ctypes.data,
-                             0 if t is None else t.size, tap_center, 0)
+                             0 if t is None else t.size, tap_center, flags)
         self._check(self._lib.rtacx_configure_precision(self._h, ctypes.byref(desc)))
 
     def reduce_precision(self, samples, n: int, out, stream=None) -> None:

@@ -271,6 +271,13 @@ struct Context {
     uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity
     float* d_C = nullptr;               // [Mpad][Npad] GEMM output when the ping shape is not tile-aligned
     float2* d_taps = nullptr;           // [taps] range taps at bin offsets t - tap_center
+    // FP16 per-row-scaled contraction (RTACX_PRECISION_FP16_ROWSCALE): A and B
+    // hold fp16 splits instead of bf16 ones.
+    bool prec_f16 = false;
+    float2* d_Gf = nullptr;             // [nR][nB] filtered grid (fp32) before the scaled split
+    uint32_t* d_rowmax = nullptr;       // [nR] largest |component| of each filtered row (float bits)
+    float* d_row_scale = nullptr;       // [Mpad] 2^-e per row: undoes the row's scaling in the GEMM epilogue
+    float* d_col_scale = nullptr;       // [Npad] 2^-e per directivity column
 
     // Host-buffer streaming (rtacx_reduce_precision_host): two device staging
     // buffers of RTACX_STREAM_CHUNK records, a copy stream fork-joined to the
@@ -330,9 +337,10 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream);
 void free_streaming(Context& ctx);
 void free_precision(Context& ctx);
 
-// Tensor-core GEMM (rtacx_umma.cu): C = A * B^T, bf16 K-major operands.
-rtacx_status gemm_bf16_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K,
-                          int ldc, cudaStream_t stream, uint32_t* err);
+// Tensor-core GEMM (rtacx_umma.cu): C = row_scale * col_scale * (A * B^T),
+// K-major operands, both bf16 or both fp16 (f16); scales optional.
+rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K, int ldc,
+                     cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale);
 size_t gemm_smem_bytes();
 
 } // namespace rtacx

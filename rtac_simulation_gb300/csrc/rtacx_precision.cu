@@ -12,12 +12,18 @@
 //   k_prec_filter      G'[r][k] = sum_t taps[t] G[r + t - c][k] over row r's
 //                      window, written as the bf16 A operand [hi | hi | lo]
 //                      of the three-term split product.
-//   gemm_bf16_tn       out = A x B^T on tcgen05 (rtacx_umma.cu), B the
+//   gemm_tn            out = A x B^T on tcgen05 (rtacx_umma.cu), B the
 //                      [hi | lo | hi] split of the complex directivity laid
 //                      out so that output column 2b is Re(out(r, b)) and
 //                      2b + 1 is Im(out(r, b)): the GEMM writes the
 //                      complex64 ping directly.
+// FP16 form (RTACX_PRECISION_FP16_ROWSCALE): the filter writes the fp32
+// filtered grid and per-row maxima, k_prec_split_f16 scales each row by a
+// power of two and writes the fp16 split, and the GEMM (fp16 operands)
+// undoes the row and column scales in its epilogue.
 #include "rtacx_internal.cuh"
+
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <climits>
@@ -160,9 +166,14 @@ size_t filter_smem_bytes(uint32_t ntaps)
 // lane's cell (lane 0 loads its left neighbour). Each thread then filters 8
 // rows x 2 adjacent bearings and writes the bf16 A operand [hi | hi | lo],
 // two bearings per 4-byte store.
+// kF32Out: write the filtered grid as fp32 complex (Gf [nR][nB]) and each
+// row's largest |component| (rowmax, float bits, atomicMax) for the FP16
+// per-row-scaled split instead of the bf16 A operand.
+template <bool kF32Out>
 __global__ void __launch_bounds__(kFiltThreads, 4)
 k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const float2* __restrict__ taps,
-              uint32_t ntaps, uint32_t center, uint32_t nR, uint32_t nB, uint32_t Kp, uint16_t* __restrict__ A)
+              uint32_t ntaps, uint32_t center, uint32_t nR, uint32_t nB, uint32_t Kp, uint16_t* __restrict__ A,
+              float2* __restrict__ Gf, uint32_t* __restrict__ rowmax)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int ntc = min((int)max(ntaps, 1u), kFiltTapsMax);
@@ -227,6 +238,23 @@ k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const 
         }
     }
     const int k = k0 + 2 * lane;
+    if constexpr(kF32Out) {
+#pragma unroll
+        for(int q = 0; q < 8; q++) {
+            const int r = r0 + warp * 8 + q;
+            if(r >= (int)nR) continue;     // warp-uniform
+            float m = 0.0f;
+#pragma unroll
+            for(int h = 0; h < 2; h++) {
+                if(k + h >= (int)nB) continue;
+                Gf[(size_t)r * nB + k + h] = acc[q][h];
+                m = fmaxf(m, fmaxf(fabsf(acc[q][h].x), fabsf(acc[q][h].y)));
+            }
+            for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if(lane == 0 && m > 0.0f) atomicMax(&rowmax[r], __float_as_uint(m));
+        }
+        return;
+    }
     const bool packed = (nB & 1u) == 0u && k + 1 < (int)nB;
 #pragma unroll
     for(int q = 0; q < 8; q++) {
@@ -256,6 +284,73 @@ k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const 
             }
         }
     }
+}
+
+// FP16 per-row-scaled split: row r of the filtered grid is scaled by
+// 2^(14 - e), e = floor(log2(rowmax[r])), so that its largest component lies
+// in [2^14, 2^15), then split into fp16 [hi | hi | lo] (lo = x - hi, so
+// hi + lo carries 22 significant bits); row_scale[r] = 2^(e - 14) undoes the
+// scaling exactly in the GEMM epilogue. One CTA per row.
+__device__ __forceinline__ int scale_exponent(uint32_t maxbits)
+{
+    if(maxbits == 0u) return 0;                       // zero row: scale 1
+    const int e = (int)((maxbits >> 23) & 0xffu) - 127;
+    return min(max(14 - e, -126), 127);
+}
+
+__global__ void k_prec_split_f16(const float2* __restrict__ Gf, const uint32_t* __restrict__ rowmax, uint32_t nR,
+                                 uint32_t nB, uint32_t Kp, uint16_t* __restrict__ A, float* __restrict__ row_scale)
+{
+    const uint32_t r = blockIdx.x;
+    if(r >= nR) return;
+    const int se = scale_exponent(rowmax[r]);
+    const float s = __uint_as_float((uint32_t)(se + 127) << 23);
+    if(threadIdx.x == 0) row_scale[r] = __uint_as_float((uint32_t)(127 - se) << 23);
+    uint16_t* row = A + (size_t)r * Kp;
+    for(uint32_t k = threadIdx.x; k < nB; k += blockDim.x) {
+        const float2 v = Gf[(size_t)r * nB + k];
+        const float xr = v.x * s, xi = v.y * s;
+        const __half hr = __float2half_rn(xr), hi = __float2half_rn(xi);
+        const __half lr = __float2half_rn(xr - __half2float(hr)), li = __float2half_rn(xi - __half2float(hi));
+        row[k] = __half_as_ushort(hr);            row[nB + k] = __half_as_ushort(hi);
+        row[2 * nB + k] = __half_as_ushort(hr);   row[3 * nB + k] = __half_as_ushort(hi);
+        row[4 * nB + k] = __half_as_ushort(lr);   row[5 * nB + k] = __half_as_ushort(li);
+    }
+}
+
+// Round-to-nearest-even float -> IEEE-754 binary16 bit pattern (from the
+// format definition: 10-bit mantissa, exponent bias 15, subnormal unit 2^-24).
+uint16_t host_f16_bits(float x)
+{
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    const uint32_t sign = (u >> 16) & 0x8000u, a = u & 0x7fffffffu;
+    if(a >= 0x7f800000u) return (uint16_t)(sign | 0x7c00u | (a > 0x7f800000u ? 0x200u : 0u));
+    if(a >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);          // >= 65520 rounds to infinity
+    if(a <= 0x33000000u) return (uint16_t)sign;                      // <= 2^-25 rounds to zero
+    const int e = (int)(a >> 23) - 127;
+    const uint32_t m = (a & 0x7fffffu) | 0x800000u;
+    if(e >= -14) {
+        uint32_t h = ((uint32_t)(e + 15) << 10) | ((m >> 13) & 0x3ffu);
+        const uint32_t rem = m & 0x1fffu;
+        if(rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+        return (uint16_t)(sign | h);
+    }
+    const int shift = -e - 1;                                        // 14 .. 24
+    uint32_t h = m >> shift;
+    const uint32_t rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
+    if(rem > half || (rem == half && (h & 1u))) h++;
+    return (uint16_t)(sign | h);
+}
+
+float host_f16_value(uint16_t h)
+{
+    const uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+    float v;
+    if(e == 0u) v = std::ldexp((float)m, -24);
+    else if(e == 31u) v = m ? NAN : INFINITY;
+    else v = std::ldexp((float)(m | 0x400u), (int)e - 25);
+    return (h & 0x8000u) ? -v : v;
 }
 
 uint16_t host_bf16_bits(float x)
@@ -307,6 +402,8 @@ void free_precision(Context& c)
 {
     free_dev(c.d_G); free_dev(c.d_flags); free_dev(c.d_pwin); free_dev(c.d_A); free_dev(c.d_B);
     free_dev(c.d_C); free_dev(c.d_taps); free_dev(c.d_lut);
+    free_dev(c.d_Gf); free_dev(c.d_rowmax); free_dev(c.d_row_scale); free_dev(c.d_col_scale);
+    c.prec_f16 = false;
     c.prec_configured = false;
 }
 
@@ -397,7 +494,9 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         return RTACX_ERR_CUDA;
     }
     ctx.acc_blocks_per_sm = (uint32_t)acc_blocks;
-    if(cudaFuncSetAttribute(k_prec_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if(cudaFuncSetAttribute(k_prec_filter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)filter_smem_bytes(kFiltTapsMax)) != cudaSuccess ||
+       cudaFuncSetAttribute(k_prec_filter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
         cudaGetLastError();
         ctx.error = "cannot reserve shared memory for the range filter";
@@ -410,18 +509,37 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     ctx.Kp = (6 * nB + 63) / 64 * 64;
 
     // B operand: row n = 2b (real) / 2b + 1 (imag); K blocks [hi | lo | hi]
-    // of [real part of G pairs | imaginary part of G pairs].
+    // of [real part of G pairs | imaginary part of G pairs]. FP16 form: each
+    // row n is first scaled by 2^(14 - e_n) (largest |value| in [2^14, 2^15))
+    // and col_scale[n] = 2^(e_n - 14) undoes it in the GEMM epilogue.
+    const bool f16 = (d->flags & RTACX_PRECISION_FP16_ROWSCALE) != 0;
+    if(d->flags & ~RTACX_PRECISION_FP16_ROWSCALE) { ctx.error = "unknown precision flags"; return RTACX_ERR_INVALID_ARGUMENT; }
     std::vector<uint16_t> B((size_t)ctx.Npad * ctx.Kp, 0);
+    std::vector<float> col_scale(ctx.Npad, 1.0f);
     for(uint32_t b = 0; b < nB; b++)
-        for(uint32_t k = 0; k < nB; k++) {
-            const float dr = D[((size_t)k * nB + b) * 2], di = D[((size_t)k * nB + b) * 2 + 1];
-            const float vals[2][2] = {{dr, -di}, {di, dr}};     // [re/im output][G real / G imag]
-            for(int o = 0; o < 2; o++)
+        for(int o = 0; o < 2; o++) {
+            auto value = [&](uint32_t k, int h) {
+                const float dr = D[((size_t)k * nB + b) * 2], di = D[((size_t)k * nB + b) * 2 + 1];
+                const float vals[2][2] = {{dr, -di}, {di, dr}};     // [re/im output][G real / G imag]
+                return vals[o][h];
+            };
+            float scale = 1.0f;
+            if(f16) {
+                float mx = 0.0f;
+                for(uint32_t k = 0; k < nB; k++) mx = std::max(mx, std::max(std::fabs(value(k, 0)), std::fabs(value(k, 1))));
+                if(mx > 0.0f) {
+                    const int se = std::min(std::max(14 - std::ilogb(mx), -126), 127);
+                    scale = std::ldexp(1.0f, se);
+                    col_scale[2 * b + o] = std::ldexp(1.0f, -se);
+                }
+            }
+            uint16_t* row = B.data() + (size_t)(2 * b + o) * ctx.Kp;
+            for(uint32_t k = 0; k < nB; k++)
                 for(int h = 0; h < 2; h++) {
-                    const float v = vals[o][h];
-                    const uint16_t bh = host_bf16_bits(v);
-                    const uint16_t bl = host_bf16_bits(v - host_bf16_value(bh));
-                    uint16_t* row = B.data() + (size_t)(2 * b + o) * ctx.Kp;
+                    const float v = value(k, h) * scale;
+                    uint16_t bh, bl;
+                    if(f16) { bh = host_f16_bits(v); bl = host_f16_bits(v - host_f16_value(bh)); }
+                    else { bh = host_bf16_bits(v); bl = host_bf16_bits(v - host_bf16_value(bh)); }
                     row[h * nB + k] = bh;
                     row[2 * nB + h * nB + k] = bl;
                     row[4 * nB + h * nB + k] = bh;
@@ -437,7 +555,10 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
        !alloc(ctx.d_lut, (size_t)cells * sizeof(int)) ||
        !alloc(ctx.d_pwin, (size_t)nR * sizeof(int2)) || !alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) ||
        !alloc(ctx.d_B, B.size() * 2) || !alloc(ctx.d_taps, taps.size() * sizeof(float)) ||
-       (!direct && !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float)))) {
+       (!direct && !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float))) ||
+       (f16 && (!alloc(ctx.d_Gf, (size_t)nR * nB * sizeof(float2)) || !alloc(ctx.d_rowmax, (size_t)nR * 4) ||
+                !alloc(ctx.d_row_scale, (size_t)ctx.Mpad * sizeof(float)) ||
+                !alloc(ctx.d_col_scale, (size_t)ctx.Npad * sizeof(float))))) {
         free_precision(ctx);
         ctx.error = "out of device memory for the precision form";
         return RTACX_ERR_OUT_OF_MEMORY;
@@ -445,13 +566,17 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     if(cudaMemset(ctx.d_A, 0, (size_t)ctx.Mpad * ctx.Kp * 2) != cudaSuccess ||
        cudaMemcpy(ctx.d_B, B.data(), B.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
        cudaMemcpy(ctx.d_taps, taps.data(), taps.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
-       cudaMemcpy(ctx.d_lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+       cudaMemcpy(ctx.d_lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+       (f16 && (cudaMemcpy(ctx.d_col_scale, col_scale.data(), col_scale.size() * sizeof(float),
+                           cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemset(ctx.d_row_scale, 0, (size_t)ctx.Mpad * sizeof(float)) != cudaSuccess))) {
         cudaGetLastError();
         free_precision(ctx);
         ctx.error = "uploading the precision tables failed";
         return RTACX_ERR_CUDA;
     }
     if(gemm_smem_bytes() > 227 * 1024) { ctx.error = "GEMM tile exceeds shared memory"; return RTACX_ERR_UNSUPPORTED; }
+    ctx.prec_f16 = f16;
     ctx.prec_configured = true;
     return RTACX_OK;
 }
@@ -499,16 +624,27 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
     RTACX_CUDA(cudaGetLastError());
     ctx.mark(1, true, stream);
     ctx.mark(2, false, stream);
-    k_prec_filter<<<dim3((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows), kFiltThreads,
-                    filter_smem_bytes(ctx.taps), stream>>>(
-        ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, ctx.d_A);
-    RTACX_CUDA(cudaGetLastError());
+    const dim3 fgrid((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows);
+    if(!ctx.prec_f16) {
+        k_prec_filter<false><<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
+            ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, ctx.d_A, nullptr, nullptr);
+        RTACX_CUDA(cudaGetLastError());
+    }
+    else {
+        RTACX_CUDA(cudaMemsetAsync(ctx.d_rowmax, 0, (size_t)nR * 4, stream));
+        k_prec_filter<true><<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
+            ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, nullptr, ctx.d_Gf, ctx.d_rowmax);
+        RTACX_CUDA(cudaGetLastError());
+        k_prec_split_f16<<<nR, 256, 0, stream>>>(ctx.d_Gf, ctx.d_rowmax, nR, nB, ctx.Kp, ctx.d_A, ctx.d_row_scale);
+        RTACX_CUDA(cudaGetLastError());
+    }
     ctx.mark(2, true, stream);
     ctx.mark(3, false, stream);
     const bool direct = ctx.d_C == nullptr;
     float* C = direct ? out : ctx.d_C;
-    rtacx_status st = gemm_bf16_tn(ctx.error, ctx.d_A, ctx.d_B, C, (int)ctx.Mpad, (int)ctx.Npad, (int)ctx.Kp,
-                                   (int)ctx.Npad, stream, ctx.d_err);
+    rtacx_status st = gemm_tn(ctx.error, ctx.d_A, ctx.d_B, C, (int)ctx.Mpad, (int)ctx.Npad, (int)ctx.Kp,
+                              (int)ctx.Npad, stream, ctx.d_err, ctx.prec_f16, ctx.prec_f16 ? ctx.d_row_scale : nullptr,
+                              ctx.prec_f16 ? ctx.d_col_scale : nullptr);
     if(st != RTACX_OK) return st;
     ctx.mark(3, true, stream);
     ctx.mark(4, false, stream);

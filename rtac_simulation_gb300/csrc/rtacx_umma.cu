@@ -1,8 +1,10 @@
-// BF16 tensor-core GEMM on sm_103a: C[M][N] (fp32) = A[M][K] * B[N][K]^T.
+// 16-bit tensor-core GEMM on sm_103a: C[M][N] (fp32) =
+// row_scale[M] * col_scale[N] * (A[M][K] * B[N][K]^T), A and B both bf16 or
+// both fp16 (the scales are optional).
 //
 // Used by the precision form for the dense complex bearing-directivity
 // contraction, written as one real GEMM (see rtacx_precision.cu). Both
-// operands are K-major bf16 ("TN"); M % 128 == 0, N % 256 == 0, K % 64 == 0
+// operands are K-major ("TN"); M % 128 == 0, N % 256 == 0, K % 64 == 0
 // (callers pad).
 //
 // One CTA computes a 128 x 256 tile with four warps:
@@ -13,7 +15,8 @@
 //                   stage into a 128-lane x 256-column fp32 TMEM accumulator,
 //                   tcgen05.commit frees the stage;
 //   warps 0-3       epilogue: tcgen05.ld 32x32b of their TMEM lane quadrant,
-//                   fp32 stores of whole 128-byte row segments.
+//                   optional row / column scaling, fp32 stores of whole
+//                   128-byte row segments.
 // Every mbarrier wait is bounded (about two seconds); a timeout sets an
 // error bit and the CTA skips its remaining work, still waiting (bounded) for
 // issued MMAs and freeing its TMEM.
@@ -36,10 +39,14 @@ constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long long kWaitCycles = 4000000000ll;
 
 // Instruction descriptor of tcgen05.mma.kind::f16: D = f32 (bits 4-5 = 1),
-// A = B = bf16 (bits 7-9 = 1, bits 10-12 = 1), both K-major (bits 15, 16 = 0),
-// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// A and B format at bits 7-9 and 10-12 (0 = f16, 1 = bf16; always the same
+// type for both), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22,
+// M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_for(bool f16)
+{
+    return (1u << 4) | ((f16 ? 0u : 1u) << 7) | ((f16 ? 0u : 1u) << 10) | ((uint32_t)(BN >> 3) << 17) |
+           ((uint32_t)(BM >> 4) << 24);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -95,12 +102,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+template <bool kF16>
+__device__ __forceinline__ void umma_16bit(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
 {
     asm volatile("{\n\t.reg .pred p;\n\t"
                  "setp.ne.b32 p, %4, 0;\n\t"
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc_for(kF16)), "r"(accumulate)
                  : "memory");
 }
 
@@ -127,9 +135,11 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+template <bool kF16>
 __global__ void __launch_bounds__(kThreads, 1)
-k_gemm_bf16_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-               float* __restrict__ C, int M, int N, int K, int ldc, uint32_t* __restrict__ err)
+k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+          float* __restrict__ C, int M, int N, int K, int ldc, const float* __restrict__ row_scale,
+          const float* __restrict__ col_scale, uint32_t* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
@@ -185,7 +195,7 @@ k_gemm_bf16_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const uint64_t ad = smem_desc(a), bd = smem_desc(a + A_BYTES);
 #pragma unroll
             for(int kk = 0; kk < BK / 16; kk++)   // 32 bytes of K per MMA: +2 in descriptor units
-                umma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
+                umma_16bit<kF16>(tmem, ad + 2 * kk, bd + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
             umma_commit(empty_bar(s));
         }
         umma_commit(accum_bar);   // arrives once every MMA issued above has completed
@@ -199,16 +209,30 @@ k_gemm_bf16_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     if(__all_sync(0xffffffffu, ok ? 1 : 0)) {
         const int row = m0 + warp * 32 + lane;
         float* crow = C + (size_t)row * ldc + n0;
+        const float rs = (row_scale && row < M) ? row_scale[row] : 1.0f;
 #pragma unroll 1
         for(int c = 0; c < BN / 32; c++) {
             uint32_t r[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
             if(row < M && n0 + c * 32 < N) {
+                float v[32];
+#pragma unroll
+                for(int q = 0; q < 32; q++) v[q] = __uint_as_float(r[q]);
+                if(row_scale) {
+#pragma unroll
+                    for(int q = 0; q < 32; q++) v[q] *= rs;
+                }
+                if(col_scale) {
+                    const float4* cs = reinterpret_cast<const float4*>(col_scale + n0 + c * 32);
+#pragma unroll
+                    for(int q = 0; q < 8; q++) {
+                        const float4 s4 = __ldg(cs + q);
+                        v[4 * q] *= s4.x; v[4 * q + 1] *= s4.y; v[4 * q + 2] *= s4.z; v[4 * q + 3] *= s4.w;
+                    }
+                }
                 float4* dst = reinterpret_cast<float4*>(crow + c * 32);
 #pragma unroll
-                for(int q = 0; q < 8; q++)
-                    dst[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
-                                         __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+                for(int q = 0; q < 8; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
             }
         }
     }
@@ -242,7 +266,7 @@ EncodeTiledFn encode_fn()
     return fn;
 }
 
-bool make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k, uint32_t box_rows)
+bool make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k, uint32_t box_rows, bool f16)
 {
     EncodeTiledFn enc = encode_fn();
     if(!enc) return false;
@@ -250,7 +274,8 @@ bool make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k, uint
     cuuint64_t strides[1] = {k * 2};
     cuuint32_t box[2] = {(cuuint32_t)BK, box_rows};
     cuuint32_t estr[2] = {1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+    return enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+               const_cast<void*>(ptr), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -259,27 +284,33 @@ bool make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k, uint
 
 size_t gemm_smem_bytes() { return SMEM_BYTES; }
 
-// C = A * B^T; A [M][K], B [N][K] bf16 (16-byte aligned, row stride K),
-// C [M][ldc] fp32. Shapes must be multiples of the tile (128, 256, 64).
-rtacx_status gemm_bf16_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K,
-                          int ldc, cudaStream_t stream, uint32_t* err)
+// C = row_scale * col_scale * (A * B^T); A [M][K], B [N][K] both bf16 or
+// both fp16 (16-byte aligned, row stride K), C [M][ldc] fp32, scales
+// optional (row_scale [M], col_scale [N], 16-byte aligned). Shapes must be
+// multiples of the tile (128, 256, 64).
+rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K, int ldc,
+                     cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale)
 {
     if(M <= 0 || N <= 0 || K <= 0 || M % BM || N % BN || K % BK || ldc < N || ldc % 4) {
         error = "gemm shape must be multiples of 128 x 256 x 64";
         return RTACX_ERR_INVALID_ARGUMENT;
     }
-    if((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16 || reinterpret_cast<uintptr_t>(C) % 16) {
+    if((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16 || reinterpret_cast<uintptr_t>(C) % 16 ||
+       reinterpret_cast<uintptr_t>(col_scale) % 16) {
         error = "gemm operands must be 16-byte aligned";
         return RTACX_ERR_INVALID_ARGUMENT;
     }
     CUtensorMap ma, mb;
-    if(!make_map(&ma, A, (uint64_t)M, (uint64_t)K, BM) || !make_map(&mb, B, (uint64_t)N, (uint64_t)K, BN)) {
+    if(!make_map(&ma, A, (uint64_t)M, (uint64_t)K, BM, f16) || !make_map(&mb, B, (uint64_t)N, (uint64_t)K, BN, f16)) {
         error = "cuTensorMapEncodeTiled failed";
         return RTACX_ERR_CUDA;
     }
     static bool attr = false;
     if(!attr) {
-        if(cudaFuncSetAttribute(k_gemm_bf16_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) != cudaSuccess) {
+        if(cudaFuncSetAttribute(k_gemm_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) !=
+               cudaSuccess ||
+           cudaFuncSetAttribute(k_gemm_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) !=
+               cudaSuccess) {
             cudaGetLastError();
             error = "cannot reserve shared memory for the tensor-core GEMM";
             return RTACX_ERR_CUDA;
@@ -287,9 +318,10 @@ rtacx_status gemm_bf16_tn(std::string& error, const void* A, const void* B, floa
         attr = true;
     }
     dim3 grid(N / BN, M / BM);
-    k_gemm_bf16_tn<<<grid, kThreads, SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, err);
+    if(f16) k_gemm_tn<true><<<grid, kThreads, SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
+    else k_gemm_tn<false><<<grid, kThreads, SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
     const cudaError_t e = cudaGetLastError();
-    if(e != cudaSuccess) { error = std::string("k_gemm_bf16_tn: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    if(e != cudaSuccess) { error = std::string("k_gemm_tn: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;
 }
 
@@ -310,7 +342,7 @@ extern "C" rtacx_status rtacx_gemm_bf16_tn(const void* A, const void* B, float* 
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if(cudaMemsetAsync(err, 0, sizeof(uint32_t), s) != cudaSuccess) { cudaGetLastError(); return RTACX_ERR_CUDA; }
-    rtacx_status st = rtacx::gemm_bf16_tn(error, A, B, C, M, N, K, N, s, err);
+    rtacx_status st = rtacx::gemm_tn(error, A, B, C, M, N, K, N, s, err, false, nullptr, nullptr);
     if(st != RTACX_OK) return st;
     uint32_t word = 0;
     if(cudaStreamSynchronize(s) != cudaSuccess ||
