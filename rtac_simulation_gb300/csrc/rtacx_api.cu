@@ -118,7 +118,7 @@ bool allocate_bins(Context& c)
     configure_hist_launch(c);
     const size_t cols = (size_t)c.bin.nBins * kCursorStride;
     return upload<uint32_t>(c, c.d_offsets, nullptr, c.bin.nBins + 1) &&
-           upload<uint32_t>(c, c.d_totals, nullptr, c.bin.nBins) &&
+           upload<uint32_t>(c, c.d_totals, nullptr, c.bin.nBins + c.bin.nBins / 1024 + 1) &&   // + block sums
            upload<int2>(c, c.d_win, nullptr, c.nR) &&
            upload<uint32_t>(c, c.d_hist, nullptr, cols) &&
            ((c.hist_cols = cols), true);

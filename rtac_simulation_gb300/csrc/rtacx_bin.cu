@@ -35,6 +35,7 @@ namespace rtacx {
 namespace {
 
 constexpr int kScanThreads = 1024;
+constexpr uint32_t kScanBlock = 1024;   // bins per CTA of the parallel bin scan
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -120,6 +121,15 @@ __device__ void count_chunk(const float* __restrict__ samples, uint64_t n, const
     }
     for(uint32_t b = threadIdx.x; b < p.nBins; b += blockDim.x)
         if(sh[b]) atomicAdd(&totals[b], sh[b]);
+    // Per-block sums of kScanBlock bins (totals[nBins + blk]) for the
+    // parallel bin scan: one warp per block of bins.
+    const uint32_t blocks = (p.nBins + kScanBlock - 1) / kScanBlock;
+    for(uint32_t blk = threadIdx.x >> 5; blk < blocks; blk += blockDim.x >> 5) {
+        uint32_t s = 0;
+        for(uint32_t b = blk * kScanBlock + lane_id(); b < min((blk + 1) * kScanBlock, p.nBins); b += 32) s += sh[b];
+        for(int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if(lane_id() == 0 && s) atomicAdd(&totals[p.nBins + blk], s);
+    }
 }
 
 namespace {
@@ -163,23 +173,41 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 
 // Exclusive scan of totals[0, nBins) into offsets[0, nBins] by one CTA of
 // kScanThreads threads; cursor (optional) receives offsets[0, nBins).
+// The totals pass through shared memory in segments of kScanSeg bins
+// (coalesced loads and stores; each thread scans 8 consecutive bins of the
+// segment, padded against bank conflicts), carrying the running total.
+constexpr uint32_t kScanPer = 8, kScanSeg = kScanThreads * kScanPer;
+
+__device__ __forceinline__ uint32_t scan_pad(uint32_t i) { return i + i / 32; }
+
 __device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins, uint32_t* __restrict__ offsets,
                             uint32_t* __restrict__ cursor)
 {
     __shared__ uint32_t s_warp[32];
-    const uint32_t per = (nBins + blockDim.x - 1) / blockDim.x;
-    const uint32_t b0 = threadIdx.x * per;
-    const uint32_t b1 = min(b0 + per, nBins);
-    uint32_t sum = 0;
-    for(uint32_t b = b0; b < b1; b++) sum += totals[b];
-    uint32_t total;
-    uint32_t run = block_exclusive_scan(sum, s_warp, total);
-    for(uint32_t b = b0; b < b1; b++) {
-        offsets[b] = run;
-        if(cursor) cursor[(size_t)b * kCursorStride] = run;
-        run += totals[b];
+    __shared__ uint32_t s_seg[kScanSeg + kScanSeg / 32];
+    uint32_t carry = 0;
+    for(uint32_t s0 = 0; s0 < nBins; s0 += kScanSeg) {
+        const uint32_t len = min(kScanSeg, nBins - s0);
+        for(uint32_t i = threadIdx.x; i < kScanSeg; i += blockDim.x) s_seg[scan_pad(i)] = i < len ? totals[s0 + i] : 0u;
+        __syncthreads();
+        const uint32_t q0 = threadIdx.x * kScanPer;
+        uint32_t v[kScanPer], sum = 0;
+#pragma unroll
+        for(uint32_t u = 0; u < kScanPer; u++) { v[u] = s_seg[scan_pad(q0 + u)]; sum += v[u]; }
+        uint32_t seg_total;
+        uint32_t run = carry + block_exclusive_scan(sum, s_warp, seg_total);
+#pragma unroll
+        for(uint32_t u = 0; u < kScanPer; u++) { s_seg[scan_pad(q0 + u)] = run; run += v[u]; }
+        __syncthreads();
+        for(uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+            const uint32_t o = s_seg[scan_pad(i)];
+            offsets[s0 + i] = o;
+            if(cursor) cursor[(size_t)(s0 + i) * kCursorStride] = o;
+        }
+        carry += seg_total;
+        __syncthreads();
     }
-    if(threadIdx.x == 0) offsets[nBins] = total;
+    if(threadIdx.x == 0) offsets[nBins] = carry;
 }
 
 namespace {
@@ -188,6 +216,34 @@ __global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __rest
                                                            uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursor)
 {
     binscan_cta(totals, nBins, offsets, cursor);
+}
+
+// Parallel exclusive scan of the bin totals: CTA i scans bins
+// [i kScanBlock, (i + 1) kScanBlock) and adds the sum of the block sums
+// before it (totals[nBins + j], accumulated by the count pass). Writes
+// offsets[0, nBins] and the scatter's per-bin cursors.
+__global__ void __launch_bounds__(kScanBlock) k_binscan_blocks(const uint32_t* __restrict__ totals, uint32_t nBins,
+                                                               uint32_t* __restrict__ offsets,
+                                                               uint32_t* __restrict__ cursor)
+{
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_prefix;
+    const uint32_t blk = blockIdx.x, b = blk * kScanBlock + threadIdx.x;
+    if(threadIdx.x < 32) {
+        uint32_t s = 0;
+        for(uint32_t j = threadIdx.x; j < blk; j += 32) s += totals[nBins + j];
+        for(int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if(threadIdx.x == 0) s_prefix = s;
+    }
+    const uint32_t v = b < nBins ? totals[b] : 0u;
+    uint32_t blk_total;
+    const uint32_t x = block_exclusive_scan(v, s_warp, blk_total);   // synchronises: s_prefix is visible
+    const uint32_t o = s_prefix + x;
+    if(b < nBins) {
+        offsets[b] = o;
+        cursor[(size_t)b * kCursorStride] = o;
+    }
+    if(b == nBins - 1) offsets[nBins] = o + v;
 }
 
 } // namespace
@@ -243,6 +299,93 @@ __global__ void k_scatter(const float* __restrict__ samples, uint64_t n, BinPara
 {
     extern __shared__ uint32_t sh[];
     scatter_chunk(samples, n, p, blockIdx.x, gridDim.x, cursor, offsets, sorted, err, sh);
+}
+
+// Staged scatter (single ping; one 1024-thread CTA per SM): tiles of
+// 1024 * U records are sorted by bin in shared memory before they are
+// written, so consecutive lanes store consecutive slots of each bin's run and
+// the stores coalesce into whole sectors. Per tile:
+//   pass 1   load records, key, rank among the tile's samples of the bin
+//            (shared histogram);
+//   scan     block exclusive scan of the histogram = local run starts; one
+//            atomicAdd per non-empty (tile, bin) on the bin's shared cursor
+//            reserves the run; delta = global base - local start;
+//   pass 2   reload the tile (L2-resident since pass 1) into its sorted
+//            shared-memory slot;
+//   write    slot j goes to j + delta[key(j)] (the key recomputed from the
+//            record's travel and bearing, as in pass 1).
+// Shared memory: 16 B x NT U records + 8 B per bin. Shapes, in order of
+// preference: 1024 x 12 (one CTA per SM, longest runs), 512 x 10 (two CTAs
+// per SM), 1024 x 4.
+size_t staged_smem_bytes(int NT, int U, uint32_t nBins) { return (size_t)NT * U * sizeof(float4) + (size_t)nBins * 8; }
+
+template <int NT, int U>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+k_scatter_staged(const float* __restrict__ samples, uint64_t n, BinParams p, uint32_t* __restrict__ cursor,
+                 const uint32_t* __restrict__ offsets, float4* __restrict__ sorted, uint32_t* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ uint32_t s_warp[32];
+    const uint32_t nb = p.nBins;
+    float4* s_rec = reinterpret_cast<float4*>(s_raw);
+    uint32_t* s_start = reinterpret_cast<uint32_t*>(s_rec + NT * U);     // histogram, then local run starts
+    uint32_t* s_delta = s_start + nb;                                     // global base - local start
+    const uint32_t tid = threadIdx.x;
+    const uint32_t per = (nb + NT - 1) / NT, b0 = min(tid * per, nb), b1 = min(b0 + per, nb);
+    const uint32_t total = offsets[nb];
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t begin = (uint64_t)blockIdx.x * chunk, end = min(begin + chunk, n);
+    for(uint32_t b = tid; b < nb; b += NT) s_start[b] = 0u;
+    __syncthreads();
+    for(uint64_t t0 = begin; t0 < end; t0 += (uint64_t)NT * U) {
+        uint32_t key[U], rank[U];
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            const uint64_t i = t0 + (uint64_t)u * NT + tid;
+            key[u] = kOutOfRange;
+            if(i < end) {
+                const float4 rec = load_record(samples, i, p);
+                int side;
+                key[u] = sample_key(p, rec.z, rec.w, side);
+            }
+        }
+#pragma unroll
+        for(int u = 0; u < U; u++) rank[u] = key[u] != kOutOfRange ? atomicAdd(&s_start[key[u]], 1u) : 0u;
+        __syncthreads();
+        uint32_t sum = 0;
+        for(uint32_t b = b0; b < b1; b++) sum += s_start[b];
+        uint32_t tile_total;
+        uint32_t run = block_exclusive_scan(sum, s_warp, tile_total);
+        for(uint32_t b = b0; b < b1; b++) {
+            const uint32_t c = s_start[b];
+            s_start[b] = run;
+            if(c) s_delta[b] = atomicAdd(&cursor[(size_t)b * kCursorStride], c) - run;
+            run += c;
+        }
+        __syncthreads();
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            if(key[u] == kOutOfRange) continue;
+            float4 rec = load_record(samples, t0 + (uint64_t)u * NT + tid, p);
+            if(p.echo_flags) {
+                const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z);
+                rec.x = v.x; rec.y = v.y;
+            }
+            s_rec[s_start[key[u]] + rank[u]] = rec;
+        }
+        __syncthreads();
+        for(uint32_t j = tid; j < tile_total; j += NT) {
+            const float4 rec = s_rec[j];
+            int side;
+            const uint32_t k = sample_key(p, rec.z, rec.w, side);
+            const uint32_t pos = j + s_delta[k];
+            if(pos < total) sorted[pos] = rec;
+            else atomicOr(err, kErrScatterOverflow);
+        }
+        __syncthreads();
+        for(uint32_t b = b0; b < b1; b++) s_start[b] = 0u;
+        __syncthreads();
+    }
 }
 
 __device__ __forceinline__ uint32_t bin_count(const uint32_t* off, uint32_t nBB, int j)
@@ -344,13 +487,14 @@ __global__ void k_count_batch(const PingDev* __restrict__ pings, const uint2* __
     count_chunk(P.samples, P.n, P.bin, m.y, P.chunks, P.totals, P.oor, sh, s_oor);
 }
 
-// Zeroes every ping's bin totals (one thread per (ping, bin)).
+// Zeroes every ping's bin totals and block sums (one thread per (ping, bin)).
 __global__ void k_zero_totals_batch(const PingDev* __restrict__ pings, const uint2* __restrict__ map)
 {
     const uint2 m = map[blockIdx.x];
     const PingDev& P = pings[m.x];
     const uint32_t b = m.y * blockDim.x + threadIdx.x;
     if(b < P.bin.nBins) P.totals[b] = 0u;
+    if(b < (P.bin.nBins + kScanBlock - 1) / kScanBlock) P.totals[P.bin.nBins + b] = 0u;
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_binscan_batch(const PingDev* __restrict__ pings)
@@ -428,7 +572,8 @@ rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStre
         const size_t smem = (size_t)p.nBins * sizeof(uint32_t);
         const float* s = static_cast<const float*>(samples);
         ctx.mark(1, false, stream);
-        RTACX_CUDA(cudaMemsetAsync(ctx.d_totals, 0, p.nBins * sizeof(uint32_t), stream));
+        const uint32_t scan_blocks = (p.nBins + kScanBlock - 1) / kScanBlock;
+        RTACX_CUDA(cudaMemsetAsync(ctx.d_totals, 0, (p.nBins + scan_blocks) * sizeof(uint32_t), stream));
         ctx.mark(1, true, stream);
         ctx.mark(0, false, stream);
         k_count<<<grid, ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_totals, ctx.d_oor);
@@ -436,13 +581,25 @@ rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStre
         ctx.mark(0, true, stream);
         ctx.mark(2, false, stream);
         // d_hist holds the per-bin write cursors of the scatter.
-        k_binscan<<<1, kScanThreads, 0, stream>>>(ctx.d_totals, p.nBins, ctx.d_offsets, ctx.d_hist);
+        k_binscan_blocks<<<scan_blocks, kScanBlock, 0, stream>>>(ctx.d_totals, p.nBins, ctx.d_offsets, ctx.d_hist);
         RTACX_CUDA(cudaGetLastError());
         ctx.mark(2, true, stream);
         ctx.mark(3, false, stream);
-        k_scatter<<<hist_grid(ctx.scatter_ctas, n), ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist,
-                                                                                       ctx.d_offsets, ctx.d_sorted,
-                                                                                       ctx.d_err);
+        if(ctx.staged_U) {
+            const int NT = ctx.staged_U == 10 ? 512 : 1024;
+            const uint32_t g = hist_grid((uint32_t)ctx.sm_count * (NT == 512 ? 2u : 1u), n);
+            const size_t ss = staged_smem_bytes(NT, ctx.staged_U, p.nBins);
+            switch(ctx.staged_U) {
+            case 10: k_scatter_staged<512, 10><<<g, 512, ss, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets, ctx.d_sorted, ctx.d_err); break;
+            case 12: k_scatter_staged<1024, 12><<<g, 1024, ss, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets, ctx.d_sorted, ctx.d_err); break;
+            default: k_scatter_staged<1024, 4><<<g, 1024, ss, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets, ctx.d_sorted, ctx.d_err); break;
+            }
+        }
+        else {
+            k_scatter<<<hist_grid(ctx.scatter_ctas, n), ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist,
+                                                                                           ctx.d_offsets, ctx.d_sorted,
+                                                                                           ctx.d_err);
+        }
         RTACX_CUDA(cudaGetLastError());
         ctx.mark(3, true, stream);
     }
@@ -532,6 +689,22 @@ void configure_hist_launch(Context& ctx)
     };
     ctx.hist_ctas = resident((const void*)k_count);
     ctx.scatter_ctas = resident((const void*)k_scatter);
+    // Staged scatter: the longest runs first (one 1024 x 12 CTA per SM), then
+    // two 512 x 10 CTAs per SM, then 1024 x 4.
+    ctx.staged_U = 0;
+    int optin = 0, smem_sm = 0;
+    if(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device) != cudaSuccess) optin = 0;
+    if(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx.device) != cudaSuccess) smem_sm = 0;
+    const int cand_nt[3] = {1024, 512, 1024}, cand_u[3] = {12, 10, 4};   // 1024 x 12 measured fastest
+    const void* fns[3] = {(const void*)k_scatter_staged<1024, 12>, (const void*)k_scatter_staged<512, 10>,
+                          (const void*)k_scatter_staged<1024, 4>};
+    for(int c = 0; c < 3 && !ctx.staged_U; c++) {
+        const size_t need = staged_smem_bytes(cand_nt[c], cand_u[c], ctx.bin.nBins);
+        const size_t resident = cand_nt[c] == 512 ? 2 * (need + 1024) : need + 1024;
+        if(need + 1024 <= (size_t)optin && resident <= (size_t)smem_sm &&
+           cudaFuncSetAttribute(fns[c], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) == cudaSuccess)
+            ctx.staged_U = cand_u[c];
+    }
     cudaGetLastError();
 }
 

@@ -55,7 +55,7 @@ constexpr size_t kOffHist    = align256(kOffSorted + kMaxSamples * sizeof(float4
 constexpr size_t kOffOffsets = align256(kOffHist + (size_t)kMaxHistCtas * kMaxBins * 4);
 static_assert(kMaxHistCtas >= kCursorStride, "cursor region of the static scratch");
 constexpr size_t kOffTotals  = align256(kOffOffsets + (kMaxBins + 1) * 4);
-constexpr size_t kOffWin     = align256(kOffTotals + kMaxBins * 4);
+constexpr size_t kOffWin     = align256(kOffTotals + (kMaxBins + kMaxBins / 1024 + 1) * 4);   // + block sums
 constexpr size_t kOffOor     = align256(kOffWin + kMaxRanges * sizeof(int2));
 constexpr size_t kOffErr     = align256(kOffOor + 2 * sizeof(unsigned long long));
 constexpr size_t kOffPulse   = align256(kOffErr + sizeof(uint32_t));
