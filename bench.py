@@ -43,6 +43,17 @@ sys.path.insert(0, str(ROOT))
 from rtac_simulation_gb300 import workloads  # noqa: E402
 
 DEFAULT_CONFIG = "precision_2d"
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# ncu captures of the default workload, each taken with
+#   ncu --set full --clock-control none -k regex:<kernel> -s <n> -c 1 \
+#       python bench.py --steps 2 --warmup 3 --no-cpu-baseline
+# on a GB300. Reported as `traffic` beside the live `achieved` numbers.
+NCU_TRAFFIC_BYTES = {
+    "k_prec_accumulate": 302.046e6 + 3.603e6,
+    "k_gemm_tn": 31.470e6 + 0.003e6,
+    "sort_bin": (268.531e6 + 3.186e6) + (274.855e6 + 223.261e6),   # k_count + k_scatter_staged
+}
+
 KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
 
 
@@ -404,14 +415,16 @@ def run_ours(args, world, rank, local):
     gather_tf = 8.0 * pairs / gather_s / 1e12 if gather_s > 0 else 0.0
     roof_plain = {"bound": "fp32", "achieved": gather_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                   "frac": gather_tf / fp32_peak, "traffic": None,
-                  "kernel": "k_gather_2d" if wk.dims == 2 else "k_gather_1d",
+                  "kernel": "k_gather_split" if wk.dims == 2 else "k_gather_1d",
                   "peak_source": "nominal FP32 SIMT (152 SMs x 128 FMA x max clock); no measured FP32 peak",
                   "algorithmic": "8 flop per useful (sample, output cell) pair, %.3e pairs" % pairs}
     bin_bytes = n * (rec_in + 16)
     bin_s = (st["count"] + st["reset"] + st["binscan"] + st["scatter"] + st["windows"]) / 1e3
     bin_gbs = bin_bytes / bin_s / 1e9 if bin_s > 0 else 0.0
+    ncu = NCU_TRAFFIC_BYTES if args.config == DEFAULT_CONFIG else {}
     line["roofline_sort_bin"] = {"bound": "hbm", "achieved": bin_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                                 "frac": bin_gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
+                                 "frac": bin_gbs / peaks["hbm_gbs"], "traffic": ncu.get("sort_bin"),
+                                 "peak_source": peaks["source"],
                                  "algorithmic": f"{rec_in}+16 bytes per sample over count+reset+binscan+scatter+windows"}
     if "precision" in forms:
         ps = res["precision"]["stage"]
@@ -422,11 +435,12 @@ def run_ours(args, world, rank, local):
         Mp, Np, Kp = -(-nR // 128) * 128, -(-2 * nB // 256) * 256, -(-6 * nB // 64) * 64
         gemm_tf = 2.0 * Mp * Np * Kp / (ps["gemm"] / 1e3) / 1e12
         roof_acc = {"bound": "hbm", "achieved": acc_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                    "frac": acc_gbs / peaks["hbm_gbs"], "traffic": None, "kernel": "k_prec_accumulate",
+                    "frac": acc_gbs / peaks["hbm_gbs"], "traffic": ncu.get("k_prec_accumulate"),
+                    "kernel": "k_prec_accumulate",
                     "peak_source": peaks["source"],
                     "algorithmic": f"{rec_in} B per sample read + 8 B per binned cell"}
         roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                     "frac": gemm_tf / peaks["bf16_tflops"], "traffic": None, "kernel": "k_gemm_bf16_tn",
+                     "frac": gemm_tf / peaks["bf16_tflops"], "traffic": ncu.get("k_gemm_tn"), "kernel": "k_gemm_tn",
                      "peak_source": peaks["source"],
                      "algorithmic": f"2*M*N*K with M={Mp} N={Np} K={Kp} (three BF16 split products as one K)"}
         dominant = max(("accumulate", "gemm", "filter"), key=lambda k: ps[k])
