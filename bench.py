@@ -260,7 +260,7 @@ def wk_desc(wk) -> str:
             f"{len(s['pulse'])}-tap pulse x {len(s['beam'])}-tap beam")
 
 
-def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, local, torch, echo=None):
+def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, local, torch, echo=None, alt=None):
     """Device time of `steps` pings (samples resident), per-stage event times
     and the end-to-end time with pinned host buffers, for one form. The form
     "precision_compensated" is the precision form with the carrier phase
@@ -268,7 +268,8 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     from rtac_simulation_gb300 import _lib
     if echo:
         extra = _lib.RTACX_ECHO_PHASE_COMPENSATED if form == "precision_compensated" else 0
-        ctx.set_echo_model(echo["carrier_hz"], echo["flags"] | extra)
+        for c in (ctx, alt[0]) if alt else (ctx,):
+            c.set_echo_model(echo["carrier_hz"], echo["flags"] | extra)
     call = ctx.reduce if form == "plain" else ctx.reduce_precision
     stream = torch.cuda.current_stream()
     for _ in range(max(warmup, 3)):
@@ -300,27 +301,44 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
 
     # End to end from pinned host memory through the public C ABI: the
     # precision forms use rtacx_reduce_precision_host (chunked host->device
-    # copies overlapped with the accumulation, ping copied back); the plain
-    # form copies the samples in, runs rtacx_reduce and copies the ping out.
-    def e2e_step():
+    # copies overlapped with the accumulation, ping copied back) with two
+    # pings in flight (two contexts on two streams, as a streaming caller
+    # double-buffers: one ping's filter, GEMM and read-back overlap the next
+    # ping's copies); the plain form copies the samples in, runs rtacx_reduce
+    # and copies the ping out.
+    lanes = [(ctx, stream, host_out)]
+    if alt and form != "plain":
+        lanes.append((alt[0], torch.cuda.Stream(), alt[1]))
+
+    def e2e_step(i):
         if form == "plain":
             d_in.copy_(host_in, non_blocking=True)
             call(d_in, n, out, stream=stream)
             host_out.copy_(out, non_blocking=True)
         else:
-            ctx.reduce_precision_host(host_in, n, host_out, stream=stream)
+            c, s, h = lanes[i % len(lanes)]
+            c.reduce_precision_host(host_in, n, h, stream=s)
 
-    e2e_step()
+    for i in range(len(lanes)):
+        e2e_step(i)
     torch.cuda.synchronize()
-    ctx.stream_status(stream)
+    for c, s, _ in lanes:
+        c.stream_status(s)
     if dist:
         dist.barrier()
     ev0.record(stream)
-    for _ in range(steps):
-        e2e_step()
+    for _, s, _ in lanes[1:]:
+        s.wait_event(ev0)
+    for i in range(steps):
+        e2e_step(i)
+    for _, s, _ in lanes[1:]:
+        done = torch.cuda.Event()
+        done.record(s)
+        stream.wait_event(done)
     ev1.record(stream)
     torch.cuda.synchronize()
-    ctx.stream_status(stream)
+    for c, s, _ in lanes:
+        c.stream_status(s)
     t_e2e = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
     # Serial reference points of one step: host->device copy of the samples,
     # the device-resident ping, device->host copy of the ping.
@@ -368,14 +386,22 @@ def run_ours(args, world, rank, local):
     d_in = host_in.to("cuda")
     outs = {f: torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda") for f in forms}
     host_out = torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory()
+    alt = None
+    if "precision" in forms:   # second context: two pings in flight in the end-to-end loop
+        ctx2 = _lib.Context(local)
+        ctx2.configure_2d(**wk.sensor)
+        ctx2.configure_precision(D, taps, center)
+        alt = (ctx2, torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory())
     res = {}
     for f in forms:
         if f == "precision_fp16":   # FP16 per-row-scaled contraction, FP64 carrier phase
-            ctx.configure_precision(D, taps, center, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE)
+            for c in (ctx, alt[0]):
+                c.configure_precision(D, taps, center, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE)
         res[f] = time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch,
-                           wk.echo)
+                           wk.echo, alt)
         if f == "precision_fp16":
-            ctx.configure_precision(D, taps, center)
+            for c in (ctx, alt[0]):
+                c.configure_precision(D, taps, center)
     if rank != 0:
         return
     head = forms[0]
@@ -401,6 +427,9 @@ def run_ours(args, world, rank, local):
                    "form": ("precision: bin-first, BF16x3 tcgen05 complex contraction, FP32 range filter, FP64 carrier phase"
                             if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
                    "l2": "inputs larger than L2 (%.0f MB of samples)" % (n * rec_in / 1e6),
+                   "e2e_path": ("rtacx_reduce_precision_host from pinned host memory, two pings in flight "
+                                "(two contexts, two streams)" if head == "precision" else
+                                "pinned H2D copy + rtacx_reduce + D2H copy"),
                    "parallelism": f"replicas x{world}"},
         "forms": {f: form_line(f) for f in forms},
     }

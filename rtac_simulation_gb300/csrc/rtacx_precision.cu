@@ -216,24 +216,62 @@ k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const 
                 const int k = k0 + 32 * h + lane;
                 float2 g = make_float2(c[h].x, c[h].y);
                 if(k > 0) { g.x += zx; g.y += zy; }
-                sG[rr * kFiltCols + 32 * h + lane] = g;
+                // column cc = 32 h + lane is stored at (cc & 1) * 32 + cc / 2: the
+                // compute loop's lane reads columns 2 lane and 2 lane + 1 from two
+                // conflict-free 32-float2 planes
+                sG[rr * kFiltCols + (lane & 1) * 32 + 16 * h + (lane >> 1)] = g;
             }
         }
         __syncthreads();
+        // Fast path (every row of this warp's eight takes all nt taps of the
+        // chunk): a sliding window of eight staged rows per column in
+        // registers, one shared load per tap and column instead of one per
+        // tap, row and column. Same operations in the same tap order as the
+        // general path.
+        bool full = true;
 #pragma unroll
         for(int q = 0; q < 8; q++) {
             const int rr = warp * 8 + q, r = r0 + rr;
             const int2 w = sW[rr];
-            if(w.x > w.y) continue;
-            // taps t (absolute) with bin j = r + t - center inside the window
-            const int tlo = max(tc, w.x - r + (int)center), thi = min(tc + nt - 1, w.y - r + (int)center);
-            for(int t = tlo; t <= thi; t++) {
-                const float2 c = sT[t - tc];
-                const float4 g2 = *reinterpret_cast<const float4*>(&sG[(rr + t - tc) * kFiltCols + 2 * lane]);
-                acc[q][0].x = fmaf(c.x, g2.x, fmaf(-c.y, g2.y, acc[q][0].x));
-                acc[q][0].y = fmaf(c.x, g2.y, fmaf(c.y, g2.x, acc[q][0].y));
-                acc[q][1].x = fmaf(c.x, g2.z, fmaf(-c.y, g2.w, acc[q][1].x));
-                acc[q][1].y = fmaf(c.x, g2.w, fmaf(c.y, g2.z, acc[q][1].y));
+            if(w.x > w.y || w.x - r + (int)center > tc || w.y - r + (int)center < tc + nt - 1) full = false;
+        }
+        if(full) {
+#pragma unroll
+            for(int h = 0; h < 2; h++) {
+                const float2* col = sG + h * 32 + lane;
+                float2 g[8];
+#pragma unroll
+                for(int i = 0; i < 7; i++) g[i] = col[(warp * 8 + i) * kFiltCols];
+                for(int tt = 0; tt < nt; tt++) {
+                    g[7] = col[(warp * 8 + tt + 7) * kFiltCols];
+                    const float2 c = sT[tt];
+#pragma unroll
+                    for(int q = 0; q < 8; q++) {
+                        acc[q][h].x = fmaf(c.x, g[q].x, fmaf(-c.y, g[q].y, acc[q][h].x));
+                        acc[q][h].y = fmaf(c.x, g[q].y, fmaf(c.y, g[q].x, acc[q][h].y));
+                    }
+#pragma unroll
+                    for(int i = 0; i < 7; i++) g[i] = g[i + 1];
+                }
+            }
+        }
+        else {
+#pragma unroll
+            for(int q = 0; q < 8; q++) {
+                const int rr = warp * 8 + q, r = r0 + rr;
+                const int2 w = sW[rr];
+                if(w.x > w.y) continue;
+                // taps t (absolute) with bin j = r + t - center inside the window
+                const int tlo = max(tc, w.x - r + (int)center), thi = min(tc + nt - 1, w.y - r + (int)center);
+                for(int t = tlo; t <= thi; t++) {
+                    const float2 c = sT[t - tc];
+#pragma unroll
+                    for(int h = 0; h < 2; h++) {
+                        const float2 g = sG[(rr + t - tc) * kFiltCols + h * 32 + lane];
+                        acc[q][h].x = fmaf(c.x, g.x, fmaf(-c.y, g.y, acc[q][h].x));
+                        acc[q][h].y = fmaf(c.x, g.y, fmaf(c.y, g.x, acc[q][h].y));
+                    }
+                }
             }
         }
     }
