@@ -426,7 +426,8 @@ def run_ours(args, world, rank, local):
         "config": {"workload": wk_desc(wk),
                    "form": ("precision: bin-first, BF16x3 tcgen05 complex contraction, FP32 range filter, FP64 carrier phase"
                             if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
-                   "l2": "inputs larger than L2 (%.0f MB of samples)" % (n * rec_in / 1e6),
+                   "l2": ("inputs larger than L2 (%.0f MB of samples)" if n * rec_in > 129e6 else
+                          "inputs smaller than L2 (%.0f MB of samples): timed warm, not flushed") % (n * rec_in / 1e6),
                    "e2e_path": ("rtacx_reduce_precision_host from pinned host memory, two pings in flight "
                                 "(two contexts, two streams)" if head == "precision" else
                                 "pinned H2D copy + rtacx_reduce + D2H copy"),

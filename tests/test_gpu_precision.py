@@ -213,3 +213,41 @@ def test_precision_fp16_rowscale_wide_dynamic_range(oracle):
     rows = np.linalg.norm(want, axis=1) > 0
     rel = np.linalg.norm(got - want, axis=1)[rows] / np.linalg.norm(want, axis=1)[rows]
     assert np.median(rel) <= TOL and np.percentile(rel, 99) <= 10 * TOL, (np.median(rel), np.percentile(rel, 99))
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_precision_long_pulse_multi_chunk_filter(oracle, flags):
+    """101 range taps: the range filter stages its taps in several chunks."""
+    wk = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512, taps=101)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    assert taps.size > 64
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    got = gpu_precision(precision_context(wk, flags=flags), wk.samples, wk.out_shape)
+    assert rel_l2(got, want) <= TOL
+
+
+def test_precision_host_entry_graph_capture():
+    """rtacx_reduce_precision_host is stream-ordered with its copy stream
+    fork-joined by events, so it can be captured in a CUDA graph and replayed."""
+    wk = wl.precision_2d(n_samples=(1 << 21) + 5, n_bearings=128, n_ranges=512)
+    ctx = precision_context(wk)
+    n = wk.samples.shape[0]
+    h = torch.from_numpy(np.ascontiguousarray(wk.samples, dtype=np.float32)).pin_memory()
+    out = torch.zeros(tuple(wk.out_shape) + (2,), dtype=torch.float32).pin_memory()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx.reduce_precision_host(h, n, out, stream=s)     # first call allocates the staging buffers
+    torch.cuda.synchronize()
+    ctx.stream_status(s)
+    ref = out.clone()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ctx.reduce_precision_host(h, n, out, stream=s)
+    out.fill_(float("nan"))
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    ctx.stream_status(s)
+    a, b = out.numpy(), ref.numpy()
+    assert np.isfinite(a).all()
+    assert rel_l2(a[..., 0] + 1j * a[..., 1], b[..., 0] + 1j * b[..., 1]) <= 1e-5
