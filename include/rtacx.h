@@ -321,7 +321,7 @@ int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);
 
 /* Diagnostic: synchronous C = A * B^T on the tensor cores (the GEMM of the
  * precision form). A [M][K], B [N][K] bf16, C [M][N] fp32, row-major,
- * device pointers 16-byte aligned; M % 128 == 0, N % 256 == 0, K % 64 == 0.
+ * device pointers 16-byte aligned; M % 128 == 0, N % 128 == 0, K % 64 == 0.
  * No counterpart in the reference. */
 rtacx_status rtacx_gemm_bf16_tn(const void* A, const void* B, float* C, int M, int N, int K, void* stream);
 

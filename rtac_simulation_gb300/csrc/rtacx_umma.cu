@@ -7,12 +7,14 @@
 // operands are K-major ("TN"); M % 128 == 0, N % 256 == 0, K % 64 == 0
 // (callers pad).
 //
-// One CTA computes a 128 x 256 tile with four warps:
+// One CTA computes a 128 x BN tile with four warps (BN = 256 with a 4-stage
+// ring, one CTA per SM; BN = 128 with a 3-stage ring, two CTAs per SM, when N
+// is a multiple of 128 but not of 256):
 //   warp 0, lane 0  TMA producer: cp.async.bulk.tensor 2D loads of a 128x64
-//                   A tile and a 256x64 B tile per stage (128-byte swizzle)
-//                   into a 4-stage shared-memory ring guarded by mbarriers;
+//                   A tile and a BNx64 B tile per stage (128-byte swizzle)
+//                   into the shared-memory ring guarded by mbarriers;
 //   warp 1, lane 0  MMA issuer: four tcgen05.mma.kind::f16 (K = 16 each) per
-//                   stage into a 128-lane x 256-column fp32 TMEM accumulator,
+//                   stage into a 128-lane x BN-column fp32 TMEM accumulator,
 //                   tcgen05.commit frees the stage;
 //   warps 0-3       epilogue: tcgen05.ld 32x32b of their TMEM lane quadrant,
 //                   optional row / column scaling, fp32 stores of whole
@@ -29,22 +31,30 @@ namespace rtacx {
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int BM = 128, BK = 64;
 constexpr int kThreads = 128;
 constexpr uint32_t A_BYTES = BM * BK * 2;
-constexpr uint32_t B_BYTES = BN * BK * 2;
-constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr uint32_t TMEM_COLS = 256;
-constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+
+template <int BN_, int STAGES_>
+struct Tile {
+    static constexpr int BN = BN_, STAGES = STAGES_;
+    static constexpr uint32_t B_BYTES = BN * BK * 2;
+    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr uint32_t TMEM_COLS = BN;           // power of two >= 32
+    static constexpr size_t SMEM_BYTES = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr int CTAS_PER_SM = BN == 128 ? 2 : 1;
+};
+using TileWide = Tile<256, 4>;
+using TileNarrow = Tile<128, 3>;
 constexpr long long kWaitCycles = 4000000000ll;
 
 // Instruction descriptor of tcgen05.mma.kind::f16: D = f32 (bits 4-5 = 1),
 // A and B format at bits 7-9 and 10-12 (0 = f16, 1 = bf16; always the same
 // type for both), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22,
 // M >> 4 at bits 24-28.
-__host__ __device__ constexpr uint32_t idesc_for(bool f16)
+__host__ __device__ constexpr uint32_t idesc_for(bool f16, int bn)
 {
-    return (1u << 4) | ((f16 ? 0u : 1u) << 7) | ((f16 ? 0u : 1u) << 10) | ((uint32_t)(BN >> 3) << 17) |
+    return (1u << 4) | ((f16 ? 0u : 1u) << 7) | ((f16 ? 0u : 1u) << 10) | ((uint32_t)(bn >> 3) << 17) |
            ((uint32_t)(BM >> 4) << 24);
 }
 
@@ -102,13 +112,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-template <bool kF16>
+template <bool kF16, int BN>
 __device__ __forceinline__ void umma_16bit(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
 {
     asm volatile("{\n\t.reg .pred p;\n\t"
                  "setp.ne.b32 p, %4, 0;\n\t"
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc_for(kF16)), "r"(accumulate)
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc_for(kF16, BN)), "r"(accumulate)
                  : "memory");
 }
 
@@ -135,12 +145,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-template <bool kF16>
-__global__ void __launch_bounds__(kThreads, 1)
+template <bool kF16, typename T>
+__global__ void __launch_bounds__(kThreads, T::CTAS_PER_SM)
 k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
           float* __restrict__ C, int M, int N, int K, int ldc, const float* __restrict__ row_scale,
           const float* __restrict__ col_scale, uint32_t* __restrict__ err)
 {
+    constexpr int BN = T::BN, STAGES = T::STAGES;
+    constexpr uint32_t STAGE_BYTES = T::STAGE_BYTES, TMEM_COLS = T::TMEM_COLS;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
@@ -195,7 +207,7 @@ k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
             const uint64_t ad = smem_desc(a), bd = smem_desc(a + A_BYTES);
 #pragma unroll
             for(int kk = 0; kk < BK / 16; kk++)   // 32 bytes of K per MMA: +2 in descriptor units
-                umma_16bit<kF16>(tmem, ad + 2 * kk, bd + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
+                umma_16bit<kF16, BN>(tmem, ad + 2 * kk, bd + 2 * kk, (kb > 0 || kk > 0) ? 1u : 0u);
             umma_commit(empty_bar(s));
         }
         umma_commit(accum_bar);   // arrives once every MMA issued above has completed
@@ -282,7 +294,7 @@ bool make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k, uint
 
 } // namespace
 
-size_t gemm_smem_bytes() { return SMEM_BYTES; }
+size_t gemm_smem_bytes() { return std::max(TileWide::SMEM_BYTES, TileNarrow::SMEM_BYTES); }
 
 // C = row_scale * col_scale * (A * B^T); A [M][K], B [N][K] both bf16 or
 // both fp16 (16-byte aligned, row stride K), C [M][ldc] fp32, scales
@@ -291,35 +303,51 @@ size_t gemm_smem_bytes() { return SMEM_BYTES; }
 rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K, int ldc,
                      cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale)
 {
-    if(M <= 0 || N <= 0 || K <= 0 || M % BM || N % BN || K % BK || ldc < N || ldc % 4) {
-        error = "gemm shape must be multiples of 128 x 256 x 64";
+    if(M <= 0 || N <= 0 || K <= 0 || M % BM || N % 128 || K % BK || ldc < N || ldc % 4) {
+        error = "gemm shape must be multiples of 128 x 128 x 64";
         return RTACX_ERR_INVALID_ARGUMENT;
     }
+    // 128 x 256 tiles whenever N allows them; 128 x 128 tiles (two CTAs per
+    // SM) for N a multiple of 128 only. Measured on the 4096 x 1024 x 3072
+    // contraction: 27 us wide, 30 us narrow (the narrow grid re-reads A twice
+    // as often through L2).
+    const bool wide = N % 256 == 0;
+    const int bn = wide ? TileWide::BN : TileNarrow::BN;
     if((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16 || reinterpret_cast<uintptr_t>(C) % 16 ||
        reinterpret_cast<uintptr_t>(col_scale) % 16) {
         error = "gemm operands must be 16-byte aligned";
         return RTACX_ERR_INVALID_ARGUMENT;
     }
     CUtensorMap ma, mb;
-    if(!make_map(&ma, A, (uint64_t)M, (uint64_t)K, BM, f16) || !make_map(&mb, B, (uint64_t)N, (uint64_t)K, BN, f16)) {
+    if(!make_map(&ma, A, (uint64_t)M, (uint64_t)K, BM, f16) || !make_map(&mb, B, (uint64_t)N, (uint64_t)K, bn, f16)) {
         error = "cuTensorMapEncodeTiled failed";
         return RTACX_ERR_CUDA;
     }
     static bool attr = false;
     if(!attr) {
-        if(cudaFuncSetAttribute(k_gemm_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) !=
-               cudaSuccess ||
-           cudaFuncSetAttribute(k_gemm_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES) !=
-               cudaSuccess) {
+        if(cudaFuncSetAttribute(k_gemm_tn<false, TileWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TileWide::SMEM_BYTES) != cudaSuccess ||
+           cudaFuncSetAttribute(k_gemm_tn<true, TileWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TileWide::SMEM_BYTES) != cudaSuccess ||
+           cudaFuncSetAttribute(k_gemm_tn<false, TileNarrow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TileNarrow::SMEM_BYTES) != cudaSuccess ||
+           cudaFuncSetAttribute(k_gemm_tn<true, TileNarrow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TileNarrow::SMEM_BYTES) != cudaSuccess) {
             cudaGetLastError();
             error = "cannot reserve shared memory for the tensor-core GEMM";
             return RTACX_ERR_CUDA;
         }
         attr = true;
     }
-    dim3 grid(N / BN, M / BM);
-    if(f16) k_gemm_tn<true><<<grid, kThreads, SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
-    else k_gemm_tn<false><<<grid, kThreads, SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
+    dim3 grid(N / bn, M / BM);
+    if(wide) {
+        if(f16) k_gemm_tn<true, TileWide><<<grid, kThreads, TileWide::SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
+        else k_gemm_tn<false, TileWide><<<grid, kThreads, TileWide::SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
+    }
+    else {
+        if(f16) k_gemm_tn<true, TileNarrow><<<grid, kThreads, TileNarrow::SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
+        else k_gemm_tn<false, TileNarrow><<<grid, kThreads, TileNarrow::SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
+    }
     const cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) { error = std::string("k_gemm_tn: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;

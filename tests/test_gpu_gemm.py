@@ -14,7 +14,10 @@ if not torch.cuda.is_available():
     pytest.skip("needs a GPU", allow_module_level=True)
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 512, 192), (384, 256, 1024), (4096, 1024, 3072)])
+# 128 x 256 tiles (N a multiple of 256) and 128 x 128 tiles, two CTAs per SM
+# (N = 384: a multiple of 128 only).
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 512, 192), (384, 256, 1024), (256, 384, 128),
+                                   (4096, 1024, 3072), (8192, 2048, 256)])
 def test_gemm_bf16_matches_fp32_reference(M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N * 3 + K)
     A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
