@@ -24,6 +24,7 @@ on the data path): `value` is the sum of the ranks' pings over the max time.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import math
 import os
@@ -60,7 +61,8 @@ KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default: 500 for this implementation's pings, 3 for the host reference)")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", default=DEFAULT_CONFIG, choices=sorted(workloads.CONFIGS))
@@ -94,9 +96,9 @@ def max_over_ranks(dist, x: float) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms."""
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -104,6 +106,14 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.path = None
+        self.t_begin = self.t_end = None
+
+    def begin(self):
+        """Marks the start of the timed region (host wall clock)."""
+        self.t_begin = datetime.datetime.now()
+
+    def end(self):
+        self.t_end = datetime.datetime.now()
 
     def start(self):
         if not shutil.which("nvidia-smi"):
@@ -111,7 +121,7 @@ class ClockSampler:
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
-                                      "--format=csv,noheader,nounits", "-lms", "200"],
+                                      "--format=csv,noheader,nounits", "-lms", "20"],
                                      stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         time.sleep(0.3)
 
@@ -123,22 +133,26 @@ class ClockSampler:
         self.proc.wait()
         rows = [l.split(",") for l in open(self.path).read().strip().split("\n") if l.strip()]
         os.unlink(self.path)
-        sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        parsed = []
         for r in rows:
             r = [x.strip() for x in r]
             try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
+                ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f")
+                parsed.append((ts, float(r[2]), float(r[3]), [n for n, v in zip(names, r[6:10]) if v.lower() == "active"]))
             except (ValueError, IndexError):
                 continue
-            for name, v in zip(names, r[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        if not sm:
+        region = []
+        if self.t_begin and self.t_end:      # the samples taken during the timed region
+            lo = self.t_begin - datetime.timedelta(milliseconds=25)
+            hi = self.t_end + datetime.timedelta(milliseconds=25)
+            region = [p for p in parsed if lo <= p[0] <= hi]
+        inside = region or parsed
+        if not inside:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(p[1] for p in inside), "sm_max_mhz": max(p[2] for p in inside),
+                "reasons": sorted({n for p in inside for n in p[3]}), "samples": len(inside),
+                "in_timed_region": bool(region)}
 
 
 def measured_peaks() -> dict:
@@ -281,11 +295,13 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.begin()
     ev0.record(stream)
     for _ in range(steps):
         call(d_in, n, out, stream=stream)
     ev1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     clk = clocks.stop()
     ctx.stream_status(stream)
     t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
@@ -293,10 +309,11 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     ctx.set_tracing(True)
     names = _lib.STAGES if form == "plain" else _lib.PRECISION_STAGES
     stage = {k: 0.0 for k in names}
-    for _ in range(steps):
+    traced = min(steps, 20)
+    for _ in range(traced):
         call(d_in, n, out, stream=stream)
         for k, v in ctx.stage_times(precision=(form != "plain")).items():
-            stage[k] += v / steps
+            stage[k] += v / traced
     ctx.set_tracing(False)
 
     # End to end from pinned host memory through the public C ABI: the
@@ -397,8 +414,12 @@ def run_ours(args, world, rank, local):
         if f == "precision_fp16":   # FP16 per-row-scaled contraction, FP64 carrier phase
             for c in (ctx, alt[0]):
                 c.configure_precision(D, taps, center, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE)
-        res[f] = time_form(ctx, f, d_in, n, outs[f], host_in, host_out, args.steps, args.warmup, dist, local, torch,
+        # The plain form (~72 ms per ping here) is timed over at most 20 steps
+        # when it is not the headline form.
+        steps_f = min(args.steps, 20) if (f == "plain" and forms[0] != "plain") else args.steps
+        res[f] = time_form(ctx, f, d_in, n, outs[f], host_in, host_out, steps_f, args.warmup, dist, local, torch,
                            wk.echo, alt)
+        res[f]["steps"] = steps_f
         if f == "precision_fp16":
             for c in (ctx, alt[0]):
                 c.configure_precision(D, taps, center)
@@ -410,8 +431,8 @@ def run_ours(args, world, rank, local):
 
     def form_line(f):
         r = res[f]
-        return {"samples_per_s": world * n * args.steps / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / args.steps,
-                "e2e_samples_per_s": world * n * args.steps / r["t_e2e"],
+        return {"samples_per_s": world * n * r["steps"] / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / r["steps"],
+                "e2e_samples_per_s": world * n * r["steps"] / r["t_e2e"], "steps": r["steps"],
                 "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()},
                 "e2e_step_ms": {k: round(v, 4) for k, v in r["e2e_split"].items()},
                 "clocks": r["clocks"]}
@@ -574,11 +595,13 @@ def run_batch(args, world, rank, local):
         dist.barrier()
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.begin()
     ev0.record(stream)
     for _ in range(args.steps):
         batch.run(stream)
     ev1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     clk = clocks.stop()
     t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
     # Per-ping device latency: each ping alone through rtacx_reduce.
@@ -633,6 +656,8 @@ def run_batch(args, world, rank, local):
 
 def main():
     args = parse_args()
+    if args.steps is None:   # the host reference's steps take seconds, a batch ~70 ms, a precision ping ~0.2 ms
+        args.steps = 3 if args.impl == "reference" else (20 if args.config == "batched_mix" else 500)
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
