@@ -4,7 +4,7 @@
 // context (1D or 2D). rtacx_batch_plan builds, once:
 //   * a device descriptor per ping (PingDev: its samples, scratch, tables);
 //   * (ping, index) maps that let one launch per binning stage cover every
-//     ping (count, column scan, bin scan, scatter, windows);
+//     ping (reset of the totals, count, bin scan, scatter, windows);
 //   * the gather work list: 2D output tiles and 1D row groups of every ping,
 //     heaviest first, consumed by one persistent kernel through an atomic
 //     work counter;

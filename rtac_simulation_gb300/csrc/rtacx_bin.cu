@@ -10,16 +10,23 @@
 //
 // Passes (persistent CTAs, each owning one contiguous chunk of the input,
 // processed in tiles of kTileLoads independent record loads per thread):
-//   k_count      key of every sample, per-CTA histogram in shared memory,
-//                added into the zeroed bin totals; out-of-range counts.
-//   k_binscan    exclusive scan of bin totals -> bin offsets, and one shared
-//                write cursor per bin initialised to its offset.
-//   k_scatter    re-reads the chunk; per tile, ranks each sample in a
-//                shared-memory histogram, reserves one run per (tile, bin)
-//                with a global atomicAdd on the bin's cursor and writes the
-//                float4 {re, im, travel, bearing} records of the run.
-//   k_windows    reference windows (do_make_bins, src/Binner.cu:82-106) as
-//                range-bin intervals, intersected with each row's PSF support.
+//   k_count           key of every sample, per-CTA histogram in shared
+//                     memory, added into the zeroed bin totals and per-1024-bin
+//                     block sums; out-of-range counts.
+//   k_binscan_blocks  one CTA per 1024 bins: exclusive scan of the totals ->
+//                     bin offsets, and one shared write cursor per bin
+//                     initialised to its offset (k_binscan: the single-CTA
+//                     scan of the batched form and of the split gather).
+//   k_scatter_staged  re-reads the chunk in tiles of 12K records, sorts each
+//                     tile by bin in shared memory, reserves one run per
+//                     (tile, bin) with a global atomicAdd on the bin's cursor
+//                     and writes the float4 {re, im, travel, bearing} records
+//                     of each run with consecutive lanes (k_scatter: the same
+//                     reservation without staging, when the per-bin tables do
+//                     not fit next to a tile, and in the batched form).
+//   k_windows         reference windows (do_make_bins, src/Binner.cu:82-106)
+//                     as range-bin intervals, intersected with each row's PSF
+//                     support.
 // Every bin has one write frontier shared by all CTAs, so the partially
 // written 128-byte lines of the sorted array number about one per bin and
 // complete in L2 before eviction (per-CTA sub-ranges inside each bin would

@@ -232,7 +232,7 @@ struct Context {
     size_t acc_smem = 0;                // dynamic shared memory of the precision accumulation
     uint32_t acc_blocks_per_sm = 1;
     uint32_t hist_threads = 0;
-    size_t hist_cols = 0;               // allocated CTA x bin entries
+    size_t hist_cols = 0;               // allocated words of d_hist (the write cursors)
     uint32_t* d_hist = nullptr;         // [nBins][kCursorStride]: the scatter's per-bin write cursors
 
     // Split persistent gather of 2D pings (see rtacx_reduce.cu).
