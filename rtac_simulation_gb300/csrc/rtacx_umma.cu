@@ -24,6 +24,7 @@
 // issued MMAs and freeing its TMEM.
 #include "rtacx_internal.cuh"
 
+#include <atomic>
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -323,8 +324,15 @@ rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C,
         error = "cuTensorMapEncodeTiled failed";
         return RTACX_ERR_CUDA;
     }
-    static bool attr = false;
-    if(!attr) {
+    // Function attributes belong to a device's context: set them once per device.
+    static std::atomic<uint64_t> attr_done{0};
+    int dev = 0;
+    if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        error = "cannot query the current device";
+        return RTACX_ERR_CUDA;
+    }
+    if(!(attr_done.load() & (1ull << dev))) {
         if(cudaFuncSetAttribute(k_gemm_tn<false, TileWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)TileWide::SMEM_BYTES) != cudaSuccess ||
            cudaFuncSetAttribute(k_gemm_tn<true, TileWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -337,7 +345,7 @@ rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C,
             error = "cannot reserve shared memory for the tensor-core GEMM";
             return RTACX_ERR_CUDA;
         }
-        attr = true;
+        attr_done.fetch_or(1ull << dev);
     }
     dim3 grid(N / bn, M / BM);
     if(wide) {

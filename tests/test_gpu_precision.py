@@ -251,3 +251,64 @@ def test_precision_host_entry_graph_capture():
     a, b = out.numpy(), ref.numpy()
     assert np.isfinite(a).all()
     assert rel_l2(a[..., 0] + 1j * a[..., 1], b[..., 0] + 1j * b[..., 1]) <= 1e-5
+
+
+def _small_precision():
+    return wl.precision_2d(n_samples=1 << 12, n_bearings=128, n_ranges=512)
+
+
+def _bin_travel(oracle, sensor, r):
+    """A travel whose reference key is range bin r."""
+    t = np.float32(sensor["range_min"] + r * float(wl.linspace_resolution(sensor["range_min"], sensor["range_max"],
+                                                                           sensor["range_count"])))
+    keys, _ = oracle.range_keys(sensor["range_count"], sensor["range_min"], sensor["range_max"], sensor["margin"],
+                                np.array([t], np.float32))
+    assert keys[0] == r
+    return t
+
+
+def test_precision_all_out_of_range_and_single_bin_are_zero(oracle):
+    """No in-range sample, or samples in one range bin only: every window is
+    the reference's empty view, so the ping is zero (src/Binner.cu:95-104)."""
+    wk = _small_precision()
+    ctx = precision_context(wk)
+    smp = wk.samples.copy()
+    smp[:, 2] = np.float32(1e4)                      # above the range
+    assert np.all(gpu_precision(ctx, smp, wk.out_shape) == 0)
+    smp[:, 2] = _bin_travel(oracle, wk.sensor, 200)   # all in bin 200
+    assert np.all(gpu_precision(ctx, smp, wk.out_shape) == 0)
+
+
+def test_precision_zero_amplitude_samples_open_windows(oracle):
+    """A zero-amplitude sample still makes its bin non-empty: bins 200 + 201
+    give non-empty windows, bin 200 alone gives the empty view."""
+    wk = _small_precision()
+    ctx = precision_context(wk)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    smp = wk.samples[:64].copy()
+    smp[:, 2] = _bin_travel(oracle, wk.sensor, 200)
+    zero = smp[:8].copy()
+    zero[:, 0] = 0.0
+    zero[:, 1] = 0.0
+    zero[:, 2] = _bin_travel(oracle, wk.sensor, 201)
+    both = np.concatenate([smp, zero])
+    got = gpu_precision(ctx, both, wk.out_shape)
+    want = oracle.reduce_binned(oracle.apply_echo(both, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    assert np.linalg.norm(want) > 0
+    assert rel_l2(got, want) <= TOL
+    assert np.all(gpu_precision(ctx, smp, wk.out_shape) == 0)
+
+
+def test_precision_degenerate_bearings_match_oracle(oracle):
+    """NaN, infinite and out-of-table bearings clamp to the edge cells in the
+    kernel exactly as in the oracle's binary search."""
+    wk = _small_precision()
+    ctx = precision_context(wk)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    smp = wk.samples.copy()
+    bad = np.array([np.nan, np.inf, -np.inf, 3.0, -3.0, 1e30], np.float32)
+    smp[:bad.size * 64, 3] = np.repeat(bad, 64)
+    got = gpu_precision(ctx, smp, wk.out_shape)
+    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    assert np.isfinite(got).all()
+    assert rel_l2(got, want) <= TOL
