@@ -278,7 +278,11 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     """Device time of `steps` pings (samples resident), per-stage event times
     and the end-to-end time with pinned host buffers, for one form. The form
     "precision_compensated" is the precision form with the carrier phase
-    reduced in compensated float arithmetic instead of FP64."""
+    reduced in compensated float arithmetic instead of FP64. With `alt` (a
+    second context, its host and device ping buffers) the precision forms are
+    timed with two pings in flight: consecutive pings alternate between the
+    two contexts on two streams, as a streaming caller double-buffers; the
+    single-stream time of the same pings is reported beside it."""
     from rtac_simulation_gb300 import _lib
     if echo:
         extra = _lib.RTACX_ECHO_PHASE_COMPENSATED if form == "precision_compensated" else 0
@@ -295,14 +299,43 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks.begin()
+    # Single stream: one ping after the other (the per-ping latency).
     ev0.record(stream)
     for _ in range(steps):
         call(d_in, n, out, stream=stream)
     ev1.record(stream)
     torch.cuda.synchronize()
+    t_single = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
+    # Two pings in flight (precision forms): the timed throughput.
+    dev_lanes = [(ctx, stream, out)]
+    if alt and form != "plain":
+        dev_lanes.append((alt[0], torch.cuda.Stream(), alt[2]))
+
+    def dev_step(i):
+        c, s, o = dev_lanes[i % len(dev_lanes)]
+        (c.reduce if form == "plain" else c.reduce_precision)(d_in, n, o, stream=s)
+
+    for i in range(max(warmup, 3) * len(dev_lanes)):
+        dev_step(i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks.begin()
+    ev0.record(stream)
+    for _, s, _ in dev_lanes[1:]:
+        s.wait_event(ev0)
+    for i in range(steps):
+        dev_step(i)
+    for _, s, _ in dev_lanes[1:]:
+        done = torch.cuda.Event()
+        done.record(s)
+        stream.wait_event(done)
+    ev1.record(stream)
+    torch.cuda.synchronize()
     clocks.end()
     clk = clocks.stop()
+    for c, s, _ in dev_lanes:
+        c.stream_status(s)
     ctx.stream_status(stream)
     t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
 
@@ -370,7 +403,8 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     e2e_split = {"h2d_ms": evs[0].elapsed_time(evs[1]), "ping_ms": evs[1].elapsed_time(evs[2]),
                  "d2h_ms": evs[2].elapsed_time(evs[3]), "e2e_step_ms": 1e3 * t_e2e / steps}
-    return dict(t_dev=t_dev, stage=stage, t_e2e=t_e2e, clocks=clk, e2e_split=e2e_split)
+    return dict(t_dev=t_dev, t_single=t_single, stage=stage, t_e2e=t_e2e, clocks=clk, e2e_split=e2e_split,
+                lanes=len(dev_lanes))
 
 
 def to_complex(t):
@@ -408,7 +442,8 @@ def run_ours(args, world, rank, local):
         ctx2 = _lib.Context(local)
         ctx2.configure_2d(**wk.sensor)
         ctx2.configure_precision(D, taps, center)
-        alt = (ctx2, torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory())
+        alt = (ctx2, torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory(),
+               torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda"))
     res = {}
     for f in forms:
         if f == "precision_fp16":   # FP16 per-row-scaled contraction, FP64 carrier phase
@@ -432,6 +467,7 @@ def run_ours(args, world, rank, local):
     def form_line(f):
         r = res[f]
         return {"samples_per_s": world * n * r["steps"] / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / r["steps"],
+                "pings_in_flight": r["lanes"], "latency_ms_single_stream": 1e3 * r["t_single"] / r["steps"],
                 "e2e_samples_per_s": world * n * r["steps"] / r["t_e2e"], "steps": r["steps"],
                 "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()},
                 "e2e_step_ms": {k: round(v, 4) for k, v in r["e2e_split"].items()},
@@ -442,6 +478,7 @@ def run_ours(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * res[head]["t_dev"] / args.steps,
         "pings_per_s": world * args.steps / res[head]["t_dev"],
+        "latency_ms": 1e3 * res[head]["t_single"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": wk_desc(wk),
@@ -449,6 +486,9 @@ def run_ours(args, world, rank, local):
                             if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
                    "l2": ("inputs larger than L2 (%.0f MB of samples)" if n * rec_in > 129e6 else
                           "inputs smaller than L2 (%.0f MB of samples): timed warm, not flushed") % (n * rec_in / 1e6),
+                   "timing": ("two pings in flight (two contexts on two streams, consecutive pings alternate); "
+                              "latency_ms = one ping at a time on one stream" if head == "precision" else
+                              "one ping at a time on one stream"),
                    "e2e_path": ("rtacx_reduce_precision_host from pinned host memory, two pings in flight "
                                 "(two contexts, two streams)" if head == "precision" else
                                 "pinned H2D copy + rtacx_reduce + D2H copy"),
