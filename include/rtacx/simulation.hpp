@@ -301,11 +301,13 @@ class SensorInstance2D_Complex : public SensorInstance {
     SensorInfo2D::ConstPtr info_;
     DeviceVector<SimSample2D> receivedSamples_;
     DeviceVector<Complex> sensorOutput_;
+protected:
     SensorInstance2D_Complex(const SensorInfo2D::ConstPtr& info, float c)
         : SensorInstance(info->ranges(), info->waveform(), c), info_(info)
     {
         this->set_ranges(info->ranges());
     }
+private:
     void configure() override
     {
         const std::vector<Complex> pulse = pulse_table();
@@ -345,6 +347,62 @@ public:
                            reinterpret_cast<float*>(sensorOutput_.data()), nullptr));
         check(rtacx_stream_status(ctx_, nullptr));
     }
+};
+
+// A device ping with its geometry: the counterpart of rtac_base's
+// cuda::CudaPing2D<Complex<float>> as returned by the reference's
+// SensorInstance2D_2<T>::get_ping() (include/rtac_simulation/SensorInstance2D.h:144):
+// range Linspace, bearings, [range][bearing] complex64 data on the device.
+class Ping2D {
+    Linspace ranges_;
+    std::vector<float> bearings_;
+    const Complex* data_;
+public:
+    Ping2D(const Linspace& ranges, std::vector<float> bearings, const Complex* data)
+        : ranges_(ranges), bearings_(std::move(bearings)), data_(data) {}
+    const Linspace& ranges() const { return ranges_; }
+    const std::vector<float>& bearings() const { return bearings_; }
+    unsigned int width() const { return (unsigned int)bearings_.size(); }
+    unsigned int height() const { return ranges_.size(); }
+    unsigned int size() const { return width() * height(); }
+    const Complex* ping_data() const { return data_; }
+    std::vector<Complex> to_host() const
+    {
+        std::vector<Complex> out(size());
+        if(!out.empty())
+            check_cuda(cudaMemcpy(out.data(), data_, out.size() * sizeof(Complex), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return out;
+    }
+};
+
+// The reference's scalar-templated 2D instance
+// (include/rtac_simulation/SensorInstance2D.h:96-151), which its factory
+// creates as SensorInstance2D_2<Complex<float>> (src/factories/SensorInfoFactory.cpp:28).
+// The reference reduces into complex pings only (src/SensorInstance2D.cu:85-119),
+// so Complex is the only supported scalar. The receiver pose of the
+// reference's Create() belongs to the ray caster and is not modelled here.
+template <typename T>
+class SensorInstance2D_2 {
+    static_assert(sizeof(T) == 0, "SensorInstance2D_2 supports Complex pings only, as the reference's do_reduce");
+};
+
+template <>
+class SensorInstance2D_2<Complex> : public SensorInstance2D_Complex {
+    SensorInstance2D_2(const SensorInfo2D::ConstPtr& info, float c) : SensorInstance2D_Complex(info, c) {}
+public:
+    using Ptr = std::shared_ptr<SensorInstance2D_2<Complex>>;
+    static Ptr Create(const SensorInfo2D::ConstPtr& info, float soundCelerity = 1500.0f)
+    {
+        return Ptr(new SensorInstance2D_2<Complex>(info, soundCelerity));
+    }
+    static Ptr Create(const SensorInfo::ConstPtr& info, float soundCelerity = 1500.0f)
+    {
+        auto info2d = std::dynamic_pointer_cast<const SensorInfo2D>(info);
+        if(!info2d) throw std::runtime_error("A SensorInstance2D must be created with a SensorInfo2D instance");
+        return Create(info2d, soundCelerity);
+    }
+    bool is_complex() const { return true; }
+    Ping2D get_ping() const { return Ping2D(this->ranges(), this->bearings(), this->output().data()); }
 };
 
 // Ping file sink (include/rtac_simulation/sinks/FileSink.h:12-31,

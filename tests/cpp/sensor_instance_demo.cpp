@@ -49,17 +49,28 @@ int main(int argc, char** argv)
         if((int)scalars["dims"] == 2) {
             auto beam = BeamDirectivity::Create((float)scalars["beam_span"], arrays["beam"]);
             auto info = SensorInfo2D::Create(arrays["bearings"], ranges, waveform, beam);
-            auto sensor = SensorInstance2D_Complex::Create(SensorInfo2D::ConstPtr(info), (float)scalars["celerity"]);
             const size_t n = raw.size() / sizeof(SimSample2D);
-            sensor->set_sample_count((unsigned)n);
-            sensor->samples().copy_from_host(reinterpret_cast<const SimSample2D*>(raw.data()), n);
-            sensor->compute_output();
-            out = sensor->output().to_host();
             if(argc == 5) {
+                // The reference factory's spelling: SensorInstance2D_2<Complex<float>>, read through get_ping().
+                auto sensor = SensorInstance2D_2<Complex>::Create(SensorInfo::ConstPtr(info), (float)scalars["celerity"]);
+                sensor->set_sample_count((unsigned)n);
+                sensor->samples().copy_from_host(reinterpret_cast<const SimSample2D*>(raw.data()), n);
+                sensor->compute_output();
+                const Ping2D ping = sensor->get_ping();
+                if(ping.width() != sensor->width() || ping.height() != sensor->height() || !sensor->is_complex())
+                    throw std::runtime_error("get_ping geometry");
+                out = ping.to_host();
                 auto sink = FileSink::Create(argv[4], true);
                 sink->set_output(sensor);
                 sensor->compute_output();
                 sink->set_output(sensor);
+            }
+            else {
+                auto sensor = SensorInstance2D_Complex::Create(SensorInfo2D::ConstPtr(info), (float)scalars["celerity"]);
+                sensor->set_sample_count((unsigned)n);
+                sensor->samples().copy_from_host(reinterpret_cast<const SimSample2D*>(raw.data()), n);
+                sensor->compute_output();
+                out = sensor->output().to_host();
             }
         }
         else {

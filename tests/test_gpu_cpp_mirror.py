@@ -51,10 +51,14 @@ def test_cpp_mirror_1d_fixed_waveform(tmp_path, oracle):
     assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-5
 
 
-def test_cpp_file_sink_records(tmp_path):
+def test_cpp_file_sink_records(tmp_path, oracle):
+    """SensorInstance2D_2<Complex> (the reference factory's type) read through
+    get_ping(), and two FileSink records of its pings."""
     from rtac_simulation_gb300.sink import read_pings
     wk = wl.oculus_reference_2d(n_samples=20000)
     got = run_demo(tmp_path, wk, 1.2e6, 1.0, fixed=False, sink=tmp_path / "pings.bin")
+    want = oracle.reduce(wk.samples, wk.sensor)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-5
     recs = read_pings(tmp_path / "pings.bin")
     assert len(recs) == 2
     for r in recs:
