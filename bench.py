@@ -432,6 +432,8 @@ def run_ours(args, world, rank, local):
         D, taps, center = workloads.precision_tables(wk.sensor)
         ctx.configure_precision(D, taps, center)
         forms = ["precision", "precision_compensated", "precision_fp16", "plain"]
+        if args.config == "stress_2d":   # the clustered ping: also with the hot-range replicas
+            forms.insert(3, "precision_hot")
     ctx.reserve(n)
     host_in = torch.from_numpy(wk.samples.reshape(-1)).pin_memory()
     d_in = host_in.to("cuda")
@@ -446,16 +448,17 @@ def run_ours(args, world, rank, local):
                torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda"))
     res = {}
     for f in forms:
-        if f == "precision_fp16":   # FP16 per-row-scaled contraction, FP64 carrier phase
+        if f in ("precision_fp16", "precision_hot"):   # FP16 contraction / hot-range replicas, FP64 phase
+            fl = _lib.RTACX_PRECISION_FP16_ROWSCALE if f == "precision_fp16" else _lib.RTACX_PRECISION_HOT_RANGE
             for c in (ctx, alt[0]):
-                c.configure_precision(D, taps, center, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE)
+                c.configure_precision(D, taps, center, flags=fl)
         # The plain form (~72 ms per ping here) is timed over at most 20 steps
         # when it is not the headline form.
         steps_f = min(args.steps, 20) if (f == "plain" and forms[0] != "plain") else args.steps
         res[f] = time_form(ctx, f, d_in, n, outs[f], host_in, host_out, steps_f, args.warmup, dist, local, torch,
                            wk.echo, alt)
         res[f]["steps"] = steps_f
-        if f == "precision_fp16":
+        if f in ("precision_fp16", "precision_hot"):
             for c in (ctx, alt[0]):
                 c.configure_precision(D, taps, center)
     if rank != 0:
@@ -593,7 +596,7 @@ def run_ours(args, world, rank, local):
                 float(np.linalg.norm(got_plain[b0:b1] - want) / np.linalg.norm(want)))
             if "precision" in forms:
                 want_b = oracle.reduce_binned(exact, wk.sensor, D, taps, center, rows=(b0, b1), threads=threads)
-                for f in ("precision", "precision_compensated", "precision_fp16"):
+                for f in [f_ for f_ in forms if f_.startswith("precision")]:
                     got_p = to_complex(outs[f])
                     acc.setdefault(f"{f}_rel_l2_vs_fp64_binned", []).append(
                         float(np.linalg.norm(got_p[b0:b1] - want_b) / np.linalg.norm(want_b)))

@@ -188,6 +188,15 @@ typedef struct {
  * products exact in the FP32 accumulator) and the scales are undone exactly
  * in the GEMM epilogue. */
 #define RTACX_PRECISION_FP16_ROWSCALE 1u
+/* Contention relief for clustered scenes (a strong target concentrating many
+ * samples in few range bins): a strided subsample of each ping (1/128 of the
+ * samples, or of the first 2^21-record chunk of rtacx_reduce_precision_host)
+ * finds the densest 256-row range interval; if it holds at least a tenth of
+ * the samples and four times its uniform share, those rows are accumulated
+ * into eight replicas (chosen by CTA and warp), added back into the grid
+ * before the range filter, so vector reductions to the same cells no longer
+ * serialise. Same result up to the order of float additions. */
+#define RTACX_PRECISION_HOT_RANGE 2u
 rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_desc* desc);
 rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n,
                                     float* out, void* stream);

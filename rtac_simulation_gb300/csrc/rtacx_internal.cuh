@@ -279,6 +279,11 @@ struct Context {
     uint32_t* d_rowmax = nullptr;       // [nR] largest |component| of each filtered row (float bits)
     float* d_row_scale = nullptr;       // [Mpad] 2^-e per row: undoes the row's scaling in the GEMM epilogue
     float* d_col_scale = nullptr;       // [Npad] 2^-e per directivity column
+    // Hot range interval (RTACX_PRECISION_HOT_RANGE).
+    bool prec_hot = false;
+    int2* d_hot = nullptr;              // {first row, length} of the hot interval (length 0: none)
+    uint32_t* d_hotcnt = nullptr;       // [nR] subsample counts (zero between pings)
+    float4* d_rep = nullptr;            // [hot rows][replicas][nB] pair-cell replicas
 
     // Host-buffer streaming (rtacx_reduce_precision_host): two device staging
     // buffers of RTACX_STREAM_CHUNK records, a copy stream fork-joined to the
@@ -333,6 +338,7 @@ int gather_shape_bearings(int shape);
 // Precision form (rtacx_precision.cu).
 rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float* out, cudaStream_t stream);
 rtacx_status precision_begin(Context& ctx, cudaStream_t stream);
+rtacx_status precision_hot_scan(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream);
 rtacx_status precision_accumulate(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream);
 rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream);
 void free_streaming(Context& ctx);

@@ -58,6 +58,11 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float4 v)
 constexpr int kMaxRangeWords = 8192 / 32 * 4;   // bitmap words for up to 32768 range bins
 constexpr int kLutCells = 4 * kMaxBearingsSmem;
 constexpr int kAccThreads = 256;
+// Hot range interval (RTACX_PRECISION_HOT_RANGE): kHotRows consecutive range
+// rows whose pair cells are replicated kHotReplicas times; samples in them
+// reduce into the replica of their warp, and k_hot_fold adds the replicas
+// back into the grid before the range filter.
+constexpr int kHotRows = 256, kHotReplicas = 8;
 constexpr int kAccLoads = 4;                     // independent record loads per thread in flight
 
 size_t accumulate_smem_bytes(uint32_t nB, uint32_t nR, uint32_t lut_cells)
@@ -69,10 +74,19 @@ __global__ void __launch_bounds__(kAccThreads)
 k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
                   const float* __restrict__ bearings, uint32_t nB, const int* __restrict__ lut,
                   uint32_t lut_cells, float lut_origin, float lut_scale,
-                  float4* __restrict__ P, uint32_t* __restrict__ nonempty)
+                  float4* __restrict__ P, uint32_t* __restrict__ nonempty, const int2* __restrict__ hot,
+                  float4* __restrict__ rep)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     float4* s_cell = reinterpret_cast<float4*>(s_raw);
+    int hot_lo = 0, hot_len = 0;
+    if(hot) { const int2 h = *hot; hot_lo = h.x; hot_len = h.y; }
+    const uint32_t rsel = (blockIdx.x + (threadIdx.x >> 5)) & (kHotReplicas - 1);   // by CTA and warp
+    // Pair-cell row of range bin j: the grid's, or this warp's replica of a hot row.
+    auto cell_row = [&](uint32_t j) -> float4* {
+        const uint32_t hj = j - (uint32_t)hot_lo;
+        return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * nB : P + (size_t)j * nB;
+    };
     const uint32_t words = (p.key.nR + 31) / 32;
     uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_cell + nB);
     int16_t* s_lut = reinterpret_cast<int16_t*>(s_bits + words);
@@ -101,7 +115,7 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
             if(j == kOutOfRange) continue;
             const float2 v = apply_echo(p, make_float2(rec[u].x, rec[u].y), rec[u].z);
             atomicOr(&s_bits[j >> 5], 1u << (j & 31));
-            if(nB == 1) { red_add_v4(P + j, make_float4(v.x, v.y, 0.f, 0.f)); continue; }
+            if(nB == 1) { red_add_v4(cell_row(j), make_float4(v.x, v.y, 0.f, 0.f)); continue; }
             const float th = rec[u].w;
             const float q = fminf(fmaxf((th - lut_origin) * lut_scale, 0.0f), (float)(lut_cells - 1));
             int k = s_lut[(int)q];                       // NaN bearings: q = 0
@@ -111,12 +125,117 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
             float w = (th - c.x) * c.y;
             w = fminf(fmaxf(w, 0.0f), 1.0f);          // NaN bearings -> 0
             const float w0 = 1.0f - w;
-            red_add_v4(P + (size_t)j * nB + k, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y));
+            red_add_v4(cell_row(j) + k, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y));
         }
     }
     __syncthreads();
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x)
         if(s_bits[i]) atomicOr(&nonempty[i], s_bits[i]);
+}
+
+// Hot-range detection (RTACX_PRECISION_HOT_RANGE): range-bin counts of a
+// strided subsample of the ping, then one CTA picks the kHotRows-row window
+// with the largest count. The window is hot when it holds at least a tenth of
+// the counted samples and four times its uniform share; otherwise its length
+// is 0 and every sample reduces into the grid. The counts are zeroed for the
+// next ping.
+__global__ void k_hot_count(const float* __restrict__ samples, uint64_t n, BinParams p, uint64_t step,
+                            uint32_t* __restrict__ cnt)
+{
+    const uint64_t m = (n + step - 1) / step;
+    for(uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < m; s += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 rec = load_record(samples, s * step, p);
+        int side;
+        const uint32_t j = range_key(p.key, rec.z, side);
+        if(j != kOutOfRange) atomicAdd(&cnt[j], 1u);
+    }
+}
+
+constexpr int kHotPickThreads = 1024;
+
+// Exclusive block scan of one value per thread (blockDim.x a multiple of 32).
+__device__ __forceinline__ uint32_t block_exclusive_scan_hot(uint32_t v, uint32_t* s_warp, uint32_t& total)
+{
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for(int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if(lane >= (unsigned)o) x += y;
+    }
+    if(lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    const unsigned nw = blockDim.x >> 5;
+    if(warp == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0u;
+        for(int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if(lane >= (unsigned)o) w += y;
+        }
+        if(lane < nw) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[nw - 1];
+    const uint32_t before = warp ? s_warp[warp - 1] : 0u;
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kHotPickThreads) k_hot_pick(uint32_t* __restrict__ cnt, uint32_t nR,
+                                                               int2* __restrict__ hot)
+{
+    extern __shared__ uint32_t s_pre[];           // [nR + 1] inclusive prefix: s_pre[j + 1] = sum cnt[0..j]
+    __shared__ unsigned long long s_best;
+    const uint32_t per = (nR + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = min(threadIdx.x * per, nR), b1 = min(b0 + per, nR);
+    uint32_t sum = 0;
+    for(uint32_t b = b0; b < b1; b++) sum += cnt[b];
+    __shared__ uint32_t s_warp[32];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan_hot(sum, s_warp, total);
+    if(threadIdx.x == 0) { s_pre[0] = 0; s_best = 0ull; }
+    for(uint32_t b = b0; b < b1; b++) { run += cnt[b]; s_pre[b + 1] = run; cnt[b] = 0u; }
+    __syncthreads();
+    const uint32_t H = min((uint32_t)kHotRows, nR);
+    unsigned long long best = 0ull;   // (window count << 32) | (0xFFFFFFFF - start): ties go to the lowest start
+    for(uint32_t s = threadIdx.x; s + H <= nR; s += blockDim.x) {
+        const uint32_t w = s_pre[s + H] - s_pre[s];
+        const unsigned long long key = ((unsigned long long)w << 32) | (0xFFFFFFFFu - s);
+        best = key > best ? key : best;
+    }
+    atomicMax(&s_best, best);
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        const uint32_t w = (uint32_t)(s_best >> 32), s = 0xFFFFFFFFu - (uint32_t)(s_best & 0xFFFFFFFFu);
+        const bool dense = nR > 2u * H && (double)w >= 0.1 * total && (double)w * nR >= 4.0 * H * (double)total;
+        *hot = dense && total > 0 ? make_int2((int)s, (int)H) : make_int2(0, 0);
+    }
+}
+
+// Adds the replicas of the hot rows into the grid once every sample is in
+// (nothing when the interval is empty).
+__global__ void k_hot_fold(const int2* __restrict__ hot, uint32_t nB, const float4* __restrict__ rep,
+                           float4* __restrict__ P)
+{
+    const int2 h = *hot;
+    const uint64_t cells = (uint64_t)h.y * nB;
+    for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cells; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t row = i / nB, k = i % nB;
+        const float4* rb = rep + row * kHotReplicas * nB + k;
+        float4 acc = P[((uint64_t)h.x + row) * nB + k];
+        for(int r = 0; r < kHotReplicas; r++) {
+            const float4 e = rb[(uint64_t)r * nB];
+            acc.x += e.x; acc.y += e.y; acc.z += e.z; acc.w += e.w;
+        }
+        P[((uint64_t)h.x + row) * nB + k] = acc;
+    }
+}
+
+// Zeroes the replicas of the hot rows (nothing when the interval is empty).
+__global__ void k_hot_zero(const int2* __restrict__ hot, uint32_t nB, float4* __restrict__ rep)
+{
+    const uint64_t cells = (uint64_t)hot->y * kHotReplicas * nB;
+    for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cells; i += (uint64_t)gridDim.x * blockDim.x)
+        rep[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __device__ __forceinline__ bool bit_set(const uint32_t* bits, long long j)
@@ -441,7 +560,9 @@ void free_precision(Context& c)
     free_dev(c.d_G); free_dev(c.d_flags); free_dev(c.d_pwin); free_dev(c.d_A); free_dev(c.d_B);
     free_dev(c.d_C); free_dev(c.d_taps); free_dev(c.d_lut);
     free_dev(c.d_Gf); free_dev(c.d_rowmax); free_dev(c.d_row_scale); free_dev(c.d_col_scale);
+    free_dev(c.d_hot); free_dev(c.d_hotcnt); free_dev(c.d_rep);
     c.prec_f16 = false;
+    c.prec_hot = false;
     c.prec_configured = false;
 }
 
@@ -551,7 +672,11 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     // row n is first scaled by 2^(14 - e_n) (largest |value| in [2^14, 2^15))
     // and col_scale[n] = 2^(e_n - 14) undoes it in the GEMM epilogue.
     const bool f16 = (d->flags & RTACX_PRECISION_FP16_ROWSCALE) != 0;
-    if(d->flags & ~RTACX_PRECISION_FP16_ROWSCALE) { ctx.error = "unknown precision flags"; return RTACX_ERR_INVALID_ARGUMENT; }
+    const bool hot = (d->flags & RTACX_PRECISION_HOT_RANGE) != 0;
+    if(d->flags & ~(RTACX_PRECISION_FP16_ROWSCALE | RTACX_PRECISION_HOT_RANGE)) {
+        ctx.error = "unknown precision flags";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
     std::vector<uint16_t> B((size_t)ctx.Npad * ctx.Kp, 0);
     std::vector<float> col_scale(ctx.Npad, 1.0f);
     for(uint32_t b = 0; b < nB; b++)
@@ -596,7 +721,9 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
        (!direct && !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float))) ||
        (f16 && (!alloc(ctx.d_Gf, (size_t)nR * nB * sizeof(float2)) || !alloc(ctx.d_rowmax, (size_t)nR * 4) ||
                 !alloc(ctx.d_row_scale, (size_t)ctx.Mpad * sizeof(float)) ||
-                !alloc(ctx.d_col_scale, (size_t)ctx.Npad * sizeof(float))))) {
+                !alloc(ctx.d_col_scale, (size_t)ctx.Npad * sizeof(float)))) ||
+       (hot && (!alloc(ctx.d_hot, sizeof(int2)) || !alloc(ctx.d_hotcnt, (size_t)nR * 4) ||
+                !alloc(ctx.d_rep, (size_t)kHotRows * kHotReplicas * nB * sizeof(float4))))) {
         free_precision(ctx);
         ctx.error = "out of device memory for the precision form";
         return RTACX_ERR_OUT_OF_MEMORY;
@@ -607,14 +734,24 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
        cudaMemcpy(ctx.d_lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
        (f16 && (cudaMemcpy(ctx.d_col_scale, col_scale.data(), col_scale.size() * sizeof(float),
                            cudaMemcpyHostToDevice) != cudaSuccess ||
-                cudaMemset(ctx.d_row_scale, 0, (size_t)ctx.Mpad * sizeof(float)) != cudaSuccess))) {
+                cudaMemset(ctx.d_row_scale, 0, (size_t)ctx.Mpad * sizeof(float)) != cudaSuccess)) ||
+       (hot && (cudaMemset(ctx.d_hot, 0, sizeof(int2)) != cudaSuccess ||
+                cudaMemset(ctx.d_hotcnt, 0, (size_t)nR * 4) != cudaSuccess))) {
         cudaGetLastError();
         free_precision(ctx);
         ctx.error = "uploading the precision tables failed";
         return RTACX_ERR_CUDA;
     }
     if(gemm_smem_bytes() > 227 * 1024) { ctx.error = "GEMM tile exceeds shared memory"; return RTACX_ERR_UNSUPPORTED; }
+    if(hot && cudaFuncSetAttribute(k_hot_pick, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)((nR + 1) * sizeof(uint32_t))) != cudaSuccess) {
+        cudaGetLastError();
+        free_precision(ctx);
+        ctx.error = "cannot reserve shared memory for the hot-range scan";
+        return RTACX_ERR_CUDA;
+    }
     ctx.prec_f16 = f16;
+    ctx.prec_hot = hot;
     ctx.prec_configured = true;
     return RTACX_OK;
 }
@@ -636,7 +773,27 @@ rtacx_status precision_accumulate(Context& ctx, const void* samples, uint64_t n,
                                                          (uint64_t)ctx.sm_count * ctx.acc_blocks_per_sm);
     k_prec_accumulate<<<blocks, kAccThreads, ctx.acc_smem, stream>>>(static_cast<const float*>(samples), n, ctx.bin,
                                                                      ctx.d_bearings, ctx.nB, ctx.d_lut, ctx.lut_cells,
-                                                                     ctx.lut_origin, ctx.lut_scale, ctx.d_G, ctx.d_flags);
+                                                                     ctx.lut_origin, ctx.lut_scale, ctx.d_G, ctx.d_flags,
+                                                                     ctx.prec_hot ? ctx.d_hot : nullptr, ctx.d_rep);
+    RTACX_CUDA(cudaGetLastError());
+    return RTACX_OK;
+}
+
+// Hot-range detection on (a strided subsample of) these samples and zeroing
+// of the hot rows' replicas; nothing without RTACX_PRECISION_HOT_RANGE.
+rtacx_status precision_hot_scan(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream)
+{
+    if(!ctx.prec_hot) return RTACX_OK;
+    const uint64_t step = std::max<uint64_t>(1, n / 131072);
+    const uint64_t m = n ? (n + step - 1) / step : 0;
+    if(m) {
+        const uint32_t blocks = (uint32_t)std::min<uint64_t>((m + 255) / 256, (uint64_t)ctx.sm_count * 4);
+        k_hot_count<<<blocks, 256, 0, stream>>>(static_cast<const float*>(samples), n, ctx.bin, step, ctx.d_hotcnt);
+        RTACX_CUDA(cudaGetLastError());
+    }
+    k_hot_pick<<<1, kHotPickThreads, (ctx.nR + 1) * sizeof(uint32_t), stream>>>(ctx.d_hotcnt, ctx.nR, ctx.d_hot);
+    RTACX_CUDA(cudaGetLastError());
+    k_hot_zero<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, ctx.nB, ctx.d_rep);
     RTACX_CUDA(cudaGetLastError());
     return RTACX_OK;
 }
@@ -647,6 +804,7 @@ rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float*
 {
     ctx.mark(0, false, stream);
     rtacx_status st = precision_begin(ctx, stream);
+    if(st == RTACX_OK) st = precision_hot_scan(ctx, samples, n, stream);
     if(st == RTACX_OK) st = precision_accumulate(ctx, samples, n, stream);
     if(st != RTACX_OK) return st;
     ctx.mark(0, true, stream);
@@ -657,6 +815,10 @@ rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float*
 rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
 {
     const uint32_t nR = ctx.nR, nB = ctx.nB;
+    if(ctx.prec_hot) {
+        k_hot_fold<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, nB, ctx.d_rep, ctx.d_G);
+        RTACX_CUDA(cudaGetLastError());
+    }
     ctx.mark(1, false, stream);
     k_prec_windows<<<(nR + 255) / 256, 256, 0, stream>>>(ctx.d_flags, nR, ctx.overlap, ctx.d_pwin);
     RTACX_CUDA(cudaGetLastError());

@@ -80,9 +80,11 @@ rtacx_status reduce_precision_host(Context& c, const void* samples, uint64_t n, 
         RTACX_CUDA(cudaMemcpyAsync(c.d_stage[b], host + first * rec, cnt * rec, cudaMemcpyHostToDevice, c.copy_stream));
         RTACX_CUDA(cudaEventRecord(copied[b], c.copy_stream));
         RTACX_CUDA(cudaStreamWaitEvent(s, copied[b], 0));
+        if(i == 0 && (st = precision_hot_scan(c, c.d_stage[0], cnt, s)) != RTACX_OK) return st;
         if((st = precision_accumulate(c, c.d_stage[b], cnt, s)) != RTACX_OK) return st;
         RTACX_CUDA(cudaEventRecord(used[b], s));
     }
+    if(chunks == 0 && (st = precision_hot_scan(c, nullptr, 0, s)) != RTACX_OK) return st;
     if(chunks == 0) {   // join the forked copy stream
         RTACX_CUDA(cudaEventRecord(copied[0], c.copy_stream));
         RTACX_CUDA(cudaStreamWaitEvent(s, copied[0], 0));

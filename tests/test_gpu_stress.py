@@ -74,3 +74,33 @@ def test_stress_reduced_precision_matches_oracle(oracle):
     D, taps, c = wl.precision_tables(wk.sensor)
     want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
     assert rel_l2(got, want) <= 1e-4
+
+
+@pytest.mark.parametrize("flags_name", ["RTACX_PRECISION_HOT_RANGE", "RTACX_PRECISION_HOT_RANGE|FP16"])
+def test_stress_reduced_precision_hot_range_matches_oracle(oracle, flags_name):
+    """Clustered ping with the hot-range replicas (the densest 256 range rows
+    accumulate into 8 replicas the filter sums): same oracle bar, through the
+    device and the host-buffer entry points."""
+    from rtac_simulation_gb300 import _lib
+    from test_gpu_precision import gpu_precision_host
+    flags = _lib.RTACX_PRECISION_HOT_RANGE
+    if "FP16" in flags_name:
+        flags |= _lib.RTACX_PRECISION_FP16_ROWSCALE
+    wk = wl.stress_2d(n_samples=1 << 20, n_ranges=2048)
+    ctx = precision_context(wk, flags=flags)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    assert rel_l2(got, want) <= 1e-4
+    host = gpu_precision_host(ctx, wk.samples, wk.out_shape)
+    assert rel_l2(host, want) <= 1e-4
+
+
+def test_uniform_ping_with_hot_range_flag_unchanged():
+    """No dense interval on a uniform ping: the flag changes nothing but the
+    order of float additions."""
+    from rtac_simulation_gb300 import _lib
+    wk = wl.precision_2d(n_samples=1 << 18, n_bearings=128, n_ranges=2048)
+    a = gpu_precision(precision_context(wk), wk.samples, wk.out_shape)
+    b = gpu_precision(precision_context(wk, flags=_lib.RTACX_PRECISION_HOT_RANGE), wk.samples, wk.out_shape)
+    assert rel_l2(b, a) <= 1e-5
