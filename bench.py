@@ -67,6 +67,8 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", default=DEFAULT_CONFIG, choices=sorted(workloads.CONFIGS))
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-next-rows", action="store_true",
+                   help="skip the timing of the echo-sample epilogue, directivity tables and rasteriser")
     return p.parse_args()
 
 
@@ -407,6 +409,120 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
                 lanes=len(dev_lanes))
 
 
+def time_next_rows(torch, local, peaks, reps=20, warmup=3):
+    """CUDA-event times of the rows either side of the ping reduction, each
+    through its C ABI entry point on device-resident inputs:
+      make_samples   2^24 ray hits (24 B) -> SimSample2D records (16 B), the
+                     ray generator's carrier phase, spreading and receiver
+                     directivity lookup (rtacx_make_samples);
+      directivity    a rectangle and a disk receiver table (host call + kernel);
+      rasterize      a 1.05M-triangle seafloor + sphere at 2048 x 1536 pixels
+                     (rtacx_rasterize), and the same followed by the plain
+                     ping of an Oculus-like 256-bearing receiver (the GL
+                     simulation's per-ping path)."""
+    from rtac_simulation_gb300 import _lib, scene
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / 1e3 / reps
+
+    hbm = peaks["hbm_gbs"]
+    res = {"timing": f"CUDA events on the launching stream, {warmup} warm-up + {reps} timed calls, mean per call"}
+
+    # Receiver directivity tables.
+    rect = [1.56e-3, 8e-3, 1.25e-3, 1.0, 8.0]
+    disk = [6e-3, 1.25e-3, 1.0, 8.0]
+    tabs = {}
+    for name, kind, par in (("rectangle", _lib.RTACX_DIRECTIVITY_RECTANGLE, rect),
+                            ("disk", _lib.RTACX_DIRECTIVITY_DISK, disk)):
+        t = timed(lambda: _lib.directivity_table(kind, par, stream=stream))
+        tabs[name] = _lib.directivity_table(kind, par, stream=stream)
+        e = tabs[name].numel()
+        res[f"directivity_{name}"] = {"entries": e, "us_per_table": 1e6 * t, "entries_per_s": e / t,
+                                      "params": par, "bound": "launch (host size query + one kernel)"}
+
+    # Echo-sample epilogue on 2^24 hits.
+    wk = workloads.oculus_reference_2d(n_samples=16)
+    ctx = _lib.Context(local)
+    ctx.configure_2d(**wk.sensor)
+    ctx.configure_receiver(np.eye(3), tabs["rectangle"].cpu().numpy(), carrier_hz=1.2e6,
+                           flags=_lib.RTACX_ECHO_PHASE | _lib.RTACX_ECHO_SPREADING)
+    n = 1 << 24
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    hits = torch.empty((n, 6), dtype=torch.float32, device="cuda")
+    hits[:, 0:2].normal_(generator=g)
+    hits[:, 2].uniform_(0.2, 6.0, generator=g)
+    az = torch.empty(n, device="cuda").uniform_(-1.3, 1.3, generator=g)
+    el = torch.empty(n, device="cuda").uniform_(-0.4, 0.4, generator=g)
+    hits[:, 3], hits[:, 4], hits[:, 5] = torch.cos(el) * torch.cos(az), torch.cos(el) * torch.sin(az), torch.sin(el)
+    del az, el
+    smp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    t = timed(lambda: ctx.make_samples(hits, n, smp, stream=stream))
+    ctx.stream_status(stream)
+    gbs = n * 40 / t / 1e9
+    res["make_samples"] = {"hits": n, "ms": 1e3 * t, "hits_per_s": n / t,
+                           "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                                        "algorithmic": "24 B hit read + 16 B sample written per hit",
+                                        "peak_source": peaks["source"]},
+                           "l2": "inputs larger than L2 (671 MB per call)"}
+    del hits, smp
+
+    # Rasteriser.
+    V, N, T = scene.seafloor_and_sphere(grid=724)
+    W, H = 2048, 1536
+    S = (scene.perspective(70.0, W / H, 0.1, 100.0)).astype(np.float32)
+    L = np.eye(4, dtype=np.float32)
+    dV, dN = torch.from_numpy(V).cuda(), torch.from_numpy(N).cuda()
+    dT = torch.from_numpy(T.view(np.int32)).cuda()
+    px = torch.empty((H * W, 4), dtype=torch.float32, device="cuda")
+    raster = lambda: ctx.rasterize(dV, dN, dT, L, S, np.zeros(3, np.float32), W, H, px, stream=stream)
+    t = timed(raster)
+    ctx.stream_status(stream)
+    covered = int((px[:, 2] > 0).sum().item())
+    # Lower bound of the DRAM bytes: visibility buffer cleared, read by the
+    # resolve (8 B each) and one sample written per pixel (16 B); vertices
+    # read (24 B) and transformed (48 B); triangle indices read (12 B).
+    alg = W * H * (8 + 8 + 16) + V.shape[0] * (24 + 48) + T.shape[0] * 12
+    gbs = alg / t / 1e9
+    res["rasterize"] = {"triangles": int(T.shape[0]), "vertices": int(V.shape[0]), "pixels": W * H,
+                        "covered_pixels": covered, "ms": 1e3 * t, "pixels_per_s": W * H / t,
+                        "triangles_per_s": T.shape[0] / t,
+                        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                                     "algorithmic": "32 B per pixel + 72 B per vertex + 12 B per triangle (lower bound)",
+                                     "peak_source": peaks["source"]}}
+    # Mesh -> ping: rasterised samples reduced by a receiver ranged to the
+    # scene (1 .. 45 m, adaptive pulse), as the GL simulation does per ping.
+    rmin, rmax, c = 1.0, 45.0, 1500.0
+    duration = workloads.adaptive_duration(rmin, rmax, 500, c)
+    sensor = dict(wk.sensor)
+    sensor.update(range_min=rmin, range_max=rmax, pulse_duration=float(duration),
+                  margin=float(workloads.F32(workloads.F32(c) * duration)),
+                  pulse=workloads.waveform_sine(1.2e6, float(duration), 8))
+    ctx.configure_2d(**sensor)
+    ping = torch.empty((sensor["range_count"], len(sensor["bearings"]), 2), dtype=torch.float32, device="cuda")
+
+    def mesh_to_ping():
+        raster()
+        ctx.reduce(px, W * H, ping, stream=stream)
+
+    t = timed(mesh_to_ping)
+    ctx.stream_status(stream)
+    res["mesh_to_ping"] = {"ms": 1e3 * t, "pings_per_s": 1.0 / t,
+                           "receiver": f"{sensor['range_count']} ranges x {len(sensor['bearings'])} bearings, 1-45 m, "
+                                       "plain form"}
+    return res
+
+
 def to_complex(t):
     o = t.cpu().numpy()
     return o[..., 0].astype(np.float64) + 1j * o[..., 1]
@@ -550,6 +666,8 @@ def run_ours(args, world, rank, local):
                    "h2d_bytes_per_step": n * rec_in, "d2h_bytes_per_step": int(np.prod(wk.out_shape)) * 8}
     line["gpu_launches"] = (4 if head == "precision" else KERNELS_PER_PING) * args.steps
     line["clocks"] = r["clocks"]
+    if world == 1 and args.config == DEFAULT_CONFIG and not args.no_next_rows:
+        line["next_rows"] = time_next_rows(torch, local, peaks)
 
     if world == 1 and not args.no_cpu_baseline:
         from oracle import oracle

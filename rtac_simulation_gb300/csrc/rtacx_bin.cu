@@ -643,9 +643,8 @@ rtacx_status run_bin_outputs(Context& ctx, const void* samples, uint64_t n,
 rtacx_status prepare_bin_batch(std::string& error, uint32_t max_bins)
 {
     const size_t smem = std::max<size_t>((size_t)max_bins * sizeof(uint32_t), 1);
-    if(cudaFuncSetAttribute(k_count_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-       cudaFuncSetAttribute(k_scatter_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-        cudaGetLastError();
+    if(raise_smem_limit((const void*)k_count_batch, smem) != cudaSuccess ||
+       raise_smem_limit((const void*)k_scatter_batch, smem) != cudaSuccess) {
         error = "cannot reserve shared memory for the batched histograms";
         return RTACX_ERR_CUDA;
     }
@@ -678,8 +677,8 @@ void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t stream
 void configure_hist_launch(Context& ctx)
 {
     const size_t smem = (size_t)ctx.bin.nBins * sizeof(uint32_t);
-    cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
-    cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1));
+    raise_smem_limit((const void*)k_count, std::max<size_t>(smem, 1));
+    raise_smem_limit((const void*)k_scatter, std::max<size_t>(smem, 1));
     // 512-thread CTAs when two histograms fit in one SM's shared memory, one
     // 1024-thread CTA otherwise; each pass gets as many CTAs as are resident
     // at once (registers and shared memory), so that the scatter's per-tile
@@ -709,7 +708,7 @@ void configure_hist_launch(Context& ctx)
         const size_t need = staged_smem_bytes(cand_nt[c], cand_u[c], ctx.bin.nBins);
         const size_t resident = cand_nt[c] == 512 ? 2 * (need + 1024) : need + 1024;
         if(need + 1024 <= (size_t)optin && resident <= (size_t)smem_sm &&
-           cudaFuncSetAttribute(fns[c], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) == cudaSuccess)
+           raise_smem_limit(fns[c], need) == cudaSuccess)
             ctx.staged_U = cand_u[c];
     }
     cudaGetLastError();

@@ -5,7 +5,8 @@
 // (src/RayCaster.cu:49-81, include/rtac_simulation/Receiver.h:51-60,
 // include/rtac_simulation/Sample.h:144-153):
 //   distance < 1e-4          -> null sample (value 0, travel -1)
-//   value *= exp(i 4 pi f d / c) / d^2        (carrier phase reduced in FP64)
+//   value *= exp(i 4 pi f d / c) / d^2        (carrier phase reduced by one
+//                                              FP64 fused multiply-add)
 //   localDir = R^T * dir                      (receiver frame)
 //   value *= directivity(atan2(ly, lx) / pi, atan2(lz, lx) / pi)
 //   bearing = atan2(-ly, lx)
@@ -61,6 +62,7 @@ struct ReceiverParams {
     int dir_w, dir_h;           // 0: uniform directivity
     uint32_t flags;
     double cycles;              // 2 f / c
+    float cycles_hi;            // (float)cycles
     int dims;
 };
 
@@ -75,27 +77,38 @@ __global__ void k_make_samples(const rtacx_echo* __restrict__ hits, uint64_t n, 
         if(d >= 1.0e-4f) {
             float2 v = make_float2(e.re, e.im);
             if(rp.flags & RTACX_ECHO_PHASE) {
-                const double cyc = (double)d * rp.cycles;
-                const double frac = cyc - rint(cyc);
+                // Below 2^22 cycles the float-rounded cycle count is within
+                // one of the nearest integer and the one-FMA reduction lands in
+                // [-0.5, 0.5]; longer (or infinite) travels take the full FP64
+                // reduction. |phase| <= pi: the hardware sine / cosine are
+                // accurate to ~4e-7 there.
+                float frac;
+                if(d * rp.cycles_hi < 4194304.0f) frac = carrier_fraction_f64(d, rp.cycles, rp.cycles_hi);
+                else {
+                    const double cyc = (double)d * rp.cycles;
+                    frac = (float)(cyc - rint(cyc));
+                }
                 float sn, cs;
-                sincosf((float)frac * 6.28318530717958647692f, &sn, &cs);
+                __sincosf(frac * 6.28318530717958647692f, &sn, &cs);
                 v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
             }
             if(rp.flags & RTACX_ECHO_SPREADING) {
-                const float inv = 1.0f / (d * d);
+                const float inv = __fdividef(1.0f, d * d);
                 v = make_float2(v.x * inv, v.y * inv);
             }
             // receiver frame: R^T * dir (column k of R dotted with dir)
             const float lx = fmaf(rp.R[0], e.dir_x, fmaf(rp.R[3], e.dir_y, rp.R[6] * e.dir_z));
             const float ly = fmaf(rp.R[1], e.dir_x, fmaf(rp.R[4], e.dir_y, rp.R[7] * e.dir_z));
             const float lz = fmaf(rp.R[2], e.dir_x, fmaf(rp.R[5], e.dir_y, rp.R[8] * e.dir_z));
+            // atan2 is odd in its first argument: atan2(-ly, lx) = -atan2(ly, lx).
+            const float az = atan2f(ly, lx);
             if(rp.dir_w > 0) {
-                const float g = directivity_lookup(dir_tab, rp.dir_w, rp.dir_h, atan2f(ly, lx) * 0.318309886183790671538f,
+                const float g = directivity_lookup(dir_tab, rp.dir_w, rp.dir_h, az * 0.318309886183790671538f,
                                                    atan2f(lz, lx) * 0.318309886183790671538f);
                 v = make_float2(v.x * g, v.y * g);
             }
             re = v.x; im = v.y; travel = d;
-            bearing = atan2f(-ly, lx);
+            bearing = -az;
         }
         if(rp.dims == 2) reinterpret_cast<float4*>(out)[i] = make_float4(re, im, travel, bearing);
         else { out[3 * i] = re; out[3 * i + 1] = im; out[3 * i + 2] = travel; }
@@ -196,6 +209,7 @@ rtacx_status make_samples(Context& c, const rtacx_echo* hits, uint64_t n, void* 
     rp.dir_w = (int)c.dir_w; rp.dir_h = (int)c.dir_h;
     rp.flags = c.rx_flags;
     rp.cycles = 2.0 * c.rx_hz / (double)c.c;
+    rp.cycles_hi = (float)rp.cycles;
     rp.dims = c.dims;
     const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + 255) / 256, (uint64_t)c.sm_count * 16);
     k_make_samples<<<blocks, 256, 0, stream>>>(hits, n, rp, c.d_dir, static_cast<float*>(samples));

@@ -25,6 +25,21 @@ constexpr uint32_t kErrGemmTimeout     = 1u << 2;  // a bounded mbarrier wait of
 // Largest (range bin x bearing bin) histogram a CTA keeps in shared memory.
 constexpr uint32_t kMaxSmemBins = 49152;
 
+// A kernel's dynamic shared-memory limit is one value per kernel and device,
+// shared by every context and host thread. Raise it to `bytes` if it is
+// lower, never lower it: a smaller limit set for one context would make the
+// larger launches of another context fail with an invalid-argument error.
+// The error of a failed call is consumed (cudaGetLastError) and returned.
+inline cudaError_t raise_smem_limit(const void* fn, size_t bytes)
+{
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, fn);
+    if(e == cudaSuccess && (size_t)a.maxDynamicSharedSizeBytes < bytes)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if(e != cudaSuccess) cudaGetLastError();
+    return e;
+}
+
 // Everything the binning kernels need, passed by value.
 struct BinParams {
     KeyParams key;
@@ -42,14 +57,17 @@ struct BinParams {
 
 // Echo-sample epilogue of the reference's ray generator
 // (src/RayCaster.cu:37-39, 69-71): value *= exp(i 4 pi f d / c) / d^2. The
-// carrier phase is reduced modulo one cycle in FP64 (d * 2f/c, minus its
-// nearest integer: three FP64 operations); the reduced fraction is then
-// exact enough for float sincos.
-// Carrier cycles of a travel reduced to [-0.5, 0.5]: in FP64 (three
-// operations), or with RTACX_ECHO_PHASE_COMPENSATED in float arithmetic
-// that is as exact for this range: t * k_hi split into its rounded product
-// and the exact rounding error (fmaf), the integer part removed from the
-// rounded product (exact below 2^23 cycles), the small terms added last.
+// carrier phase is reduced modulo one cycle (d * 2f/c minus its nearest
+// integer) before the float sincos, in one of two ways:
+//   FP64         one fused multiply-add on the FP64 pipe (the only FP64
+//                instruction per sample; GB300's FP64 rate is a small
+//                fraction of its FP32 rate, so conversions go through the
+//                bit fields below instead);
+//   compensated  RTACX_ECHO_PHASE_COMPENSATED, float arithmetic that is as
+//                exact for this range: t * k_hi split into its rounded
+//                product and the exact rounding error (fmaf), the integer
+//                part removed from the rounded product (exact below 2^23
+//                cycles), the small terms added last.
 // float -> double from the IEEE-754 bit fields (exact; the FP64 pipe is not
 // used). Zero and subnormal inputs give a signed zero; infinities and NaNs
 // do not reach the callers (their keys are out of range).
@@ -81,16 +99,22 @@ __device__ __forceinline__ float f32_from_f64_fields(double x)
 //                (the conversions are integer bit operations).
 //   compensated  no FP64: the float product's exact residual (fmaf) plus the
 //                low part of k.
+// FP64 form: k = 2 f / c, k_hi = (float)k.
+__device__ __forceinline__ float carrier_fraction_f64(float travel, double k, float k_hi)
+{
+    const double r = fma(f64_from_f32_fields(travel), k, -f64_from_f32_fields(rintf(travel * k_hi)));
+    return f32_from_f64_fields(r);
+}
+
 __device__ __forceinline__ float carrier_fraction(const BinParams& p, float travel)
 {
-    const float prod = travel * p.echo_k_hi;
     if(p.echo_flags & RTACX_ECHO_PHASE_COMPENSATED) {
+        const float prod = travel * p.echo_k_hi;
         const float err = fmaf(travel, p.echo_k_hi, -prod);
         const float whole = prod - rintf(prod);
         return whole + fmaf(travel, p.echo_k_lo, err);
     }
-    const double r = fma(f64_from_f32_fields(travel), p.echo_cycles, -f64_from_f32_fields(rintf(prod)));
-    return f32_from_f64_fields(r);
+    return carrier_fraction_f64(travel, p.echo_cycles, p.echo_k_hi);
 }
 
 __device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel)

@@ -643,8 +643,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     ctx.lut_scale = lscale;
     ctx.acc_smem = accumulate_smem_bytes(nB, nR, cells);
     int acc_blocks = 0;
-    if(cudaFuncSetAttribute(k_prec_accumulate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx.acc_smem) !=
-           cudaSuccess ||
+    if(raise_smem_limit((const void*)k_prec_accumulate, ctx.acc_smem) != cudaSuccess ||
        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&acc_blocks, k_prec_accumulate, kAccThreads, ctx.acc_smem) !=
            cudaSuccess ||
        acc_blocks < 1) {
@@ -653,11 +652,8 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         return RTACX_ERR_CUDA;
     }
     ctx.acc_blocks_per_sm = (uint32_t)acc_blocks;
-    if(cudaFuncSetAttribute(k_prec_filter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)filter_smem_bytes(kFiltTapsMax)) != cudaSuccess ||
-       cudaFuncSetAttribute(k_prec_filter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
-        cudaGetLastError();
+    if(raise_smem_limit((const void*)k_prec_filter<false>, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess ||
+       raise_smem_limit((const void*)k_prec_filter<true>, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
         ctx.error = "cannot reserve shared memory for the range filter";
         return RTACX_ERR_CUDA;
     }
@@ -743,9 +739,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         return RTACX_ERR_CUDA;
     }
     if(gemm_smem_bytes() > 227 * 1024) { ctx.error = "GEMM tile exceeds shared memory"; return RTACX_ERR_UNSUPPORTED; }
-    if(hot && cudaFuncSetAttribute(k_hot_pick, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)((nR + 1) * sizeof(uint32_t))) != cudaSuccess) {
-        cudaGetLastError();
+    if(hot && raise_smem_limit((const void*)k_hot_pick, (nR + 1) * sizeof(uint32_t)) != cudaSuccess) {
         free_precision(ctx);
         ctx.error = "cannot reserve shared memory for the hot-range scan";
         return RTACX_ERR_CUDA;

@@ -423,15 +423,10 @@ template <int TR, int TB>
 rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
 {
     const size_t smem = sizeof(GatherSmem<TR, TB>) + (ctx.H + 2) * sizeof(float2) + (ctx.W + 2) * sizeof(float);
-    static thread_local size_t configured = 0;
-    if(smem > configured) {
-        if(cudaFuncSetAttribute(k_gather_2d<TR, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-            cudaGetLastError();
-            ctx.error = "PSF tables too large for shared memory (pulse " + std::to_string(ctx.H) +
-                        " taps, beam " + std::to_string(ctx.W) + " taps)";
-            return RTACX_ERR_UNSUPPORTED;
-        }
-        configured = smem;
+    if(raise_smem_limit((const void*)k_gather_2d<TR, TB>, smem) != cudaSuccess) {
+        ctx.error = "PSF tables too large for shared memory (pulse " + std::to_string(ctx.H) +
+                    " taps, beam " + std::to_string(ctx.W) + " taps)";
+        return RTACX_ERR_UNSUPPORTED;
     }
     dim3 grid((ctx.nB + TB - 1) / TB, (ctx.nR + TR - 1) / TR);
     if(!ctx.d_tile_parts) {
@@ -443,14 +438,9 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
         if(e != cudaSuccess) { ctx.error = std::string("k_gather_2d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
         return RTACX_OK;
     }
-    static thread_local size_t split_configured = 0;
-    if(smem > split_configured) {
-        if(cudaFuncSetAttribute(k_gather_split<TR, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-            cudaGetLastError();
-            ctx.error = "PSF tables too large for shared memory";
-            return RTACX_ERR_UNSUPPORTED;
-        }
-        split_configured = smem;
+    if(raise_smem_limit((const void*)k_gather_split<TR, TB>, smem) != cudaSuccess) {
+        ctx.error = "PSF tables too large for shared memory";
+        return RTACX_ERR_UNSUPPORTED;
     }
     const uint32_t tiles = grid.x * grid.y;
     k_tile_parts<TR><<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles, ctx.nR,
@@ -487,8 +477,7 @@ size_t gather_batch_smem(int shape, uint32_t H, uint32_t W)
 template <int TR, int TB>
 rtacx_status prepare_batch_shape(std::string& error, size_t smem)
 {
-    if(cudaFuncSetAttribute(k_gather_batch<TR, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-        cudaGetLastError();
+    if(raise_smem_limit((const void*)k_gather_batch<TR, TB>, smem) != cudaSuccess) {
         error = "PSF tables too large for the batched gather";
         return RTACX_ERR_UNSUPPORTED;
     }
@@ -532,8 +521,7 @@ rtacx_status run_reduce(Context& ctx, float* out_f, cudaStream_t stream)
     float2* out = reinterpret_cast<float2*>(out_f);
     if(ctx.dims == 1) {
         const size_t smem = (ctx.H + 2) * sizeof(float2);
-        if(smem > 48 * 1024)
-            cudaFuncSetAttribute(k_gather_1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if(smem > 48 * 1024) raise_smem_limit((const void*)k_gather_1d, smem);
         k_gather_1d<<<(ctx.nR + kWarps - 1) / kWarps, kThreads, smem, stream>>>(
             ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_ranges, ctx.d_pulse, ctx.red, out);
         const cudaError_t e = cudaGetLastError();

@@ -17,6 +17,17 @@ def perspective(fovy_deg: float, aspect: float, near: float, far: float) -> np.n
                      [0, 0, -1, 0]], dtype=np.float64)
 
 
+def _grid_triangles(rows: int, quads: int, cols: int, split) -> np.ndarray:
+    """Two triangles per quad of a rows x quads grid of vertices laid out with
+    `cols` vertices per row, quad by quad in row order; split(a, b, c, d)
+    gives the two triangles of the quad with corners a (r, q), b (r, q+1),
+    c (r+1, q), d (r+1, q+1)."""
+    r, q = np.meshgrid(np.arange(rows, dtype=np.int64), np.arange(quads, dtype=np.int64), indexing="ij")
+    a = (r * cols + q).ravel()
+    t0, t1 = split(a, a + 1, a + cols, a + cols + 1)
+    return np.stack([np.stack(t0, axis=1), np.stack(t1, axis=1)], axis=1).reshape(-1, 3)
+
+
 def seafloor_and_sphere(grid: int = 40, depth: float = 3.0, extent: float = 20.0, length: float = 40.0,
                         sphere_center=(2.0, -1.0, -10.0), radius: float = 1.5, sphere_steps: int = 24):
     """(vertices [n][3], normals [n][3], triangles [m][3]) in a camera frame
@@ -27,26 +38,14 @@ def seafloor_and_sphere(grid: int = 40, depth: float = 3.0, extent: float = 20.0
     X, Z = np.meshgrid(xs, zs)
     pv = np.stack([X.ravel(), np.full(X.size, -depth), Z.ravel()], axis=1)
     pn = np.tile([0.0, 1.0, 0.0], (pv.shape[0], 1))
-    tris = []
-    for r in range(grid):
-        for q in range(grid):
-            a = r * (grid + 1) + q
-            b, c_, d = a + 1, a + grid + 1, a + grid + 2
-            tris += [(a, c_, b), (b, c_, d)]
-    pt = np.array(tris, dtype=np.int64)
+    pt = _grid_triangles(grid, grid, grid + 1, lambda a, b, c_, d: ((a, c_, b), (b, c_, d)))
     th = np.linspace(0, math.pi, sphere_steps + 1)
     ph = np.linspace(0, 2 * math.pi, 2 * sphere_steps + 1)
     T, P = np.meshgrid(th, ph, indexing="ij")
     n = np.stack([np.sin(T) * np.cos(P), np.cos(T), np.sin(T) * np.sin(P)], axis=-1).reshape(-1, 3)
     sv = np.asarray(sphere_center) + radius * n
-    st = []
-    cols = 2 * sphere_steps + 1
-    for r in range(sphere_steps):
-        for q in range(2 * sphere_steps):
-            a = r * cols + q
-            b, c_, d = a + 1, a + cols, a + cols + 1
-            st += [(a, b, c_), (b, d, c_)]
-    st = np.array(st, dtype=np.int64) + pv.shape[0]
+    st = _grid_triangles(sphere_steps, 2 * sphere_steps, 2 * sphere_steps + 1,
+                         lambda a, b, c_, d: ((a, b, c_), (b, d, c_))) + pv.shape[0]
     V = np.concatenate([pv, sv]).astype(np.float32)
     N = np.concatenate([pn, n]).astype(np.float32)
     return V, N, np.concatenate([pt, st]).astype(np.uint32)

@@ -57,6 +57,20 @@ def test_precision_matches_binned_fp64_oracle(oracle, maker):
     assert err <= TOL, err
 
 
+
+def test_precision_contexts_of_different_shapes_interleave(oracle):
+    # A second, smaller precision context configured after the first must not
+    # shrink the first one's per-kernel shared-memory limits.
+    big = wl.precision_2d(n_samples=1 << 16, n_ranges=1024)
+    small = wl.precision_2d(n_samples=1 << 12, n_bearings=100, n_ranges=300)
+    cb = precision_context(big)
+    cs = precision_context(small)
+    for wk, ctx in ((small, cs), (big, cb)):
+        got = gpu_precision(ctx, wk.samples, wk.out_shape)
+        D, taps, c = wl.precision_tables(wk.sensor)
+        want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+        assert rel_l2(got, want) <= TOL
+
 def test_precision_full_size_rows(oracle):
     wk = wl.precision_2d()
     ctx = precision_context(wk)

@@ -52,6 +52,20 @@ def test_reduce_zero_cases(oracle):
     assert np.all(gpu_reduce(ctx, wk.samples[:0], wk.out_shape) == 0)
 
 
+
+def test_contexts_of_different_shapes_interleave(oracle):
+    # Kernel launch limits (dynamic shared memory) are per kernel and device,
+    # shared by every context: configuring a smaller sensor after a larger one
+    # must leave the larger context's launches valid.
+    big = wl.oculus_2d(n_samples=1 << 16)
+    small = wl.oculus_2d(n_samples=1 << 12, n_bearings=64, n_ranges=128)
+    cb = make_context(big)
+    cs = make_context(small)
+    got_s = gpu_reduce(cs, small.samples, small.out_shape)
+    got_b = gpu_reduce(cb, big.samples, big.out_shape)
+    assert rel_l2(got_b, oracle.reduce(big.samples, big.sensor)) <= TOL
+    assert rel_l2(got_s, oracle.reduce(small.samples, small.sensor)) <= TOL
+
 def test_reduce_unaligned_matches_aligned():
     wk = wl.oculus_reference_2d(n_samples=5000)
     ctx = make_context(wk)
