@@ -135,7 +135,7 @@ RTACX_ECHO_SPREADING = 2
 RTACX_ECHO_PHASE_COMPENSATED = 4
 RTACX_PRECISION_FP16_ROWSCALE = 1
 RTACX_PRECISION_HOT_RANGE = 2
-PRECISION_STAGES = ("accumulate", "windows", "filter", "gemm", "copy")
+PRECISION_STAGES = ("accumulate", "windows", "filter", "gemm", "copy", "clear")
 
 
 class EchoModel(ctypes.Structure):

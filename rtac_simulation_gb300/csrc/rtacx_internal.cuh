@@ -21,6 +21,7 @@ constexpr uint32_t kOutOfRange = RTACX_KEY_OUT_OF_RANGE;
 constexpr uint32_t kErrScatterOverflow = 1u << 0;  // sorted position beyond the counted total
 constexpr uint32_t kErrBadWindow       = 1u << 1;  // window bounds outside the sorted array
 constexpr uint32_t kErrGemmTimeout     = 1u << 2;  // a bounded mbarrier wait of the tensor-core GEMM expired
+constexpr uint32_t kErrAccumulateTimeout = 1u << 3; // a bounded wait for a staged copy of samples expired
 
 // Largest (range bin x bearing bin) histogram a CTA keeps in shared memory.
 constexpr uint32_t kMaxSmemBins = 49152;
@@ -38,6 +39,46 @@ inline cudaError_t raise_smem_limit(const void* fn, size_t bytes)
         e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if(e != cudaSuccess) cudaGetLastError();
     return e;
+}
+
+// mbarrier helpers of the TMA pipelines (tensor-core GEMM, staged
+// accumulation). Shared-memory addresses are 32-bit shared-window offsets.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase of the given parity, for at most `limit` SM clock
+// cycles. Returns false (and sets *abort_flag) when the time runs out, or
+// when another thread of the CTA has already set *abort_flag.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                                  long long limit)
+{
+    const long long t0 = clock64();
+    while(!mbar_try_wait(bar, parity)) {
+        if(*abort_flag) return false;
+        if(clock64() - t0 > limit) { *abort_flag = 1; return false; }
+    }
+    return true;
 }
 
 // Everything the binning kernels need, passed by value.
@@ -75,9 +116,8 @@ __device__ __forceinline__ double f64_from_f32_fields(float x)
 {
     const uint32_t u = __float_as_uint(x);
     const uint32_t e = (u >> 23) & 0xffu;
-    if(e == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
     const uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)((u & 7u) << 29));
+    return e == 0u ? __hiloint2double((int)(u & 0x80000000u), 0) : __hiloint2double((int)hi, (int)((u & 7u) << 29));
 }
 
 // double -> float from the bit fields, mantissa truncated toward zero
@@ -87,8 +127,8 @@ __device__ __forceinline__ float f32_from_f64_fields(double x)
 {
     const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
     const uint32_t e = (hi >> 20) & 0x7ffu;
-    if(e <= 896u) return __uint_as_float(hi & 0x80000000u);
-    return __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+    const uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return __uint_as_float(e <= 896u ? (hi & 0x80000000u) : f);
 }
 
 // Carrier phase in cycles, reduced to about [-0.5, 0.5]: travel * 2 f / c
@@ -106,9 +146,11 @@ __device__ __forceinline__ float carrier_fraction_f64(float travel, double k, fl
     return f32_from_f64_fields(r);
 }
 
-__device__ __forceinline__ float carrier_fraction(const BinParams& p, float travel)
+// `flags` is p.echo_flags, or a compile-time constant in kernels specialised
+// for one echo model (the tests on it then fold away).
+__device__ __forceinline__ float carrier_fraction(const BinParams& p, float travel, uint32_t flags)
 {
-    if(p.echo_flags & RTACX_ECHO_PHASE_COMPENSATED) {
+    if(flags & RTACX_ECHO_PHASE_COMPENSATED) {
         const float prod = travel * p.echo_k_hi;
         const float err = fmaf(travel, p.echo_k_hi, -prod);
         const float whole = prod - rintf(prod);
@@ -117,19 +159,24 @@ __device__ __forceinline__ float carrier_fraction(const BinParams& p, float trav
     return carrier_fraction_f64(travel, p.echo_cycles, p.echo_k_hi);
 }
 
-__device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel)
+__device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel, uint32_t flags)
 {
-    if(p.echo_flags & RTACX_ECHO_PHASE) {
+    if(flags & RTACX_ECHO_PHASE) {
         // |phase| <= pi: the hardware sine / cosine are accurate to ~4e-7 here.
         float sn, cs;
-        __sincosf(carrier_fraction(p, travel) * 6.28318530717958647692f, &sn, &cs);
+        __sincosf(carrier_fraction(p, travel, flags) * 6.28318530717958647692f, &sn, &cs);
         v = make_float2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
     }
-    if(p.echo_flags & RTACX_ECHO_SPREADING) {
+    if(flags & RTACX_ECHO_SPREADING) {
         const float inv = __fdividef(1.0f, travel * travel);
         v = make_float2(v.x * inv, v.y * inv);
     }
     return v;
+}
+
+__device__ __forceinline__ float2 apply_echo(const BinParams& p, float2 v, float travel)
+{
+    return apply_echo(p, v, travel, p.echo_flags);
 }
 
 // Range key of one travel value: Binner::Key::operator()
@@ -150,6 +197,17 @@ __device__ __forceinline__ uint32_t range_key(const KeyParams& k, float travel, 
         return kOutOfRange;
     }
     return (uint32_t)res;
+}
+
+// range_key without branches (selects only), for kernels that interleave
+// several samples per thread; the same key, without the side.
+__device__ __forceinline__ uint32_t range_key_select(const KeyParams& k, float travel)
+{
+    const int res = __float2int_rz(fmaf(k.a, travel, k.b));
+    const float fr = (float)res;
+    const uint32_t below = fr >= k.lower ? 0u : kOutOfRange;
+    const uint32_t above = fr <= k.upper ? k.nR - 1u : kOutOfRange;
+    return res < 0 ? below : ((uint32_t)res >= k.nR ? above : (uint32_t)res);
 }
 
 // Bearing sub-bin (extension of the reference key, see the oracle for the
@@ -288,8 +346,11 @@ struct Context {
     uint32_t Mpad = 0, Npad = 0, Kp = 0;
     float4* d_G = nullptr;              // [nR][nB] binned pair cells {to bearing k, to bearing k+1}
     uint32_t* d_flags = nullptr;        // [(nR + 31) / 32] bitmap of non-empty range bins
-    int* d_lut = nullptr;               // bearing lookup grid
+    float2* d_lut = nullptr;            // bearing lookup grid {count below, bearing in the cell}
     uint32_t lut_cells = 0;
+    int lut_exact = 0;                  // no grid cell holds two interior bearings
+    uint32_t acc_staged_blocks[6] = {}; // resident CTAs per SM of each staged accumulation (0: not used)
+    size_t acc_staged_smem = 0;
     float lut_origin = 0.0f, lut_scale = 0.0f;
     int2* d_pwin = nullptr;             // [nR] window bin interval per row (lo > hi: empty)
     uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the filtered grid

@@ -43,20 +43,34 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float4 v)
                  : "memory");
 }
 
+// The same reduction without the "memory" clobber: the pair cells are not
+// read by the kernels that issue it, so loads may be scheduled across it.
+__device__ __forceinline__ void red_add_v4_unordered(float4* addr, float4 v)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
+}
+
 // Pair cells: P[j][k] = {contribution to bearing k, contribution to bearing
 // k + 1} of the samples of range bin j whose bearing lies in [theta_k,
 // theta_k+1). One 16-byte vector atomic per sample; the filter kernel forms
 // G[j][k] = P[j][k].xy + P[j][k - 1].zw. Non-empty range bins are collected
 // in a shared-memory bitmap per CTA and OR-ed into the global bitmap once.
-// The bearing cell comes from a uniform lookup grid (lut[c] = the table
-// index at or below the grid line c), corrected by exact comparisons with the
-// table, so it equals the largest k in [0, nB - 2] with theta_k <= theta.
-// Shared memory (dynamic, sized by nB and nR): per table bearing one 16-byte
-// cell {theta_k, 1 / (theta_k+1 - theta_k), theta_k+1, 0}, so the common case
-// (lookup already exact) costs one 16-byte shared load; the bitmap; the
-// lookup grid as int16.
+// The bearing cell k is the largest k in [0, nB - 2] with theta_k <= theta,
+// i.e. the number of interior table bearings theta_1 .. theta_nB-2 at or
+// below theta. It comes from a uniform lookup grid over the table: grid cell
+// c(theta) = (int)clamp((theta - origin) * scale, 0, cells - 1) in float, the
+// same expression on the host and the device. c is non-decreasing in theta,
+// so an interior bearing whose own grid cell lies below c(theta) is below
+// theta and one whose cell lies above is above it. Grid entry c holds {the
+// count of interior bearings in cells below c, the interior bearing in cell
+// c or +inf}; when no cell holds two interior bearings (checked on the host:
+// the lookup is then exact), k = count + (theta >= bearing) with no search.
+// Otherwise the count is corrected by comparisons with the table.
+// Shared memory (dynamic, sized by nB and nR): per table bearing an 8-byte
+// cell {theta_k, 1 / (theta_k+1 - theta_k)}; the bitmap; the grid as 8-byte
+// entries. Two 8-byte shared loads per sample in the exact case.
 constexpr int kMaxRangeWords = 8192 / 32 * 4;   // bitmap words for up to 32768 range bins
-constexpr int kLutCells = 4 * kMaxBearingsSmem;
+constexpr int kLutCells = 4096;
 constexpr int kAccThreads = 256;
 // Hot range interval (RTACX_PRECISION_HOT_RANGE): kHotRows consecutive range
 // rows whose pair cells are replicated kHotReplicas times; samples in them
@@ -64,21 +78,30 @@ constexpr int kAccThreads = 256;
 // back into the grid before the range filter.
 constexpr int kHotRows = 256, kHotReplicas = 8;
 constexpr int kAccLoads = 4;                     // independent record loads per thread in flight
+constexpr int kAccEchoModels = 6;                // echo models of k_prec_accumulate_exact
+
+// Lookup-grid cell of a bearing; one expression for the host (building the
+// grid) and the device (reading it), so both agree on every float input.
+// NaN bearings fall in cell 0.
+__host__ __device__ __forceinline__ int bearing_grid_cell(float th, float origin, float scale, uint32_t cells)
+{
+    return (int)fminf(fmaxf((th - origin) * scale, 0.0f), (float)(cells - 1));
+}
 
 size_t accumulate_smem_bytes(uint32_t nB, uint32_t nR, uint32_t lut_cells)
 {
-    return (size_t)nB * sizeof(float4) + (size_t)((nR + 31) / 32) * sizeof(uint32_t) + (size_t)lut_cells * sizeof(int16_t);
+    return (size_t)nB * sizeof(float2) + (size_t)lut_cells * sizeof(float2) + (size_t)((nR + 31) / 32) * sizeof(uint32_t);
 }
 
 __global__ void __launch_bounds__(kAccThreads)
 k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
-                  const float* __restrict__ bearings, uint32_t nB, const int* __restrict__ lut,
-                  uint32_t lut_cells, float lut_origin, float lut_scale,
+                  const float* __restrict__ bearings, uint32_t nB, const float2* __restrict__ lut,
+                  uint32_t lut_cells, float lut_origin, float lut_scale, int lut_exact,
                   float4* __restrict__ P, uint32_t* __restrict__ nonempty, const int2* __restrict__ hot,
                   float4* __restrict__ rep)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
-    float4* s_cell = reinterpret_cast<float4*>(s_raw);
+    float2* s_cell = reinterpret_cast<float2*>(s_raw);
     int hot_lo = 0, hot_len = 0;
     if(hot) { const int2 h = *hot; hot_lo = h.x; hot_len = h.y; }
     const uint32_t rsel = (blockIdx.x + (threadIdx.x >> 5)) & (kHotReplicas - 1);   // by CTA and warp
@@ -88,14 +111,13 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
         return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * nB : P + (size_t)j * nB;
     };
     const uint32_t words = (p.key.nR + 31) / 32;
-    uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_cell + nB);
-    int16_t* s_lut = reinterpret_cast<int16_t*>(s_bits + words);
+    float2* s_lut = s_cell + nB;
+    uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_lut + lut_cells);
     for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) {
         const float th = bearings[i];
-        const bool last = i + 1 >= nB;
-        s_cell[i] = make_float4(th, last ? 0.0f : 1.0f / (bearings[i + 1] - th), last ? INFINITY : bearings[i + 1], 0.0f);
+        s_cell[i] = make_float2(th, i + 1 >= nB ? 0.0f : 1.0f / (bearings[i + 1] - th));
     }
-    for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = (int16_t)lut[i];
+    for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = lut[i];
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
     __syncthreads();
     const int kmax = (int)nB - 2;
@@ -117,11 +139,14 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
             atomicOr(&s_bits[j >> 5], 1u << (j & 31));
             if(nB == 1) { red_add_v4(cell_row(j), make_float4(v.x, v.y, 0.f, 0.f)); continue; }
             const float th = rec[u].w;
-            const float q = fminf(fmaxf((th - lut_origin) * lut_scale, 0.0f), (float)(lut_cells - 1));
-            int k = s_lut[(int)q];                       // NaN bearings: q = 0
-            float4 c = s_cell[k];
-            while(k < kmax && c.z <= th) c = s_cell[++k];
-            while(k > 0 && !(c.x <= th)) c = s_cell[--k];
+            const float2 e = s_lut[bearing_grid_cell(th, lut_origin, lut_scale, lut_cells)];
+            int k = __float_as_int(e.x);
+            if(lut_exact) k += (th >= e.y) ? 1 : 0;
+            else {
+                while(k < kmax && s_cell[k + 1].x <= th) ++k;
+                while(k > 0 && !(s_cell[k].x <= th)) --k;
+            }
+            const float2 c = s_cell[k];
             float w = (th - c.x) * c.y;
             w = fminf(fmaxf(w, 0.0f), 1.0f);          // NaN bearings -> 0
             const float w0 = 1.0f - w;
@@ -131,6 +156,164 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
     __syncthreads();
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x)
         if(s_bits[i]) atomicOr(&nonempty[i], s_bits[i]);
+}
+
+// k_prec_accumulate for the common case: 16-byte aligned records, an exact
+// bearing lookup grid, more than one bearing, no hot range, and the echo
+// model kEcho fixed at compile time. The records reach shared memory by bulk
+// copies (cp.async.bulk, the TMA engine) into a ring of kStages stages of
+// kStageRecs records, so the bytes in flight per SM depend neither on
+// registers nor on how long the threads compute. Each thread computes the
+// key, value, cell and weights of its records of a stage without branches
+// (out-of-range and tail records only clear their predicate), then issues
+// the bitmap bits and the vector reductions; the results are those of
+// k_prec_accumulate. One persistent CTA
+// takes stages c = blockIdx.x, blockIdx.x + gridDim.x, ...; thread 0 issues
+// the copy of the stage kStages ahead as soon as every thread has read the
+// stage it refills. Each wait is bounded (kAccWaitCycles); a timeout sets
+// kErrAccumulateTimeout in the error word, the CTA stops, and thread 0 waits
+// (bounded again) for its copies still in flight before the CTA exits.
+constexpr int kStageRecs = 1024;                 // 16 KB of records per stage
+constexpr int kStages = 4;
+constexpr int kStagedThreads = 512;
+constexpr int kStagedPerThread = kStageRecs / kStagedThreads;
+constexpr long long kAccWaitCycles = 2000000000ll;   // about one second
+
+size_t staged_smem_bytes(uint32_t nB, uint32_t nR, uint32_t lut_cells)
+{
+    return (size_t)kStages * kStageRecs * sizeof(float4) + accumulate_smem_bytes(nB, nR, lut_cells);
+}
+
+template <uint32_t kEcho>
+__global__ void __launch_bounds__(kStagedThreads)
+k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinParams p,
+                         const float* __restrict__ bearings, uint32_t nB, const float2* __restrict__ lut,
+                         uint32_t lut_cells, float lut_origin, float lut_scale,
+                         float4* __restrict__ P, uint32_t* __restrict__ nonempty, uint32_t* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ __align__(8) uint64_t s_full[kStages];
+    __shared__ int s_abort;
+    float4* s_ring = reinterpret_cast<float4*>(s_raw);
+    float2* s_cell = reinterpret_cast<float2*>(s_ring + kStages * kStageRecs);
+    float2* s_lut = s_cell + nB;
+    uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_lut + lut_cells);
+    const uint32_t words = (p.key.nR + 31) / 32;
+    const uint64_t stages = (n + kStageRecs - 1) / kStageRecs;
+    auto issue = [&](uint64_t c, int slot) {
+        const uint64_t first = c * kStageRecs;
+        const uint64_t left = n - first;
+        const uint32_t bytes = (uint32_t)(left < (uint64_t)kStageRecs ? left : (uint64_t)kStageRecs) * (uint32_t)sizeof(float4);
+        const uint32_t bar = smem_u32(&s_full[slot]);
+        mbar_expect_tx(bar, bytes);
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(s_ring + slot * kStageRecs)), "l"(samples + first), "r"(bytes), "r"(bar)
+                     : "memory");
+    };
+    if(threadIdx.x == 0) {
+        for(int i = 0; i < kStages; i++) mbar_init(smem_u32(&s_full[i]), 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for(int i = 0; i < kStages; i++) {
+            const uint64_t c = blockIdx.x + (uint64_t)i * gridDim.x;
+            if(c < stages) issue(c, i);
+        }
+    }
+    for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) {
+        const float th = bearings[i];
+        s_cell[i] = make_float2(th, i + 1 >= nB ? 0.0f : 1.0f / (bearings[i + 1] - th));
+    }
+    for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = lut[i];
+    for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
+    __syncthreads();
+    int it = 0;
+    bool aborted = false;
+    for(uint64_t c = blockIdx.x; c < stages; c += gridDim.x, it++) {
+        const int slot = it % kStages;
+        const bool ready = mbar_wait_bounded(smem_u32(&s_full[slot]), (uint32_t)(it / kStages) & 1u, &s_abort,
+                                             kAccWaitCycles);
+        const uint64_t left = n - c * kStageRecs;
+        const uint32_t count = left < (uint64_t)kStageRecs ? (uint32_t)left : (uint32_t)kStageRecs;
+        uint32_t row[kStagedPerThread];
+        int cell[kStagedPerThread];
+        float4 add[kStagedPerThread];
+#pragma unroll
+        for(int u = 0; u < kStagedPerThread; u++) {
+            const uint32_t idx = threadIdx.x + (uint32_t)u * kStagedThreads;
+            const float4 rec = s_ring[slot * kStageRecs + min(idx, (uint32_t)kStageRecs - 1u)];
+            const uint32_t j = range_key_select(p.key, rec.z);
+            row[u] = (ready && idx < count) ? j : kOutOfRange;
+            const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z, kEcho);
+            const float th = rec.w;
+            const float2 e = s_lut[bearing_grid_cell(th, lut_origin, lut_scale, lut_cells)];
+            const int k = __float_as_int(e.x) + (th >= e.y ? 1 : 0);
+            const float2 cl = s_cell[k];
+            const float w = fminf(fmaxf((th - cl.x) * cl.y, 0.0f), 1.0f);   // NaN bearings -> 0
+            const float w0 = 1.0f - w;
+            cell[u] = k;
+            add[u] = make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y);
+        }
+        // Every thread has read the slot: refill it kStages stages ahead.
+        aborted = __syncthreads_or(!ready) != 0;
+        if(threadIdx.x == 0 && !aborted) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const uint64_t next = c + (uint64_t)kStages * gridDim.x;
+            if(next < stages) issue(next, slot);
+        }
+#pragma unroll
+        for(int u = 0; u < kStagedPerThread; u++) {
+            const uint32_t j = row[u];
+            if(j != kOutOfRange) {
+                atomicOr(&s_bits[j >> 5], 1u << (j & 31));
+                red_add_v4_unordered(P + (size_t)j * nB + cell[u], add[u]);
+            }
+        }
+        if(aborted) break;
+    }
+    if(aborted && threadIdx.x == 0) {
+        atomicOr(err, kErrAccumulateTimeout);
+        // Let the copies still in flight land before the CTA's shared memory
+        // is released: those of iterations it .. it + kStages - 1 (the refill
+        // of the aborted iteration was not issued).
+        volatile int keep_waiting = 0;
+        for(int i = it; i < it + kStages; i++) {
+            if(blockIdx.x + (uint64_t)i * gridDim.x >= stages) break;
+            if(!mbar_wait_bounded(smem_u32(&s_full[i % kStages]), (uint32_t)(i / kStages) & 1u, &keep_waiting,
+                                  kAccWaitCycles))
+                break;
+        }
+    }
+    __syncthreads();
+    for(uint32_t i = threadIdx.x; i < words; i += blockDim.x)
+        if(s_bits[i]) atomicOr(&nonempty[i], s_bits[i]);
+}
+
+// Echo models of the specialised accumulation (RTACX_ECHO_PHASE_COMPENSATED
+// only matters with RTACX_ECHO_PHASE).
+constexpr uint32_t kEchoP = RTACX_ECHO_PHASE, kEchoS = RTACX_ECHO_SPREADING, kEchoC = RTACX_ECHO_PHASE_COMPENSATED;
+constexpr uint32_t kEchoModels[kAccEchoModels] = {0u, kEchoP, kEchoS, kEchoP | kEchoS, kEchoP | kEchoC,
+                                                 kEchoP | kEchoS | kEchoC};
+
+const void* accumulate_staged_kernel(int model)
+{
+    switch(model) {
+    case 0: return (const void*)k_prec_accumulate_staged<0u>;
+    case 1: return (const void*)k_prec_accumulate_staged<kEchoP>;
+    case 2: return (const void*)k_prec_accumulate_staged<kEchoS>;
+    case 3: return (const void*)k_prec_accumulate_staged<kEchoP | kEchoS>;
+    case 4: return (const void*)k_prec_accumulate_staged<kEchoP | kEchoC>;
+    default: return (const void*)k_prec_accumulate_staged<kEchoP | kEchoS | kEchoC>;
+    }
+}
+
+// Index into kEchoModels of an echo flag word.
+int accumulate_echo_model(uint32_t flags)
+{
+    flags &= kEchoP | kEchoS | kEchoC;
+    if(!(flags & kEchoP)) flags &= ~kEchoC;
+    for(int m = 0; m < kAccEchoModels; m++)
+        if(kEchoModels[m] == flags) return m;
+    return 0;
 }
 
 // Hot-range detection (RTACX_PRECISION_HOT_RANGE): range-bin counts of a
@@ -625,19 +808,30 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     ctx.tap_center = center;
     if(nR > (uint32_t)kMaxRangeWords * 32) { ctx.error = "too many range bins for the precision form"; return RTACX_ERR_UNSUPPORTED; }
 
-    // Bearing lookup grid: lut[c] = largest k in [0, nB - 2] whose bearing is
-    // at or below the grid line origin + c / scale (0 below the table).
+    // Bearing lookup grid (see k_prec_accumulate): entry c = {number of
+    // interior bearings theta_1 .. theta_nB-2 in grid cells below c, the
+    // interior bearing in cell c or +inf}; exact when no cell holds two.
     const uint32_t cells = std::min<uint32_t>(4 * nB, (uint32_t)kLutCells);
     const float origin = ctx.bearings[0];
     const float width = (nB > 1) ? ctx.bearings[nB - 1] - ctx.bearings[0] : 1.0f;
     const float lscale = (float)cells / width;
-    std::vector<int> lut(cells, 0);
-    for(uint32_t cidx = 0; cidx < cells; cidx++) {
-        const double line = (double)origin + (double)cidx / (double)lscale;
-        int k = 0;
-        while(k + 1 <= (int)nB - 2 && (double)ctx.bearings[k + 1] <= line) k++;
-        lut[cidx] = k;
+    std::vector<int> in_cell(cells, 0);
+    std::vector<float> lut_bearing(cells, INFINITY);
+    for(uint32_t b = 1; b + 1 < nB; b++) {
+        const int cidx = bearing_grid_cell(ctx.bearings[b], origin, lscale, cells);
+        in_cell[cidx]++;
+        lut_bearing[cidx] = ctx.bearings[b];
     }
+    std::vector<float2> lut(cells);
+    bool exact = true;
+    for(uint32_t cidx = 0, below = 0; cidx < cells; cidx++) {
+        exact = exact && in_cell[cidx] <= 1;
+        float count_bits;
+        std::memcpy(&count_bits, &below, sizeof(float));
+        lut[cidx] = make_float2(count_bits, lut_bearing[cidx]);
+        below += (uint32_t)in_cell[cidx];
+    }
+    ctx.lut_exact = exact ? 1 : 0;
     ctx.lut_cells = cells;
     ctx.lut_origin = origin;
     ctx.lut_scale = lscale;
@@ -652,6 +846,16 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         return RTACX_ERR_CUDA;
     }
     ctx.acc_blocks_per_sm = (uint32_t)acc_blocks;
+    ctx.acc_staged_smem = staged_smem_bytes(nB, nR, cells);
+    for(int m = 0; m < kAccEchoModels; m++) {
+        const void* fs = accumulate_staged_kernel(m);
+        int bs = 0;
+        if(raise_smem_limit(fs, ctx.acc_staged_smem) != cudaSuccess ||
+           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, fs, kStagedThreads, ctx.acc_staged_smem) != cudaSuccess)
+            bs = 0;
+        cudaGetLastError();
+        ctx.acc_staged_blocks[m] = (uint32_t)std::max(bs, 0);
+    }
     if(raise_smem_limit((const void*)k_prec_filter<false>, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess ||
        raise_smem_limit((const void*)k_prec_filter<true>, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
         ctx.error = "cannot reserve shared memory for the range filter";
@@ -711,7 +915,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         return true;
     };
     if(!alloc(ctx.d_G, (size_t)nR * nB * sizeof(float4)) || !alloc(ctx.d_flags, (size_t)(nR + 31) / 32 * 4) ||
-       !alloc(ctx.d_lut, (size_t)cells * sizeof(int)) ||
+       !alloc(ctx.d_lut, (size_t)cells * sizeof(float2)) ||
        !alloc(ctx.d_pwin, (size_t)nR * sizeof(int2)) || !alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) ||
        !alloc(ctx.d_B, B.size() * 2) || !alloc(ctx.d_taps, taps.size() * sizeof(float)) ||
        (!direct && !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float))) ||
@@ -727,7 +931,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     if(cudaMemset(ctx.d_A, 0, (size_t)ctx.Mpad * ctx.Kp * 2) != cudaSuccess ||
        cudaMemcpy(ctx.d_B, B.data(), B.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
        cudaMemcpy(ctx.d_taps, taps.data(), taps.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
-       cudaMemcpy(ctx.d_lut, lut.data(), lut.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(ctx.d_lut, lut.data(), lut.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
        (f16 && (cudaMemcpy(ctx.d_col_scale, col_scale.data(), col_scale.size() * sizeof(float),
                            cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaMemset(ctx.d_row_scale, 0, (size_t)ctx.Mpad * sizeof(float)) != cudaSuccess)) ||
@@ -763,11 +967,26 @@ rtacx_status precision_begin(Context& ctx, cudaStream_t stream)
 rtacx_status precision_accumulate(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream)
 {
     if(!n) return RTACX_OK;
-    const uint32_t blocks = (uint32_t)std::min<uint64_t>((n + kAccThreads * kAccLoads - 1) / (kAccThreads * kAccLoads),
-                                                         (uint64_t)ctx.sm_count * ctx.acc_blocks_per_sm);
+    const uint64_t want = (n + kAccThreads * kAccLoads - 1) / (kAccThreads * kAccLoads);
+    if(ctx.lut_exact && ctx.nB > 1 && !ctx.prec_hot && ctx.bin.vec4 &&
+       (reinterpret_cast<uintptr_t>(samples) & 15u) == 0) {
+        const int m = accumulate_echo_model(ctx.bin.echo_flags);
+        if(ctx.acc_staged_blocks[m] > 0) {
+            const uint64_t stages = (n + kStageRecs - 1) / kStageRecs;
+            const uint32_t blocks = (uint32_t)std::min<uint64_t>(stages, (uint64_t)ctx.sm_count * ctx.acc_staged_blocks[m]);
+            void* args[] = {(void*)&samples, (void*)&n, (void*)&ctx.bin, (void*)&ctx.d_bearings, (void*)&ctx.nB,
+                            (void*)&ctx.d_lut, (void*)&ctx.lut_cells, (void*)&ctx.lut_origin, (void*)&ctx.lut_scale,
+                            (void*)&ctx.d_G, (void*)&ctx.d_flags, (void*)&ctx.d_err};
+            RTACX_CUDA(cudaLaunchKernel(accumulate_staged_kernel(m), dim3(blocks), dim3(kStagedThreads), args,
+                                        ctx.acc_staged_smem, stream));
+            return RTACX_OK;
+        }
+    }
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>(want, (uint64_t)ctx.sm_count * ctx.acc_blocks_per_sm);
     k_prec_accumulate<<<blocks, kAccThreads, ctx.acc_smem, stream>>>(static_cast<const float*>(samples), n, ctx.bin,
                                                                      ctx.d_bearings, ctx.nB, ctx.d_lut, ctx.lut_cells,
-                                                                     ctx.lut_origin, ctx.lut_scale, ctx.d_G, ctx.d_flags,
+                                                                     ctx.lut_origin, ctx.lut_scale, ctx.lut_exact,
+                                                                     ctx.d_G, ctx.d_flags,
                                                                      ctx.prec_hot ? ctx.d_hot : nullptr, ctx.d_rep);
     RTACX_CUDA(cudaGetLastError());
     return RTACX_OK;
@@ -796,8 +1015,10 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream);
 
 rtacx_status run_precision(Context& ctx, const void* samples, uint64_t n, float* out, cudaStream_t stream)
 {
-    ctx.mark(0, false, stream);
+    ctx.mark(5, false, stream);
     rtacx_status st = precision_begin(ctx, stream);
+    ctx.mark(5, true, stream);
+    ctx.mark(0, false, stream);
     if(st == RTACX_OK) st = precision_hot_scan(ctx, samples, n, stream);
     if(st == RTACX_OK) st = precision_accumulate(ctx, samples, n, stream);
     if(st != RTACX_OK) return st;

@@ -67,8 +67,10 @@ rtacx_status reduce_precision_host(Context& c, const void* samples, uint64_t n, 
     cudaEvent_t fork = c.stream_ev[0], copied[2] = {c.stream_ev[1], c.stream_ev[2]},
                 used[2] = {c.stream_ev[3], c.stream_ev[4]};
 
-    c.mark(0, false, s);
+    c.mark(5, false, s);
     if((st = precision_begin(c, s)) != RTACX_OK) return st;
+    c.mark(5, true, s);
+    c.mark(0, false, s);
     RTACX_CUDA(cudaEventRecord(fork, s));
     RTACX_CUDA(cudaStreamWaitEvent(c.copy_stream, fork, 0));
     const uint64_t chunks = (n + RTACX_STREAM_CHUNK - 1) / RTACX_STREAM_CHUNK;

@@ -59,39 +59,10 @@ __host__ __device__ constexpr uint32_t idesc_for(bool f16, int bn)
            ((uint32_t)(BM >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(ok)
-                 : "r"(bar), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-
-// Bounded wait: false if the CTA aborted or the wait ran out of time.
+// Bounded wait of the GEMM (about two seconds).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag)
 {
-    const long long t0 = clock64();
-    while(!mbar_try_wait(bar, parity)) {
-        if(*abort_flag) return false;
-        if(clock64() - t0 > kWaitCycles) { *abort_flag = 1; return false; }
-    }
-    return true;
+    return mbar_wait_bounded(bar, parity, abort_flag, kWaitCycles);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)

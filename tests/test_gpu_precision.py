@@ -326,3 +326,49 @@ def test_precision_degenerate_bearings_match_oracle(oracle):
     want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
     assert np.isfinite(got).all()
     assert rel_l2(got, want) <= TOL
+
+
+@pytest.mark.parametrize("gap", [None, 1e-6])
+def test_precision_bearing_lookup_exact_and_searched(oracle, gap):
+    """The bearing lookup grid is exact (one table lookup, no search) when no
+    grid cell holds two interior bearings, and falls back to a corrected
+    search otherwise: a table with two bearings 1e-6 rad apart takes the
+    search. Both match the oracle's binary search, including samples placed
+    exactly on table bearings and just below them."""
+    wk = wl.precision_2d(n_samples=1 << 14, n_bearings=128, n_ranges=512)
+    b = np.array(wk.sensor["bearings"], dtype=np.float32)
+    if gap is not None:
+        b[60] = np.float32(b[61] - np.float32(gap))
+        wk.sensor["bearings"] = b
+    smp = wk.samples.copy()
+    on = b[np.arange(smp.shape[0] // 4) % b.size]
+    smp[:on.size, 3] = on                                          # exactly on a bearing
+    smp[on.size:2 * on.size, 3] = np.nextafter(on, np.float32(-np.inf))   # just below it
+    ctx = precision_context(wk)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    got = gpu_precision(ctx, smp, wk.out_shape)
+    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    assert np.isfinite(got).all()
+    assert rel_l2(got, want) <= TOL
+
+
+@pytest.mark.parametrize("n", [(1 << 14) + 7, 1000, 1])
+def test_precision_partial_stage_and_unaligned_records(oracle, n):
+    """The staged accumulation copies the samples in stages of 1024 records:
+    a ping whose last stage is partial (or that is shorter than one stage)
+    matches the oracle, and the same samples at an address that is not
+    16-byte aligned (accumulated by the general kernel) give the same ping."""
+    wk = wl.precision_2d(n_samples=n, n_bearings=128, n_ranges=512)
+    ctx = precision_context(wk)
+    D, taps, c = wl.precision_tables(wk.sensor)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    assert np.isfinite(got).all()
+    assert rel_l2(got, want) <= TOL
+    d = to_device(wk.samples, offset_floats=1)
+    out = torch.empty(tuple(wk.out_shape) + (2,), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    ctx.reduce_precision(d, n, out, stream=stream)
+    ctx.stream_status(stream)
+    o = out.cpu().numpy()
+    assert rel_l2(o[..., 0] + 1j * o[..., 1], got) <= 1e-6
