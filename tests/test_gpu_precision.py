@@ -372,3 +372,25 @@ def test_precision_partial_stage_and_unaligned_records(oracle, n):
     ctx.stream_status(stream)
     o = out.cpu().numpy()
     assert rel_l2(o[..., 0] + 1j * o[..., 1], got) <= 1e-6
+
+
+def test_precision_consecutive_pings_start_from_a_zero_grid(oracle):
+    """Each ping zeroes the binned grid for the next one beside its GEMM: pings
+    of different samples on one context, on the caller's stream and on a
+    second stream, each match their own oracle."""
+    wk_a = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512, seed=5)
+    wk_b = wl.precision_2d(n_samples=1 << 14, n_bearings=128, n_ranges=512, seed=6)
+    ctx = precision_context(wk_a)
+    D, taps, c = wl.precision_tables(wk_a.sensor)
+    want = {id(w): oracle.reduce_binned(oracle.apply_echo(w.samples, w.sensor, w.echo), w.sensor, D, taps, c)
+            for w in (wk_a, wk_b)}
+    side = torch.cuda.Stream()
+    for w, stream in ((wk_a, None), (wk_b, None), (wk_a, side), (wk_b, side), (wk_a, None)):
+        d = to_device(w.samples)
+        out = torch.empty(tuple(w.out_shape) + (2,), dtype=torch.float32, device="cuda")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        s.wait_stream(torch.cuda.current_stream())
+        ctx.reduce_precision(d, w.samples.shape[0], out, stream=s)
+        ctx.stream_status(s)
+        o = out.cpu().numpy()
+        assert rel_l2(o[..., 0] + 1j * o[..., 1], want[id(w)]) <= TOL
