@@ -47,10 +47,10 @@ DEFAULT_CONFIG = "precision_2d"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # ncu captures of the default workload, each taken with
 #   ncu --set full --clock-control none -k regex:<kernel> -s <n> -c 1 \
-#       python bench.py --steps 2 --warmup 3 --no-cpu-baseline
+#       python bench.py --steps 2 --warmup 3 --no-cpu-baseline [--no-next-rows]
 # on a GB300. Reported as `traffic` beside the live `achieved` numbers.
 NCU_TRAFFIC_BYTES = {
-    "k_prec_accumulate": 302.046e6 + 3.603e6,
+    "k_prec_accumulate_staged": 302.126e6 + 3.701e6,
     "k_gemm_tn": 31.470e6 + 0.003e6,
     "sort_bin": (268.531e6 + 3.186e6) + (274.855e6 + 223.261e6),   # k_count + k_scatter_staged
 }
@@ -645,8 +645,8 @@ def run_ours(args, world, rank, local):
         Mp, Np, Kp = -(-nR // 128) * 128, -(-2 * nB // 256) * 256, -(-6 * nB // 64) * 64
         gemm_tf = 2.0 * Mp * Np * Kp / (ps["gemm"] / 1e3) / 1e12
         roof_acc = {"bound": "hbm", "achieved": acc_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                    "frac": acc_gbs / peaks["hbm_gbs"], "traffic": ncu.get("k_prec_accumulate"),
-                    "kernel": "k_prec_accumulate",
+                    "frac": acc_gbs / peaks["hbm_gbs"], "traffic": ncu.get("k_prec_accumulate_staged"),
+                    "kernel": "k_prec_accumulate_staged",
                     "peak_source": peaks["source"],
                     "algorithmic": f"{rec_in} B per sample read + 8 B per binned cell"}
         roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
