@@ -540,12 +540,30 @@ k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const 
         if(full) {
 #pragma unroll
             for(int h = 0; h < 2; h++) {
-                const float2* col = sG + h * 32 + lane;
+                const float2* col = sG + h * 32 + lane + warp * 8 * kFiltCols;
                 float2 g[8];
 #pragma unroll
-                for(int i = 0; i < 7; i++) g[i] = col[(warp * 8 + i) * kFiltCols];
-                for(int tt = 0; tt < nt; tt++) {
-                    g[7] = col[(warp * 8 + tt + 7) * kFiltCols];
+                for(int i = 0; i < 7; i++) g[i] = col[i * kFiltCols];
+                // Blocks of eight taps with the window rotated at compile time:
+                // at step i of a block, staged row tt + i + q sits in slot
+                // (q + i) & 7 and the new row goes to the slot of the row just
+                // dropped; after eight steps the window is back in order.
+                int tt = 0;
+                for(; tt + 8 <= nt; tt += 8) {
+#pragma unroll
+                    for(int i = 0; i < 8; i++) {
+                        g[(i + 7) & 7] = col[(tt + i + 7) * kFiltCols];
+                        const float2 c = sT[tt + i];
+#pragma unroll
+                        for(int q = 0; q < 8; q++) {
+                            const float2 gq = g[(q + i) & 7];
+                            acc[q][h].x = fmaf(c.x, gq.x, fmaf(-c.y, gq.y, acc[q][h].x));
+                            acc[q][h].y = fmaf(c.x, gq.y, fmaf(c.y, gq.x, acc[q][h].y));
+                        }
+                    }
+                }
+                for(; tt < nt; tt++) {
+                    g[7] = col[(tt + 7) * kFiltCols];
                     const float2 c = sT[tt];
 #pragma unroll
                     for(int q = 0; q < 8; q++) {
