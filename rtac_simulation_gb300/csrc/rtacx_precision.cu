@@ -316,6 +316,16 @@ int accumulate_echo_model(uint32_t flags)
     return 0;
 }
 
+// Zeroes the pair cells (16-byte stores, grid-stride) and the non-empty
+// bitmap of a new ping in one launch.
+__global__ void k_prec_clear(float4* __restrict__ P, uint64_t cells, uint32_t* __restrict__ bits, uint32_t words)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for(uint64_t i = i0; i < cells; i += stride) P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for(uint64_t i = i0; i < words; i += stride) bits[i] = 0u;
+}
+
 // Hot-range detection (RTACX_PRECISION_HOT_RANGE): range-bin counts of a
 // strided subsample of the ping, then one CTA picks the kHotRows-row window
 // with the largest count. The window is hot when it holds at least a tenth of
@@ -975,8 +985,10 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
 // Zeroes the pair cells and the non-empty bitmap of a new ping.
 rtacx_status precision_begin(Context& ctx, cudaStream_t stream)
 {
-    RTACX_CUDA(cudaMemsetAsync(ctx.d_G, 0, (size_t)ctx.nR * ctx.nB * sizeof(float4), stream));
-    RTACX_CUDA(cudaMemsetAsync(ctx.d_flags, 0, (size_t)(ctx.nR + 31) / 32 * 4, stream));
+    const uint64_t cells = (uint64_t)ctx.nR * ctx.nB;
+    const uint32_t blocks = (uint32_t)std::min<uint64_t>((cells + 255) / 256, (uint64_t)ctx.sm_count * 32);
+    k_prec_clear<<<blocks, 256, 0, stream>>>(ctx.d_G, cells, ctx.d_flags, (ctx.nR + 31) / 32);
+    RTACX_CUDA(cudaGetLastError());
     return RTACX_OK;
 }
 
