@@ -56,6 +56,7 @@ NCU_TRAFFIC_BYTES = {
 }
 
 KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
+PRECISION_KERNELS_PER_PING = 5   # clear, staged accumulate, windows, range filter, tensor-core GEMM
 
 
 def parse_args():
@@ -664,7 +665,7 @@ def run_ours(args, world, rank, local):
     r = res[head]
     line["e2e"] = {"value": world * n * args.steps / r["t_e2e"], "unit": "samples/s",
                    "h2d_bytes_per_step": n * rec_in, "d2h_bytes_per_step": int(np.prod(wk.out_shape)) * 8}
-    line["gpu_launches"] = (4 if head == "precision" else KERNELS_PER_PING) * args.steps
+    line["gpu_launches"] = (PRECISION_KERNELS_PER_PING if head == "precision" else KERNELS_PER_PING) * args.steps
     line["clocks"] = r["clocks"]
     if world == 1 and args.config == DEFAULT_CONFIG and not args.no_next_rows:
         line["next_rows"] = time_next_rows(torch, local, peaks)
