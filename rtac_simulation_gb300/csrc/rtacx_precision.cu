@@ -167,7 +167,10 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p,
 // key, value, cell and weights of its records of a stage without branches
 // (out-of-range and tail records only clear their predicate), then issues
 // the bitmap bits and the vector reductions; the results are those of
-// k_prec_accumulate. One persistent CTA
+// k_prec_accumulate. The bearing lookup is one 16-byte grid entry per sample
+// (no cell table): the weight's reciprocal 1 / (theta_k+1 - theta_k) is
+// computed per sample with the correctly rounded __frcp_rn, the same value
+// as the general kernel's table entry 1.0f / (theta_k+1 - theta_k). One persistent CTA
 // takes stages c = blockIdx.x, blockIdx.x + gridDim.x, ...; thread 0 issues
 // the copy of the stage kStages ahead as soon as every thread has read the
 // stage it refills. Each wait is bounded (kAccWaitCycles); a timeout sets
@@ -181,7 +184,8 @@ constexpr long long kAccWaitCycles = 2000000000ll;   // about one second
 
 size_t staged_smem_bytes(uint32_t nB, uint32_t nR, uint32_t lut_cells)
 {
-    return (size_t)kStages * kStageRecs * sizeof(float4) + accumulate_smem_bytes(nB, nR, lut_cells);
+    return (size_t)kStages * kStageRecs * sizeof(float4) + (size_t)lut_cells * sizeof(float4) +
+           (size_t)((nR + 31) / 32) * sizeof(uint32_t);
 }
 
 template <uint32_t kEcho>
@@ -195,8 +199,7 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
     __shared__ __align__(8) uint64_t s_full[kStages];
     __shared__ int s_abort;
     float4* s_ring = reinterpret_cast<float4*>(s_raw);
-    float2* s_cell = reinterpret_cast<float2*>(s_ring + kStages * kStageRecs);
-    float2* s_lut = s_cell + nB;
+    float4* s_lut = s_ring + kStages * kStageRecs;
     uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_lut + lut_cells);
     const uint32_t words = (p.key.nR + 31) / 32;
     const uint64_t stages = (n + kStageRecs - 1) / kStageRecs;
@@ -219,11 +222,16 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
             if(c < stages) issue(c, i);
         }
     }
-    for(uint32_t i = threadIdx.x; i < nB; i += blockDim.x) {
-        const float th = bearings[i];
-        s_cell[i] = make_float2(th, i + 1 >= nB ? 0.0f : 1.0f / (bearings[i + 1] - th));
+    // Grid entry c: {count k_lo, the interior bearing theta_b in the cell or
+    // +inf, theta_k_lo, the next bearing the weight needs: theta_k_lo+2 when
+    // theta_b is finite (samples at or above it take k_lo + 1), else
+    // theta_k_lo+1}.
+    for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) {
+        const float2 e = lut[i];
+        const int k = __float_as_int(e.x);
+        const bool has_b = e.y != INFINITY;
+        s_lut[i] = make_float4(e.x, e.y, bearings[k], bearings[has_b ? k + 2 : k + 1]);
     }
-    for(uint32_t i = threadIdx.x; i < lut_cells; i += blockDim.x) s_lut[i] = lut[i];
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
     __syncthreads();
     int it = 0;
@@ -245,10 +253,12 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
             row[u] = (ready && idx < count) ? j : kOutOfRange;
             const float2 v = apply_echo(p, make_float2(rec.x, rec.y), rec.z, kEcho);
             const float th = rec.w;
-            const float2 e = s_lut[bearing_grid_cell(th, lut_origin, lut_scale, lut_cells)];
-            const int k = __float_as_int(e.x) + (th >= e.y ? 1 : 0);
-            const float2 cl = s_cell[k];
-            const float w = fminf(fmaxf((th - cl.x) * cl.y, 0.0f), 1.0f);   // NaN bearings -> 0
+            const float4 e = s_lut[bearing_grid_cell(th, lut_origin, lut_scale, lut_cells)];
+            const bool up = th >= e.y;
+            const int k = __float_as_int(e.x) + (up ? 1 : 0);
+            const float tk = up ? e.y : e.z;
+            const float tk1 = (up || e.y == INFINITY) ? e.w : e.y;
+            const float w = fminf(fmaxf((th - tk) * __frcp_rn(tk1 - tk), 0.0f), 1.0f);   // NaN bearings -> 0
             const float w0 = 1.0f - w;
             cell[u] = k;
             add[u] = make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y);
