@@ -321,10 +321,10 @@ rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
  * the caller's stream. rtacx_stage_times waits for the last traced call and
  * writes up to `max` stage durations in milliseconds (0 for stages the last
  * call did not run): for rtacx_reduce count, reset of the bin totals, bin
- * scan, scatter, windows, reduce; for rtacx_reduce_precision accumulate, windows, range
- * filter, tensor-core GEMM, copy-out, and the zeroing of the binned grid
- * before the accumulation. Returns the number of stages written (negative on
- * error). */
+ * scan, scatter, windows, reduce; for rtacx_reduce_precision accumulate, windows (0: the
+ * range filter forms each row's window itself), range filter, tensor-core
+ * GEMM, copy-out, and the zeroing of the binned grid before the
+ * accumulation. Returns the number of stages written (negative on error). */
 #define RTACX_STAGE_COUNT 6
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
 int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);

@@ -352,7 +352,6 @@ struct Context {
     uint32_t acc_staged_blocks[6] = {}; // resident CTAs per SM of each staged accumulation (0: not used)
     size_t acc_staged_smem = 0;
     float lut_origin = 0.0f, lut_scale = 0.0f;
-    int2* d_pwin = nullptr;             // [nR] window bin interval per row (lo > hi: empty)
     uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the filtered grid
     uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity
     float* d_C = nullptr;               // [Mpad][Npad] GEMM output when the ping shape is not tile-aligned

@@ -1,15 +1,16 @@
 // Precision (tensor-core) form: bin first, contract over bearings on the
 // tensor cores, filter in range.
 //
+//   k_prec_clear       zeroes the pair cells and the non-empty bitmap.
 //   k_prec_accumulate  one pass over the samples (read once, 16 B each):
-//                      range key (Binner::Key, bit-exact), optional FP64
+//   (_staged)          range key (Binner::Key, bit-exact), optional FP64
 //                      echo pre-step, linear split between the two table
 //                      bearings around the sample bearing, one 16-byte vector
 //                      float atomic (red.global.add.v4.f32) into the pair
 //                      cell P[j][k]; non-empty range bins in a bitmap. No sort.
-//   k_prec_windows     reference window rule (src/Binner.cu:95-104) on the
-//                      non-empty bitmap.
-//   k_prec_filter      G'[r][k] = sum_t taps[t] G[r + t - c][k] over row r's
+//   k_prec_filter      row r's window by the reference rule
+//                      (src/Binner.cu:95-104) on the non-empty bitmap, then
+//                      G'[r][k] = sum_t taps[t] G[r + t - c][k] over that
 //                      window, written as the bf16 A operand [hi | hi | lo]
 //                      of the three-term split product.
 //   gemm_tn            out = A x B^T on tcgen05 (rtacx_umma.cu), B the
@@ -446,21 +447,19 @@ __device__ __forceinline__ bool bit_set(const uint32_t* bits, long long j)
     return (bits[j >> 5] >> (j & 31)) & 1u;
 }
 
-__global__ void k_prec_windows(const uint32_t* __restrict__ nonempty, uint32_t nR, int ov, int2* __restrict__ win)
+// Window of range row r by the reference rule (src/Binner.cu:95-104) on the
+// non-empty bitmap: [max(0, r - ov), min(nR - 1, r + ov)] shrunk to its first
+// and last non-empty bins; {1, 0} (empty) when fewer than two are non-empty.
+__device__ __noinline__ int2 row_window(const uint32_t* __restrict__ nonempty, uint32_t nR, int ov, int r)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if(r >= (int)nR) return;
-    const long long lo = max(0ll, (long long)r - ov);
-    const long long hi = min((long long)nR - 1, (long long)r + ov);
-    int2 w = make_int2(1, 0);
-    long long a = lo;
+    const int lo = max(0, r - ov);
+    const int hi = (int)min((long long)nR - 1, (long long)r + ov);
+    int a = lo;
     while(a <= hi && !bit_set(nonempty, a)) a++;
-    if(a < hi) {
-        long long z = hi;
-        while(z > a && !bit_set(nonempty, z)) z--;
-        if(a < z) w = make_int2((int)a, (int)z);
-    }
-    win[r] = w;
+    if(a >= hi) return make_int2(1, 0);
+    int z = hi;
+    while(z > a && !bit_set(nonempty, z)) z--;
+    return a < z ? make_int2(a, z) : make_int2(1, 0);
 }
 
 // Round-to-nearest-even fp32 -> bf16 (bit pattern).
@@ -493,7 +492,7 @@ size_t filter_smem_bytes(uint32_t ntaps)
 // per-row-scaled split instead of the bf16 A operand.
 template <bool kF32Out>
 __global__ void __launch_bounds__(kFiltThreads, 4)
-k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const float2* __restrict__ taps,
+k_prec_filter(const float4* __restrict__ P, const uint32_t* __restrict__ nonempty, int ov, const float2* __restrict__ taps,
               uint32_t ntaps, uint32_t center, uint32_t nR, uint32_t nB, uint32_t Kp, uint16_t* __restrict__ A,
               float2* __restrict__ Gf, uint32_t* __restrict__ rowmax)
 {
@@ -504,7 +503,7 @@ k_prec_filter(const float4* __restrict__ P, const int2* __restrict__ win, const 
     int2* sW = reinterpret_cast<int2*>(sT + kFiltTapsMax);              // [kFiltRows]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols;
-    if(tid < kFiltRows) sW[tid] = (r0 + tid < (int)nR) ? win[r0 + tid] : make_int2(1, 0);
+    if(tid < kFiltRows) sW[tid] = (r0 + tid < (int)nR) ? row_window(nonempty, nR, ov, r0 + tid) : make_int2(1, 0);
     float2 acc[8][2];
 #pragma unroll
     for(int q = 0; q < 8; q++) { acc[q][0] = make_float2(0.f, 0.f); acc[q][1] = make_float2(0.f, 0.f); }
@@ -778,7 +777,7 @@ void free_dev(T*& p)
 
 void free_precision(Context& c)
 {
-    free_dev(c.d_G); free_dev(c.d_flags); free_dev(c.d_pwin); free_dev(c.d_A); free_dev(c.d_B);
+    free_dev(c.d_G); free_dev(c.d_flags); free_dev(c.d_A); free_dev(c.d_B);
     free_dev(c.d_C); free_dev(c.d_taps); free_dev(c.d_lut);
     free_dev(c.d_Gf); free_dev(c.d_rowmax); free_dev(c.d_row_scale); free_dev(c.d_col_scale);
     free_dev(c.d_hot); free_dev(c.d_hotcnt); free_dev(c.d_rep);
@@ -954,7 +953,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     };
     if(!alloc(ctx.d_G, (size_t)nR * nB * sizeof(float4)) || !alloc(ctx.d_flags, (size_t)(nR + 31) / 32 * 4) ||
        !alloc(ctx.d_lut, (size_t)cells * sizeof(float2)) ||
-       !alloc(ctx.d_pwin, (size_t)nR * sizeof(int2)) || !alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) ||
+!alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) ||
        !alloc(ctx.d_B, B.size() * 2) || !alloc(ctx.d_taps, taps.size() * sizeof(float)) ||
        (!direct && !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float))) ||
        (f16 && (!alloc(ctx.d_Gf, (size_t)nR * nB * sizeof(float2)) || !alloc(ctx.d_rowmax, (size_t)nR * 4) ||
@@ -1074,21 +1073,17 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
         k_hot_fold<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, nB, ctx.d_rep, ctx.d_G);
         RTACX_CUDA(cudaGetLastError());
     }
-    ctx.mark(1, false, stream);
-    k_prec_windows<<<(nR + 255) / 256, 256, 0, stream>>>(ctx.d_flags, nR, ctx.overlap, ctx.d_pwin);
-    RTACX_CUDA(cudaGetLastError());
-    ctx.mark(1, true, stream);
     ctx.mark(2, false, stream);
     const dim3 fgrid((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows);
     if(!ctx.prec_f16) {
         k_prec_filter<false><<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
-            ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, ctx.d_A, nullptr, nullptr);
+            ctx.d_G, ctx.d_flags, ctx.overlap, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, ctx.d_A, nullptr, nullptr);
         RTACX_CUDA(cudaGetLastError());
     }
     else {
         RTACX_CUDA(cudaMemsetAsync(ctx.d_rowmax, 0, (size_t)nR * 4, stream));
         k_prec_filter<true><<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
-            ctx.d_G, ctx.d_pwin, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, nullptr, ctx.d_Gf, ctx.d_rowmax);
+            ctx.d_G, ctx.d_flags, ctx.overlap, ctx.d_taps, ctx.taps, ctx.tap_center, nR, nB, ctx.Kp, nullptr, ctx.d_Gf, ctx.d_rowmax);
         RTACX_CUDA(cudaGetLastError());
         k_prec_split_f16<<<nR, 256, 0, stream>>>(ctx.d_Gf, ctx.d_rowmax, nR, nB, ctx.Kp, ctx.d_A, ctx.d_row_scale);
         RTACX_CUDA(cudaGetLastError());
