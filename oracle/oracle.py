@@ -2,8 +2,10 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline / reference arm of bench.py, never by the product package.
-Parity status: partially pinned (range key and pulse table against the
-reference's own headers, tests/golden/); the rest is a restatement.
+Parity status: pinned for the range key and pulse table (the reference's own
+headers) and for the 2D reduction (the reference's own kernel run on a GB300:
+reduce(mode=2) reproduces its pings, tests/golden/ref_pings_2d.npz); the 1D
+reduction is a restatement.
 """
 from __future__ import annotations
 
@@ -131,7 +133,10 @@ def pulse_scale(sensor: dict, literal_1d: bool = False) -> np.float32:
 def reduce(samples: np.ndarray, sensor: dict, mode: int = 0, rows=None, threads: int = 0,
            literal_1d: bool = False) -> np.ndarray:
     """Oracle ping. mode 0: FP64 (complex128), mode 1: FP32 reference
-    arithmetic (complex64). rows = (begin, end) restricts the output rows."""
+    arithmetic (complex64), mode 2 (2D): the PSF fetched as the reference's
+    texture does on the GPU (coordinate truncated to 21 fractional bits,
+    weights rounded to 1/256), accumulated in FP64 (complex128). rows =
+    (begin, end) restricts the output rows."""
     lib = load()
     s = np.ascontiguousarray(samples, dtype=np.float32)
     n, stride = s.shape
@@ -148,7 +153,9 @@ def reduce(samples: np.ndarray, sensor: dict, mode: int = 0, rows=None, threads:
         beam = np.zeros(1, dtype=np.float32)
         bearings = np.zeros(1, dtype=np.float32)
         bscale, nB = np.float32(0.0), 1
-    out = np.zeros((r1 - r0, nB), dtype=np.complex128 if mode == 0 else np.complex64)
+    if mode == 2 and dims != 2:
+        raise ValueError("the texture-unit mode is 2D only")
+    out = np.zeros((r1 - r0, nB), dtype=np.complex64 if mode == 1 else np.complex128)
     threads = threads or (os.cpu_count() or 1)
     lib.rtacx_oracle_reduce(dims, s.ctypes.data, n, sensor["range_min"], sensor["range_max"], nR,
                             sensor["margin"], pulse_scale(sensor, literal_1d), pulse.ctypes.data, pulse.size,

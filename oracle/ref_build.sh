@@ -1,8 +1,16 @@
 #!/bin/sh
-# Builds the golden-vector probe from the reference's own headers and its
-# src/Directivity.cpp (the receiver directivity table builders).
+# Builds, from the reference tree, the test-infrastructure programs that
+# record golden vectors (outputs only under oracle/_ref, git-ignored):
+#   _ref/ref_probe          the reference's own Binner.h / Waveform.h and
+#                           src/Directivity.cpp on the host (g++), with the
+#                           host stand-ins of oracle/ref_stubs;
+#   _ref/ref_sparse2d.cubin the reference's own src/SensorInstance2D.cu
+#                           (do_sparse_convolve_2d_f and the KernelView2D
+#                           texture lookup) for sm_103a (nvcc), with the
+#                           device stand-ins of oracle/ref_stubs_cuda; it is
+#                           launched by oracle/ref_sparse_harness.cpp on a
+#                           GPU machine (tests/golden/make_ref_pings.py).
 # Usage: oracle/ref_build.sh [REFERENCE_ROOT]   (default /root/reference)
-# Output: oracle/_ref/ref_probe (git-ignored). Test infrastructure only.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${1:-/root/reference}"
@@ -10,3 +18,7 @@ mkdir -p "$HERE/_ref"
 g++ -std=c++17 -O1 -ffp-contract=off -fno-fast-math \
     -I "$HERE/ref_stubs" -I "$REF/include" \
     "$HERE/ref_probe.cpp" "$REF/src/Directivity.cpp" -o "$HERE/_ref/ref_probe"
+NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+"$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -diag-suppress 20012 \
+    -I "$HERE/ref_stubs_cuda" -I "$REF/include" \
+    "$REF/src/SensorInstance2D.cu" -o "$HERE/_ref/ref_sparse2d.cubin"

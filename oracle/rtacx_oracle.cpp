@@ -5,13 +5,17 @@
 // or as the timed CPU rendition of the reference algorithm. The product path
 // (librtacx.so) never links or calls it.
 //
-// Parity status: PARTIALLY PINNED. Binner::Key (range key) and Waveform_Sine
-// (pulse table) are pinned against golden vectors produced by compiling the
-// reference's own headers (oracle/ref_probe.cpp, tests/golden/). Everything
-// downstream of the keys -- segments, windows, the texture-equivalent PSF
-// lookup and the reductions -- is restated from the reference sources cited
-// below; the reference cannot be built here (rtac_base/rtac_cuda, yaml-cpp and
-// OptiX/GL are absent) and ships no test vectors, so that part is unpinned.
+// Parity status: PINNED for the range key, the pulse table and the 2D
+// reduction. Binner::Key and Waveform_Sine are pinned against golden vectors
+// produced by compiling the reference's own headers (oracle/ref_probe.cpp,
+// tests/golden/ref_keys.json, ref_waveforms.json). The 2D reduction
+// (segments, windows, PSF lookup, accumulation) is pinned against pings of
+// the reference's own do_sparse_convolve_2d_f kernel, compiled from the
+// reference tree and run on a GB300 (oracle/ref_sparse_harness.cpp,
+// tests/golden/ref_pings_2d.npz): mode 2 below, which emulates the texture
+// unit's fixed-point weights, reproduces them to 1e-7 relative L2. The 1D
+// reduction is restated from the cited sources only (the reference's 1D
+// texture set-up is not reproducible).
 //
 // Arithmetic contract (shared with the CUDA path):
 //   * Key parameters are computed in float exactly as the Key constructor does
@@ -143,6 +147,28 @@ inline T lerp_border_f32(const T* table, int n, float u)
     T lo = (i >= 0)    ? table[i]     : T(0);
     T hi = (i + 1 < n) ? table[i + 1] : T(0);
     return lo * (1.0f - alpha) + hi * alpha;
+}
+
+// Linear texture fetch as the texture unit performs it. CUDA's programming
+// guide (texture fetching appendix): x = u * n - 0.5 for a normalized
+// coordinate u, i = floor(x), weight frac(x) in 9-bit fixed point with 8
+// fractional bits. The remaining details were measured on GB300 with
+// in-bounds probe fetches (2e5 coordinates each; every one reproduced):
+//  * per axis (ramps T[i] = i, n = 2, 64, 164, 500, 3495): u is truncated to
+//    21 fractional bits before the scaling, and the weight k = frac(x) * 256
+//    is rounded half up to an integer in [0, 256];
+//  * bilinear (a unit texel of a 4 x 4 texture at random (u, v)): with
+//    per-axis weights a (x) and b (y), the corner weights in 1/256 are
+//    w11 = round_half_up(a b / 256), w10 = a - w11, w01 = b - w11,
+//    w00 = 256 - a - b + w11 (they sum to 256).
+// Border addressing: texels outside [0, n) are 0. Returns i and k.
+inline int texel_weight(float u, int n, int& k)
+{
+    const double uq = std::floor((double)u * 2097152.0) / 2097152.0;
+    const double x = uq * n - 0.5;
+    const double fl = std::floor(x);
+    k = (int)std::floor((x - fl) * 256.0 + 0.5);
+    return (int)std::max(-2.0, std::min(fl, (double)n + 1.0));
 }
 
 struct Sensor {
@@ -292,6 +318,41 @@ void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void*
             }
         }
     }
+    else if(mode == 2) {
+        // Texture-unit emulation (2D): the bilinear fetch of the W x H table
+        // PSF[h][w] = pulse[h] * beam[w] (rounded to float, as
+        // generate_psf_data builds it, src/SensorInstance2D.cu:20-33) with
+        // the texture unit's weights (texel_weight), at the kernel's
+        // coordinates fmaf(scale, delta, 0.5)
+        // (include/rtac_simulation/ReductionKernel.h:63-69); the weighted
+        // texel sum and the accumulation in double.
+        std::complex<double>* o = static_cast<std::complex<double>*>(out_row);
+        std::vector<std::complex<float>> psf((size_t)W * H);
+        for(int h = 0; h < H; h++)
+            for(int w = 0; w < W; w++) psf[(size_t)h * W + w] = pulse_f[h] * S.beam[w];
+        auto texel = [&](int i, int j) -> std::complex<double> {
+            if(i < 0 || i >= W || j < 0 || j >= H) return std::complex<double>(0.0, 0.0);
+            const std::complex<float> t = psf[(size_t)j * W + i];
+            return std::complex<double>(t.real(), t.imag());
+        };
+        for(uint32_t b = 0; b < nB; b++) {
+            std::complex<double> acc(0.0, 0.0);
+            const float th = S.bearings[b];
+            for(uint32_t k = 0; k < size; k++) {
+                const SortedSample& s = B.sorted[off + k];
+                const float uy = std::fmaf(S.pulse_scale, s.travel - R, 0.5f);
+                const float ux = std::fmaf(S.beam_scale, s.bearing - th, 0.5f);
+                int a, c;
+                const int i = texel_weight(ux, W, a), j = texel_weight(uy, H, c);
+                const int w11 = (a * c + 128) >> 8, w10 = a - w11, w01 = c - w11, w00 = 256 - a - c + w11;
+                const std::complex<double> w = ((double)w00 * texel(i, j) + (double)w10 * texel(i + 1, j) +
+                                                (double)w01 * texel(i, j + 1) + (double)w11 * texel(i + 1, j + 1)) /
+                                               256.0;
+                acc += std::complex<double>(s.re, s.im) * w;
+            }
+            o[b] = acc;
+        }
+    }
     else {
         // Literal per-(sample, output) loop of do_sparse_convolve_2d_f /
         // do_sparse_convolve_1d_f in float: one fused PSF evaluation per pair.
@@ -399,7 +460,8 @@ int rtacx_oracle_bin(const float* samples, uint64_t n, uint32_t stride, uint32_t
 }
 
 // Full reduction. mode 0: FP64 (out = 2 doubles per cell), mode 1: FP32
-// reference arithmetic (out = 2 floats per cell). Rows [row_begin, row_end)
+// reference arithmetic (out = 2 floats per cell), mode 2 (2D): the PSF
+// fetched as the texture unit does, accumulated in FP64 (2 doubles per cell). Rows [row_begin, row_end)
 // only; nthreads worker threads. Returns the wall time of the sort+bin step
 // in seconds through bin_seconds (optional).
 void rtacx_oracle_reduce(uint32_t dims, const float* samples, uint64_t n,
@@ -416,7 +478,7 @@ void rtacx_oracle_reduce(uint32_t dims, const float* samples, uint64_t n,
     BinResult B;
     do_bin(samples, n, dims == 2 ? 4u : 3u, dims, key, rmin, rmax, nR, margin, B);
     const uint32_t nb = (dims == 2) ? nB : 1u;
-    const size_t cell = (mode == 0) ? 16 : 8;
+    const size_t cell = (mode == 1) ? 8 : 16;
     row_end = std::min(row_end, nR);
     parallel_rows(row_begin, row_end, nthreads, [&](uint32_t r) {
         reduce_row(S, B, r, mode, static_cast<char*>(out) + (size_t)(r - row_begin) * nb * cell);

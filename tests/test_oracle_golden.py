@@ -64,3 +64,50 @@ def test_waveform_sine_matches_reference():
         for got, want in ((w.real, re), (w.imag, im)):
             ulp = np.spacing(np.maximum(np.abs(want), np.float32(1e-30)).astype(np.float32))
             assert np.all(np.abs(got.astype(np.float64) - want) <= ulp + 1e-30)
+
+
+# ---- 2D pings of the reference's own reduction kernel ----------------------
+# tests/golden/ref_pings_2d.npz holds pings computed by the reference's
+# do_sparse_convolve_2d_f (src/SensorInstance2D.cu:44-83), compiled from the
+# reference tree and launched on a GB300 by tests/golden/make_ref_pings.py.
+# The reference fetches its PSF from a linear-filtered texture, whose weights
+# the texture unit holds in 8-bit fixed point; oracle mode 2 emulates that
+# unit and reproduces the reference's pings to float round-off. The exact
+# bilinear PSF (oracle mode 0, the FP64 target of this project's kernels)
+# differs from them by the texture weights' quantization alone.
+REF_PINGS_TOL_TEXTURE = 1e-6     # oracle mode 2 vs the reference kernel (measured 7e-8 .. 1e-7)
+REF_PINGS_TOL_EXACT = 3e-3       # oracle mode 0 vs the reference kernel (measured 5.5e-4 .. 1.7e-3)
+
+
+def ref_ping_cases():
+    import ast
+    z = np.load(GOLDEN / "ref_pings_2d.npz")
+    names = sorted({k.split("__")[0] for k in z.files})
+    out = []
+    for name in names:
+        builder = str(z[f"{name}__builder"])
+        kwargs = dict(ast.literal_eval(str(z[f"{name}__kwargs"])))
+        step = int(z[f"{name}__row_step"])
+        out.append((name, getattr(workloads, builder)(**kwargs), step, z[f"{name}__ping"].astype(np.complex128)))
+    return out
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_oracle_texture_mode_reproduces_reference_kernel(oracle):
+    cases = ref_ping_cases()
+    assert len(cases) == 2
+    for name, wk, step, ref in cases:
+        got = oracle.reduce(wk.samples, wk.sensor, mode=2)[::step]
+        assert got.shape == ref.shape, name
+        assert _rel(got, ref) <= REF_PINGS_TOL_TEXTURE, (name, _rel(got, ref))
+
+
+def test_oracle_exact_psf_against_reference_kernel(oracle):
+    for name, wk, step, ref in ref_ping_cases():
+        exact = oracle.reduce(wk.samples, wk.sensor, mode=0)[::step]
+        err = _rel(exact, ref)
+        # Non-zero (the texture quantization is real) and within its envelope.
+        assert 1e-5 < err <= REF_PINGS_TOL_EXACT, (name, err)
