@@ -59,6 +59,19 @@ typedef int rtacx_status;
  * the evident intent 1 / (duration * c) that the 2D path uses. */
 #define RTACX_FLAG_1D_LITERAL_SCALING 1u
 
+/* rtacx_sensor_2d.flags: evaluate the PSF as the reference does, by a
+ * linear-filtered texture fetch (src/SensorInstance2D.cu:14-15, 20-42,
+ * include/rtac_simulation/ReductionKernel.h:63-69) on the GPU's texture
+ * unit, whose bilinear weights are fixed point (1/256): rtacx_reduce then
+ * reproduces the reference's 2D pings to float round-off. Without the flag
+ * the PSF uses exact bilinear weights (the FP64 rendition the plain form
+ * meets at 1e-5), which differ from the reference's pings by up to a few
+ * 1e-3 relative L2. The flag keeps range-only bins (one contiguous sample
+ * run per output row, as the reference's bin views) and a slower gather
+ * (one texture fetch per sample and output cell). The batched and the
+ * allocation-free entry points do not take it (RTACX_ERR_UNSUPPORTED). */
+#define RTACX_FLAG_TEXTURE_PSF 2u
+
 /* 1D echosounder (SensorInstance1D, include/rtac_simulation/SensorInstance1D.h). */
 typedef struct {
     float range_min;        /* ranges_: Linspace<float>(min, max, count)     */

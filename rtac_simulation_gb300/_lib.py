@@ -25,6 +25,7 @@ RTACX_KEY_OUT_OF_RANGE = 0xFFFFFFFF
 RTACX_SAMPLE_1D = 1
 RTACX_SAMPLE_2D = 2
 RTACX_FLAG_1D_LITERAL_SCALING = 1
+RTACX_FLAG_TEXTURE_PSF = 2
 
 _STATUS_NAMES = {
     RTACX_OK: "RTACX_OK",

@@ -32,9 +32,55 @@ void sync_echo(Context& c)
     c.bin.echo_k_lo = (float)(c.bin.echo_cycles - (double)c.bin.echo_k_hi);
 }
 
+// PSF image of the reference sensor (generate_psf_data,
+// src/SensorInstance2D.cu:20-33): PSF[h][w] = waveform[h] * beam[w] in
+// float, W = beam taps wide, H = pulse taps high, sampled by a texture with
+// linear filtering, border addressing and normalized coordinates
+// (src/SensorInstance2D.cu:14-15); KernelView2D scalings {1 / span, 0.5} and
+// {1 / (duration c), 0.5} (src/SensorInstance2D.cu:35-42).
+rtacx_status make_psf_texture(Context& c, const rtacx_sensor_2d* s)
+{
+    const uint32_t W = s->beam_len, H = s->pulse_len;
+    std::vector<float2> img((size_t)W * H);
+    for(uint32_t h = 0; h < H; h++)
+        for(uint32_t w = 0; w < W; w++)
+            img[(size_t)h * W + w] = make_float2(s->pulse[2 * h] * s->beam[w], s->pulse[2 * h + 1] * s->beam[w]);
+    const cudaChannelFormatDesc ch = cudaCreateChannelDesc<float2>();
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    if(cudaMallocArray(&c.psf_array, &ch, W, H) != cudaSuccess ||
+       cudaMemcpy2DToArray(c.psf_array, 0, 0, img.data(), W * sizeof(float2), W * sizeof(float2), H,
+                           cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        c.error = "cannot upload the PSF texture (texture limits: width and height)";
+        return RTACX_ERR_CUDA;
+    }
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = c.psf_array;
+    if(cudaCreateTextureObject(&c.psf_tex, &rd, &td, nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        c.psf_tex = 0;
+        c.error = "cannot create the PSF texture";
+        return RTACX_ERR_CUDA;
+    }
+    c.tex_xscale = 1.0f / s->beam_span;
+    c.tex_yscale = host_pulse_scale(s->pulse_duration, s->sound_celerity, false);
+    return RTACX_OK;
+}
+
 void free_config(Context& c)
 {
     free_precision(c);
+    if(c.psf_tex) cudaDestroyTextureObject(c.psf_tex);
+    c.psf_tex = 0;
+    if(c.psf_array) cudaFreeArray(c.psf_array);
+    c.psf_array = nullptr;
     free_dev(c.d_pulse); free_dev(c.d_beam); free_dev(c.d_bearings); free_dev(c.d_ranges);
     free_dev(c.d_support); free_dev(c.d_bb_tiles64); free_dev(c.d_bb_tiles128); c.d_bb_tiles = nullptr;
     free_dev(c.d_offsets); free_dev(c.d_totals);
@@ -229,6 +275,7 @@ rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* s)
     if(!s->beam || s->beam_len == 0) { c.error = "beam table is empty"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(!s->bearings || s->bearing_count == 0) { c.error = "bearing table is empty"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(!(s->beam_span > 0.0f) || !std::isfinite(s->beam_span)) { c.error = "beam_span must be positive"; return RTACX_ERR_INVALID_ARGUMENT; }
+    if(s->flags & ~RTACX_FLAG_TEXTURE_PSF) { c.error = "unknown 2D sensor flags"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(!all_finite(s->beam, s->beam_len) || !all_finite(s->bearings, s->bearing_count)) {
         c.error = "beam or bearing table holds non-finite values";
         return RTACX_ERR_INVALID_ARGUMENT;
@@ -265,7 +312,8 @@ rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* s)
     const double sb = 0.5 * (double)s->beam_span * (1.0 + 1.0 / c.W) * (1.0 + 1e-4) + 1e-6;
     const double lo = (double)*mm.first - sb, hi = (double)*mm.second + sb;
     uint32_t nBB = 1;
-    if(4.0 * 2.0 * sb < hi - lo) {   // support below a quarter of the fan
+    const bool texture_psf = (s->flags & RTACX_FLAG_TEXTURE_PSF) != 0;
+    if(!texture_psf && 4.0 * 2.0 * sb < hi - lo) {   // support below a quarter of the fan
         while(nBB < 32 && (hi - lo) / (2.0 * nBB) > sb && (uint64_t)c.nR * nBB * 2 <= kMaxSmemBins) nBB *= 2;
     }
     float bb_scale = 0.0f, bb_offset = 0.0f;
@@ -305,6 +353,7 @@ rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* s)
        !upload(c, c.d_bb_tiles128, bbt128.data(), bbt128.size()) || !allocate_bins(c))
         return RTACX_ERR_OUT_OF_MEMORY;
     c.d_bb_tiles = (c.bearing_tile == 64) ? c.d_bb_tiles64 : c.d_bb_tiles128;
+    if(texture_psf && make_psf_texture(c, s) != RTACX_OK) return RTACX_ERR_CUDA;
     {
         const uint64_t tiles = (uint64_t)((c.nB + c.bearing_tile - 1) / c.bearing_tile) * ((c.nR + c.range_tile - 1) / c.range_tile);
         if(!upload<uint32_t>(c, c.d_tile_parts, nullptr, tiles) || !upload<uint32_t>(c, c.d_tile_first, nullptr, tiles + 1) ||

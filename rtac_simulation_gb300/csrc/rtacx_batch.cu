@@ -242,6 +242,7 @@ rtacx_status rtacx_batch_plan(rtacx_batch* b, const rtacx_ping_desc* pings, uint
         if(!p.ctx || !p.samples || !p.out || p.n == 0) { B.error = "ping " + std::to_string(i) + ": null pointer or no samples"; return RTACX_ERR_INVALID_ARGUMENT; }
         Context& c = p.ctx->impl;
         if(!c.configured) { B.error = "ping " + std::to_string(i) + ": context not configured"; return RTACX_ERR_NOT_CONFIGURED; }
+        if(c.psf_tex) { B.error = "ping " + std::to_string(i) + ": RTACX_FLAG_TEXTURE_PSF is not supported in batches"; return RTACX_ERR_UNSUPPORTED; }
         if(c.device != B.device) { B.error = "ping " + std::to_string(i) + ": context on another device"; return RTACX_ERR_INVALID_ARGUMENT; }
         if(!seen.insert(p.ctx).second) { B.error = "ping " + std::to_string(i) + ": every ping needs its own context"; return RTACX_ERR_INVALID_ARGUMENT; }
         if(p.n >= (1ull << 32)) { B.error = "at most 2^32 - 1 samples per ping"; return RTACX_ERR_UNSUPPORTED; }

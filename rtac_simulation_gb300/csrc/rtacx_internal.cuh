@@ -294,6 +294,9 @@ struct Context {
     float2* d_pulse = nullptr;          // pulse padded with a zero tap on each side
     float* d_beam = nullptr;            // beam padded with a zero tap on each side
     float* d_bearings = nullptr;        // [nB]
+    cudaArray_t psf_array = nullptr;    // RTACX_FLAG_TEXTURE_PSF: W x H float2 PSF image
+    cudaTextureObject_t psf_tex = 0;    // ... linear filter, border, normalized coordinates
+    float tex_xscale = 0.0f, tex_yscale = 0.0f;   // KernelView2D scalings .x (.y = 0.5)
     float* d_ranges = nullptr;          // [nR] Linspace values
     int2* d_support = nullptr;          // [nR] range bins that can hold PSF support of row r
     int2* d_bb_tiles = nullptr;         // bearing-bin range of each tile of width bearing_tile

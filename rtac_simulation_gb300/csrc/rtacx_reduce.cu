@@ -299,6 +299,42 @@ k_gather_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
     gather_rows_1d(sorted, off, win, ranges, s_pulse, rp, out, blockIdx.x * kWarps);
 }
 
+// ---- RTACX_FLAG_TEXTURE_PSF: the reference's texture evaluation ------------
+// One warp per output cell (r, b): the lanes stride over the samples of row
+// r's window (range-only bins, so one contiguous run of the sorted samples,
+// as the reference's bin view), fetch the PSF from the texture at the
+// reference kernel's coordinates (fmaf(1 / span, theta_s - theta_b, 0.5),
+// fmaf(1 / (duration c), t_s - R_r, 0.5); src/SensorInstance2D.cu:59-64,
+// include/rtac_simulation/ReductionKernel.h:63-69) and accumulate
+// value * psf in complex float; a warp reduction writes the cell.
+__global__ void __launch_bounds__(kThreads)
+k_gather_tex(const float4* __restrict__ sorted, const uint32_t* __restrict__ off, const int2* __restrict__ win,
+             const float* __restrict__ ranges, const float* __restrict__ bearings, cudaTextureObject_t psf,
+             float xscale, float yscale, uint32_t nR, uint32_t nB, float2* __restrict__ out)
+{
+    const uint64_t cell = ((uint64_t)blockIdx.x * kThreads + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if(cell >= (uint64_t)nR * nB) return;
+    const uint32_t r = (uint32_t)(cell / nB), b = (uint32_t)(cell % nB);
+    const int2 w = win[r];
+    float2 acc = make_float2(0.f, 0.f);
+    if(w.x <= w.y) {
+        const float R = ranges[r], th = bearings[b];
+        const uint32_t p0 = off[w.x], p1 = off[w.y + 1];
+        for(uint32_t i = p0 + lane; i < p1; i += 32) {
+            const float4 s = sorted[i];
+            const float2 f = tex2D<float2>(psf, fmaf(xscale, s.w - th, 0.5f), fmaf(yscale, s.z - R, 0.5f));
+            acc.x += s.x * f.x - s.y * f.y;
+            acc.y += s.x * f.y + s.y * f.x;
+        }
+    }
+    for(int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if(lane == 0) out[cell] = acc;
+}
+
 // ---- split persistent gather of one 2D ping -------------------------------
 // k_tile_parts counts each output tile's sample stream (same definition as
 // gather_tile_2d) and splits it into parts of at most kPartSamples samples
@@ -526,6 +562,15 @@ rtacx_status run_reduce(Context& ctx, float* out_f, cudaStream_t stream)
             ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_ranges, ctx.d_pulse, ctx.red, out);
         const cudaError_t e = cudaGetLastError();
         if(e != cudaSuccess) { ctx.error = std::string("k_gather_1d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+        return RTACX_OK;
+    }
+    if(ctx.psf_tex) {
+        const uint64_t warps = (uint64_t)ctx.nR * ctx.nB;
+        k_gather_tex<<<(uint32_t)((warps + kWarps - 1) / kWarps), kThreads, 0, stream>>>(
+            ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_ranges, ctx.d_bearings, ctx.psf_tex, ctx.tex_xscale,
+            ctx.tex_yscale, ctx.nR, ctx.nB, out);
+        const cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess) { ctx.error = std::string("k_gather_tex: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
         return RTACX_OK;
     }
     if(ctx.range_tile == 32) return launch_2d<32, 128>(ctx, out, stream);

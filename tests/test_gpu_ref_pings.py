@@ -26,3 +26,34 @@ def test_plain_form_against_reference_kernel_pings(oracle):
         # the difference is the texture quantization: the exact-PSF oracle
         # matches the GPU ping at the plain form's tolerance
         assert rel_l2(got, oracle.reduce(wk.samples, wk.sensor)) <= 1e-5, name
+
+
+def test_texture_psf_flag_reproduces_reference_kernel_pings(oracle):
+    """RTACX_FLAG_TEXTURE_PSF evaluates the PSF on the texture unit, as the
+    reference does: the pings then match the reference kernel's to float
+    round-off, and the oracle's texture mode on another geometry."""
+    from rtac_simulation_gb300 import _lib
+    from rtac_simulation_gb300 import workloads as wl
+    for name, wk, step, ref in ref_ping_cases():
+        ctx = make_context(wk, flags=_lib.RTACX_FLAG_TEXTURE_PSF)
+        got = gpu_reduce(ctx, wk.samples, wk.out_shape)
+        assert rel_l2(got[::step], ref) <= 1e-6, (name, rel_l2(got[::step], ref))
+    wk = wl.oculus_2d(n_samples=1 << 14, n_bearings=100, n_ranges=300, seed=21)
+    ctx = make_context(wk, flags=_lib.RTACX_FLAG_TEXTURE_PSF)
+    got = gpu_reduce(ctx, wk.samples, wk.out_shape)
+    assert rel_l2(got, oracle.reduce(wk.samples, wk.sensor, mode=2)) <= 1e-6
+
+
+def test_texture_psf_flag_rejected_where_unsupported():
+    from rtac_simulation_gb300 import _lib
+    from rtac_simulation_gb300 import workloads as wl
+    wk = wl.oculus_2d(n_samples=1 << 12, n_bearings=64, n_ranges=128)
+    ctx = make_context(wk, flags=_lib.RTACX_FLAG_TEXTURE_PSF)
+    d = torch.from_numpy(wk.samples.reshape(-1)).cuda()
+    out = torch.empty(tuple(wk.out_shape) + (2,), dtype=torch.float32, device="cuda")
+    batch = _lib.Batch(0)
+    with pytest.raises(_lib.RtacxError):
+        batch.plan([(ctx, d, wk.n, out)])
+    with pytest.raises(_lib.RtacxError):
+        ctx2 = _lib.Context(0)
+        ctx2.configure_2d(**wk.sensor, flags=4)
