@@ -340,6 +340,15 @@ rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
  * accumulation. Returns the number of stages written (negative on error). */
 #define RTACX_STAGE_COUNT 6
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
+
+/* Diagnostic for the failure path (no counterpart in the reference): the
+ * staged precision accumulation of this context skips the bulk copy of
+ * sample stage `stage` (1024 records each; 0xFFFFFFFF: none, the default).
+ * The CTA waiting for it gives up after about one second, sets a bit in the
+ * device error word, waits (bounded) for its other copies and stops; the
+ * ping is then incomplete and rtacx_stream_status returns RTACX_ERR_DEVICE.
+ * The context stays usable: the next ping clears its grid. */
+rtacx_status rtacx_diag_drop_accumulation_stage(rtacx_ctx* ctx, uint32_t stage);
 int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);
 
 /* Diagnostic: synchronous C = A * B^T on the tensor cores (the GEMM of the

@@ -70,6 +70,7 @@ SIGNATURES = {
     "rtacx_reduce": (_I, [_P, _P, _U64, _P, _P]),
     "rtacx_stream_status": (_I, [_P, _P]),
     "rtacx_set_tracing": (_I, [_P, _I]),
+    "rtacx_diag_drop_accumulation_stage": (_I, [_P, _U32]),
     "rtacx_stage_times": (_I, [_P, ctypes.POINTER(ctypes.c_float), _I]),
     "rtacx_reduce_noalloc": (_I, [_I, _P, _P, _U64, _P, _P]),
     "rtacx_gemm_bf16_tn": (_I, [_P, _P, _P, _I, _I, _I, _P]),
@@ -304,6 +305,11 @@ class Context:
                        carrier_hz, sound_celerity)
         self._check(self._lib.rtacx_rasterize(self._h, ctypes.byref(m), ctypes.byref(v), _ptr(samples),
                                               _stream(stream)))
+
+    def diag_drop_accumulation_stage(self, stage: int = 0xFFFFFFFF) -> None:
+        """Failure-path diagnostic: the staged accumulation skips one stage's
+        copy (0xFFFFFFFF: none), so its CTA times out and flags the error word."""
+        self._check(self._lib.rtacx_diag_drop_accumulation_stage(self._h, stage))
 
     def set_tracing(self, enable: bool) -> None:
         self._check(self._lib.rtacx_set_tracing(self._h, 1 if enable else 0))

@@ -463,6 +463,13 @@ rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_
     return run_precision(c, samples, n, out, static_cast<cudaStream_t>(stream));
 }
 
+rtacx_status rtacx_diag_drop_accumulation_stage(rtacx_ctx* ctx, uint32_t stage)
+{
+    if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;
+    ctx->impl.diag_drop_stage = stage;
+    return RTACX_OK;
+}
+
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable)
 {
     if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;

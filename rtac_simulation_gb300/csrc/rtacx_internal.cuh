@@ -354,6 +354,7 @@ struct Context {
     int lut_exact = 0;                  // no grid cell holds two interior bearings
     uint32_t acc_staged_blocks[6] = {}; // resident CTAs per SM of each staged accumulation (0: not used)
     size_t acc_staged_smem = 0;
+    uint32_t diag_drop_stage = 0xFFFFFFFFu; // failure-path test: stage whose copy the staged accumulation skips
     float lut_origin = 0.0f, lut_scale = 0.0f;
     uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the filtered grid
     uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity

@@ -194,7 +194,8 @@ __global__ void __launch_bounds__(kStagedThreads)
 k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinParams p,
                          const float* __restrict__ bearings, uint32_t nB, const float2* __restrict__ lut,
                          uint32_t lut_cells, float lut_origin, float lut_scale,
-                         float4* __restrict__ P, uint32_t* __restrict__ nonempty, uint32_t* __restrict__ err)
+                         float4* __restrict__ P, uint32_t* __restrict__ nonempty, uint32_t* __restrict__ err,
+                         uint32_t drop_stage)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ __align__(8) uint64_t s_full[kStages];
@@ -205,6 +206,7 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
     const uint32_t words = (p.key.nR + 31) / 32;
     const uint64_t stages = (n + kStageRecs - 1) / kStageRecs;
     auto issue = [&](uint64_t c, int slot) {
+        if(c == drop_stage) return;      // failure-path test: this stage's copy never comes
         const uint64_t first = c * kStageRecs;
         const uint64_t left = n - first;
         const uint32_t bytes = (uint32_t)(left < (uint64_t)kStageRecs ? left : (uint64_t)kStageRecs) * (uint32_t)sizeof(float4);
@@ -286,12 +288,13 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
         // Let the copies still in flight land before the CTA's shared memory
         // is released: those of iterations it .. it + kStages - 1 (the refill
         // of the aborted iteration was not issued).
-        volatile int keep_waiting = 0;
+        // Each wait is bounded on its own; a copy that was never issued (or
+        // never lands) costs one more timeout.
         for(int i = it; i < it + kStages; i++) {
             if(blockIdx.x + (uint64_t)i * gridDim.x >= stages) break;
-            if(!mbar_wait_bounded(smem_u32(&s_full[i % kStages]), (uint32_t)(i / kStages) & 1u, &keep_waiting,
-                                  kAccWaitCycles))
-                break;
+            volatile int keep_waiting = 0;
+            mbar_wait_bounded(smem_u32(&s_full[i % kStages]), (uint32_t)(i / kStages) & 1u, &keep_waiting,
+                              kAccWaitCycles);
         }
     }
     __syncthreads();
@@ -1015,7 +1018,7 @@ rtacx_status precision_accumulate(Context& ctx, const void* samples, uint64_t n,
             const uint32_t blocks = (uint32_t)std::min<uint64_t>(stages, (uint64_t)ctx.sm_count * ctx.acc_staged_blocks[m]);
             void* args[] = {(void*)&samples, (void*)&n, (void*)&ctx.bin, (void*)&ctx.d_bearings, (void*)&ctx.nB,
                             (void*)&ctx.d_lut, (void*)&ctx.lut_cells, (void*)&ctx.lut_origin, (void*)&ctx.lut_scale,
-                            (void*)&ctx.d_G, (void*)&ctx.d_flags, (void*)&ctx.d_err};
+                            (void*)&ctx.d_G, (void*)&ctx.d_flags, (void*)&ctx.d_err, (void*)&ctx.diag_drop_stage};
             RTACX_CUDA(cudaLaunchKernel(accumulate_staged_kernel(m), dim3(blocks), dim3(kStagedThreads), args,
                                         ctx.acc_staged_smem, stream));
             return RTACX_OK;
