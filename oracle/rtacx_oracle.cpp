@@ -628,8 +628,9 @@ void rtacx_oracle_make_samples(const float* hits, uint64_t n, const float* R, co
 }
 
 // Rasteriser oracle (see rtacx_rasterize): identical integer coverage,
-// top-left rule, double depth rounded to float and (depth, triangle) ties as
-// the kernel; varyings and the fragment arithmetic in double. out: W*H*4
+// top-left rule, the same float depth plane (slopes and anchor value formed
+// per triangle in double, two float FMAs per pixel) and (depth, triangle)
+// ties as the kernel; varyings and the fragment arithmetic in double. out: W*H*4
 // floats, rows bottom-up; winner (optional): triangle per pixel or -1.
 void rtacx_oracle_rasterize(const float* vtx, const float* nrm, const uint32_t* tris, uint32_t nv, uint32_t nt,
                             const float* L, const float* S, const float* origin, uint32_t W, uint32_t H,
@@ -679,6 +680,15 @@ void rtacx_oracle_rasterize(const float* vtx, const float* nrm, const uint32_t* 
         const long long area = (p[1]->X - p[0]->X) * (p[2]->Y - p[0]->Y) - (p[1]->Y - p[0]->Y) * (p[2]->X - p[0]->X);
         if(area == 0) continue;
         const int o0 = 0, o1 = area > 0 ? 1 : 2, o2 = area > 0 ? 2 : 1;
+        // depth plane anchored at vertex 0 (the kernel's depth_plane)
+        const double A = (double)(area > 0 ? area : -area);
+        const double z0 = p[0]->z, z1 = p[o1]->z, z2 = p[o2]->z;
+        const double dy21 = (double)(p[o2]->Y - p[o1]->Y), dy02 = (double)(p[0]->Y - p[o2]->Y), dy10 = (double)(p[o1]->Y - p[0]->Y);
+        const double dx21 = (double)(p[o2]->X - p[o1]->X), dx02 = (double)(p[0]->X - p[o2]->X), dx10 = (double)(p[o1]->X - p[0]->X);
+        double sx = dy21 * z0; sx = sx + dy02 * z1; sx = sx + dy10 * z2;
+        double sy = dx21 * z0; sy = sy + dx02 * z1; sy = sy + dx10 * z2;
+        const float gx = (float)(-0.5 * (sx / A)), gy = (float)(0.5 * (sy / A));
+        const float d0 = (float)(0.5 * z0 + 0.5);
         long long minX = std::min({p[0]->X, p[1]->X, p[2]->X}), maxX = std::max({p[0]->X, p[1]->X, p[2]->X});
         long long minY = std::min({p[0]->Y, p[1]->Y, p[2]->Y}), maxY = std::max({p[0]->Y, p[1]->Y, p[2]->Y});
         const long long i0 = std::max(0ll, (minX - 128 + 255) / 256);
@@ -695,14 +705,8 @@ void rtacx_oracle_rasterize(const float* vtx, const float* nrm, const uint32_t* 
                 if(e0 == 0 && !top_left(p[o1]->X, p[o1]->Y, p[o2]->X, p[o2]->Y)) continue;
                 if(e1 == 0 && !top_left(p[o2]->X, p[o2]->Y, p[o0]->X, p[o0]->Y)) continue;
                 if(e2 == 0 && !top_left(p[o0]->X, p[o0]->Y, p[o1]->X, p[o1]->Y)) continue;
-                const double ar = (double)(e0 + e1 + e2);
-                double num = (double)e0 * (double)p[o0]->z;
-                num = num + (double)e1 * (double)p[o1]->z;
-                num = num + (double)e2 * (double)p[o2]->z;
-                const double zn = num / ar;
-                const double depth = 0.5 * zn + 0.5;
-                if(!(depth >= 0.0 && depth <= 1.0)) continue;
-                const float d = (float)depth;
+                const float d = std::fma(gx, (float)(px - p[0]->X), std::fma(gy, (float)(py - p[0]->Y), d0));
+                if(!(d >= 0.0f && d <= 1.0f)) continue;
                 uint32_t bits;
                 std::memcpy(&bits, &d, 4);
                 const unsigned long long w = ((unsigned long long)bits << 32) | t;

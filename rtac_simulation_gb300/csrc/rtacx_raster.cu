@@ -98,8 +98,29 @@ struct Tri {
     long long X[3], Y[3];
     float z[3];
     long long area;
+    float gx, gy, d0;     // depth plane: depth = d0 + gx (px - X0) + gy (py - Y0)
     bool ok;
 };
+
+// Depth plane of a triangle, anchored at vertex 0. The window depth
+// 0.5 zn + 0.5, with zn the barycentric interpolation of the vertices' NDC
+// depths (e0 z0 + e1 z1 + e2 z2) / (e0 + e1 + e2), is linear in the pixel
+// position; its slopes and its value at vertex 0 are formed once per
+// triangle in FP64 with explicitly rounded operations and rounded to float,
+// so each pixel evaluates it with two float FMAs (the host oracle restates
+// the same operations). o1, o2: the CCW order of vertices 1 and 2.
+__device__ __forceinline__ void depth_plane(Tri& T, int o1, int o2)
+{
+    const double A = (double)(T.area > 0 ? T.area : -T.area);
+    const double z0 = T.z[0], z1 = T.z[o1], z2 = T.z[o2];
+    const double dy21 = (double)(T.Y[o2] - T.Y[o1]), dy02 = (double)(T.Y[0] - T.Y[o2]), dy10 = (double)(T.Y[o1] - T.Y[0]);
+    const double dx21 = (double)(T.X[o2] - T.X[o1]), dx02 = (double)(T.X[0] - T.X[o2]), dx10 = (double)(T.X[o1] - T.X[0]);
+    const double sx = __dadd_rn(__dadd_rn(__dmul_rn(dy21, z0), __dmul_rn(dy02, z1)), __dmul_rn(dy10, z2));
+    const double sy = __dadd_rn(__dadd_rn(__dmul_rn(dx21, z0), __dmul_rn(dx02, z1)), __dmul_rn(dx10, z2));
+    T.gx = __double2float_rn(__dmul_rn(-0.5, __ddiv_rn(sx, A)));
+    T.gy = __double2float_rn(__dmul_rn(0.5, __ddiv_rn(sy, A)));
+    T.d0 = __double2float_rn(__dadd_rn(__dmul_rn(0.5, z0), 0.5));
+}
 
 __device__ __forceinline__ Tri load_tri(const RasterVertex* __restrict__ V, const uint32_t* __restrict__ tris, uint32_t t,
                                         uint32_t nv)
@@ -115,6 +136,7 @@ __device__ __forceinline__ Tri load_tri(const RasterVertex* __restrict__ V, cons
     }
     T.area = (T.X[1] - T.X[0]) * (T.Y[2] - T.Y[0]) - (T.Y[1] - T.Y[0]) * (T.X[2] - T.X[0]);
     T.ok = T.area != 0;
+    if(T.ok) depth_plane(T, T.area > 0 ? 1 : 2, T.area > 0 ? 2 : 1);
     return T;
 }
 
@@ -143,13 +165,8 @@ __device__ __forceinline__ unsigned long long shade_test(const Tri& T, int o0, i
     if(e0 == 0 && !top_left(T.X[o1], T.Y[o1], T.X[o2], T.Y[o2])) return kEmpty;
     if(e1 == 0 && !top_left(T.X[o2], T.Y[o2], T.X[o0], T.Y[o0])) return kEmpty;
     if(e2 == 0 && !top_left(T.X[o0], T.Y[o0], T.X[o1], T.Y[o1])) return kEmpty;
-    const double area = (double)(e0 + e1 + e2);
-    const double num = __dadd_rn(__dadd_rn(__dmul_rn((double)e0, (double)T.z[o0]), __dmul_rn((double)e1, (double)T.z[o1])),
-                                 __dmul_rn((double)e2, (double)T.z[o2]));
-    const double zn = __ddiv_rn(num, area);
-    const double depth = __dadd_rn(__dmul_rn(0.5, zn), 0.5);
-    if(!(depth >= 0.0 && depth <= 1.0)) return kEmpty;
-    const float d = (float)depth;
+    const float d = fmaf(T.gx, (float)(px - T.X[0]), fmaf(T.gy, (float)(py - T.Y[0]), T.d0));
+    if(!(d >= 0.0f && d <= 1.0f)) return kEmpty;
     return ((unsigned long long)__float_as_uint(d) << 32) | t;
 }
 
@@ -223,13 +240,16 @@ __global__ void k_rast_resolve(const RasterVertex* __restrict__ V, const uint32_
         const double l0 = (double)edge(b.X, b.Y, c.X, c.Y, px, py);
         const double l1 = (double)edge(c.X, c.Y, a.X, a.Y, px, py);
         const double l2 = (double)edge(a.X, a.Y, b.X, b.Y, px, py);
-        // perspective-correct weights
+        // perspective-correct weights, normalised by one reciprocal; the
+        // receiver-frame delta in FP64 (the carrier phase needs the range to
+        // ~1e-8 relative), the reflectance in float
         const double w0 = l0 * a.inv_w, w1 = l1 * b.inv_w, w2 = l2 * c.inv_w;
-        const double s = w0 + w1 + w2;
-        const double dx = (w0 * a.dx + w1 * b.dx + w2 * c.dx) / s;
-        const double dy = (w0 * a.dy + w1 * b.dy + w2 * c.dy) / s;
-        const double dz = (w0 * a.dz + w1 * b.dz + w2 * c.dz) / s;
-        const double refl = (w0 * a.refl + w1 * b.refl + w2 * c.refl) / s;
+        const double rs = __drcp_rn(w0 + w1 + w2);
+        const double b0 = w0 * rs, b1 = w1 * rs, b2 = w2 * rs;
+        const double dx = fma(b0, a.dx, fma(b1, b.dx, b2 * c.dx));
+        const double dy = fma(b0, a.dy, fma(b1, b.dy, b2 * c.dy));
+        const double dz = fma(b0, a.dz, fma(b1, b.dz, b2 * c.dz));
+        const float refl = fmaf((float)b0, a.refl, fmaf((float)b1, b.refl, (float)b2 * c.refl));
         const double r2 = dx * dx + dy * dy + dz * dz;
         const double range = sqrt(r2);
         const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
@@ -240,7 +260,7 @@ __global__ void k_rast_resolve(const RasterVertex* __restrict__ V, const uint32_
         const float frac = (float)(cyc - rint(cyc));
         float sn, cs;
         sincosf(frac * 6.28318530717958647692f, &sn, &cs);
-        const float amp = (float)(refl / r2) / cosf(bearing) / cosf(elevation);
+        const float amp = refl / (float)r2 / cosf(bearing) / cosf(elevation);
         res = make_float4(amp * cs, amp * sn, (float)range, bearing);
     }
     out[idx] = res;
