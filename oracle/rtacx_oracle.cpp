@@ -629,7 +629,7 @@ void rtacx_oracle_make_samples(const float* hits, uint64_t n, const float* R, co
 
 // Rasteriser oracle (see rtacx_rasterize): identical integer coverage,
 // top-left rule, the same float depth plane (slopes and anchor value formed
-// per triangle in double, two float FMAs per pixel) and (depth, triangle)
+// per triangle in float, two float FMAs per pixel) and (depth, triangle)
 // ties as the kernel; varyings and the fragment arithmetic in double. out: W*H*4
 // floats, rows bottom-up; winner (optional): triangle per pixel or -1.
 void rtacx_oracle_rasterize(const float* vtx, const float* nrm, const uint32_t* tris, uint32_t nv, uint32_t nt,
@@ -680,15 +680,15 @@ void rtacx_oracle_rasterize(const float* vtx, const float* nrm, const uint32_t* 
         const long long area = (p[1]->X - p[0]->X) * (p[2]->Y - p[0]->Y) - (p[1]->Y - p[0]->Y) * (p[2]->X - p[0]->X);
         if(area == 0) continue;
         const int o0 = 0, o1 = area > 0 ? 1 : 2, o2 = area > 0 ? 2 : 1;
-        // depth plane anchored at vertex 0 (the kernel's depth_plane)
-        const double A = (double)(area > 0 ? area : -area);
-        const double z0 = p[0]->z, z1 = p[o1]->z, z2 = p[o2]->z;
-        const double dy21 = (double)(p[o2]->Y - p[o1]->Y), dy02 = (double)(p[0]->Y - p[o2]->Y), dy10 = (double)(p[o1]->Y - p[0]->Y);
-        const double dx21 = (double)(p[o2]->X - p[o1]->X), dx02 = (double)(p[0]->X - p[o2]->X), dx10 = (double)(p[o1]->X - p[0]->X);
-        double sx = dy21 * z0; sx = sx + dy02 * z1; sx = sx + dy10 * z2;
-        double sy = dx21 * z0; sy = sy + dx02 * z1; sy = sy + dx10 * z2;
-        const float gx = (float)(-0.5 * (sx / A)), gy = (float)(0.5 * (sy / A));
-        const float d0 = (float)(0.5 * z0 + 0.5);
+        // depth plane anchored at vertex 0 (the kernel's depth_plane), in float
+        const float A = (float)(area > 0 ? area : -area);
+        const float z0 = p[0]->z, z1 = p[o1]->z, z2 = p[o2]->z;
+        const float dy21 = (float)(p[o2]->Y - p[o1]->Y), dy02 = (float)(p[0]->Y - p[o2]->Y), dy10 = (float)(p[o1]->Y - p[0]->Y);
+        const float dx21 = (float)(p[o2]->X - p[o1]->X), dx02 = (float)(p[0]->X - p[o2]->X), dx10 = (float)(p[o1]->X - p[0]->X);
+        float sx = dy21 * z0; sx = sx + dy02 * z1; sx = sx + dy10 * z2;
+        float sy = dx21 * z0; sy = sy + dx02 * z1; sy = sy + dx10 * z2;
+        const float gx = -0.5f * (sx / A), gy = 0.5f * (sy / A);
+        const float d0 = 0.5f * z0 + 0.5f;
         long long minX = std::min({p[0]->X, p[1]->X, p[2]->X}), maxX = std::max({p[0]->X, p[1]->X, p[2]->X});
         long long minY = std::min({p[0]->Y, p[1]->Y, p[2]->Y}), maxY = std::max({p[0]->Y, p[1]->Y, p[2]->Y});
         const long long i0 = std::max(0ll, (minX - 128 + 255) / 256);

@@ -106,20 +106,21 @@ struct Tri {
 // 0.5 zn + 0.5, with zn the barycentric interpolation of the vertices' NDC
 // depths (e0 z0 + e1 z1 + e2 z2) / (e0 + e1 + e2), is linear in the pixel
 // position; its slopes and its value at vertex 0 are formed once per
-// triangle in FP64 with explicitly rounded operations and rounded to float,
-// so each pixel evaluates it with two float FMAs (the host oracle restates
-// the same operations). o1, o2: the CCW order of vertices 1 and 2.
+// triangle in float with explicitly rounded operations (the coordinate
+// differences are integers below 2^24, exact in float), so each pixel
+// evaluates it with two float FMAs; the host oracle restates the same
+// operations. o1, o2: the CCW order of vertices 1 and 2.
 __device__ __forceinline__ void depth_plane(Tri& T, int o1, int o2)
 {
-    const double A = (double)(T.area > 0 ? T.area : -T.area);
-    const double z0 = T.z[0], z1 = T.z[o1], z2 = T.z[o2];
-    const double dy21 = (double)(T.Y[o2] - T.Y[o1]), dy02 = (double)(T.Y[0] - T.Y[o2]), dy10 = (double)(T.Y[o1] - T.Y[0]);
-    const double dx21 = (double)(T.X[o2] - T.X[o1]), dx02 = (double)(T.X[0] - T.X[o2]), dx10 = (double)(T.X[o1] - T.X[0]);
-    const double sx = __dadd_rn(__dadd_rn(__dmul_rn(dy21, z0), __dmul_rn(dy02, z1)), __dmul_rn(dy10, z2));
-    const double sy = __dadd_rn(__dadd_rn(__dmul_rn(dx21, z0), __dmul_rn(dx02, z1)), __dmul_rn(dx10, z2));
-    T.gx = __double2float_rn(__dmul_rn(-0.5, __ddiv_rn(sx, A)));
-    T.gy = __double2float_rn(__dmul_rn(0.5, __ddiv_rn(sy, A)));
-    T.d0 = __double2float_rn(__dadd_rn(__dmul_rn(0.5, z0), 0.5));
+    const float A = __ll2float_rn(T.area > 0 ? T.area : -T.area);
+    const float z0 = T.z[0], z1 = T.z[o1], z2 = T.z[o2];
+    const float dy21 = (float)(T.Y[o2] - T.Y[o1]), dy02 = (float)(T.Y[0] - T.Y[o2]), dy10 = (float)(T.Y[o1] - T.Y[0]);
+    const float dx21 = (float)(T.X[o2] - T.X[o1]), dx02 = (float)(T.X[0] - T.X[o2]), dx10 = (float)(T.X[o1] - T.X[0]);
+    const float sx = __fadd_rn(__fadd_rn(__fmul_rn(dy21, z0), __fmul_rn(dy02, z1)), __fmul_rn(dy10, z2));
+    const float sy = __fadd_rn(__fadd_rn(__fmul_rn(dx21, z0), __fmul_rn(dx02, z1)), __fmul_rn(dx10, z2));
+    T.gx = __fmul_rn(-0.5f, __fdiv_rn(sx, A));
+    T.gy = __fmul_rn(0.5f, __fdiv_rn(sy, A));
+    T.d0 = __fadd_rn(__fmul_rn(0.5f, z0), 0.5f);
 }
 
 __device__ __forceinline__ Tri load_tri(const RasterVertex* __restrict__ V, const uint32_t* __restrict__ tris, uint32_t t,
