@@ -301,6 +301,7 @@ class SensorInstance2D_Complex : public SensorInstance {
     SensorInfo2D::ConstPtr info_;
     DeviceVector<SimSample2D> receivedSamples_;
     DeviceVector<Complex> sensorOutput_;
+    bool texturePsf_ = false;
 protected:
     SensorInstance2D_Complex(const SensorInfo2D::ConstPtr& info, float c)
         : SensorInstance(info->ranges(), info->waveform(), c), info_(info)
@@ -318,10 +319,19 @@ private:
         s.pulse = reinterpret_cast<const float*>(pulse.data()); s.pulse_len = (uint32_t)pulse.size();
         s.beam = beam.data().data(); s.beam_len = beam.size(); s.beam_span = beam.span();
         s.bearings = info_->bearings().data(); s.bearing_count = (uint32_t)info_->bearings().size();
+        s.flags = texturePsf_ ? RTACX_FLAG_TEXTURE_PSF : 0u;
         check(rtacx_configure_2d(ctx_, &s));
     }
 public:
     using Ptr = std::shared_ptr<SensorInstance2D_Complex>;
+    // Evaluate the PSF on the texture unit as the reference's
+    // SensorInstance2D does (RTACX_FLAG_TEXTURE_PSF): the ping then matches
+    // the reference's own to float round-off. Off: exact bilinear weights.
+    void set_texture_psf(bool on)
+    {
+        texturePsf_ = on;
+        this->set_ranges(ranges_);
+    }
     static Ptr Create(const SensorInfo2D::ConstPtr& info, float soundCelerity = 1500.0f)
     {
         return Ptr(new SensorInstance2D_Complex(info, soundCelerity));

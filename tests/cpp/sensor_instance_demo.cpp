@@ -67,6 +67,7 @@ int main(int argc, char** argv)
             }
             else {
                 auto sensor = SensorInstance2D_Complex::Create(SensorInfo2D::ConstPtr(info), (float)scalars["celerity"]);
+                if(scalars["texture_psf"] != 0.0) sensor->set_texture_psf(true);
                 sensor->set_sample_count((unsigned)n);
                 sensor->samples().copy_from_host(reinterpret_cast<const SimSample2D*>(raw.data()), n);
                 sensor->compute_output();

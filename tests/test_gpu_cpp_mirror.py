@@ -18,13 +18,14 @@ if not torch.cuda.is_available():
     pytest.skip("needs a GPU", allow_module_level=True)
 
 
-def run_demo(tmp_path, wk, frequency, duration, fixed, sink=None):
+def run_demo(tmp_path, wk, frequency, duration, fixed, sink=None, texture_psf=False):
     if not build.DEMO_BIN.exists():
         build.build_demo()
     s = wk.sensor
     lines = [f"dims {wk.dims}", f"range_min {s['range_min']!r}", f"range_max {s['range_max']!r}",
              f"range_count {s['range_count']}", f"celerity {s['sound_celerity']!r}", f"frequency {frequency!r}",
-             f"duration {duration!r}", f"fixed {1 if fixed else 0}", "oversampling 8"]
+             f"duration {duration!r}", f"fixed {1 if fixed else 0}", "oversampling 8",
+             f"texture_psf {1 if texture_psf else 0}"]
     if wk.dims == 2:
         lines.append(f"beam_span {s['beam_span']!r}")
         lines.append("beam %d %s" % (len(s["beam"]), " ".join(repr(float(x)) for x in s["beam"])))
@@ -66,3 +67,14 @@ def test_cpp_file_sink_records(tmp_path, oracle):
         np.testing.assert_array_equal(r["bearings"], np.asarray(wk.sensor["bearings"], np.float32))
         assert np.linalg.norm(r["ping"] - got) <= 1e-6 * np.linalg.norm(got)
         assert r["range_min"] == np.float32(wk.sensor["range_min"]) and r["range_max"] == np.float32(wk.sensor["range_max"])
+
+
+def test_cpp_mirror_2d_texture_psf_matches_reference_texture_model(tmp_path, oracle):
+    """set_texture_psf(true) on the C++ mirror: the PSF is fetched from a
+    texture as the reference's SensorInstance2D does, and the ping matches
+    the oracle's texture-unit model (which reproduces the reference's own
+    kernel, tests/test_oracle_golden.py) to float round-off."""
+    wk = wl.oculus_reference_2d(n_samples=20000)
+    got = run_demo(tmp_path, wk, wk.meta["frequency"], 0.0, False, texture_psf=True).astype(np.complex128)
+    want = oracle.reduce(wk.samples, wk.sensor, mode=2)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) <= 1e-6
