@@ -103,4 +103,6 @@ def main(out_dir: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "gpurun_out")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_ref_pings.py OUT_DIR")
+    main(sys.argv[1])
