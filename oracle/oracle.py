@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline / reference arm of bench.py, never by the product package.
 Parity status: pinned for the range key and pulse table (the reference's own
-headers) and for the 2D reduction (the reference's own kernel run on a GB300:
+headers), the receiver directivity tables (the reference's own
+src/Directivity.cpp, bit for bit) and for the 2D reduction (the reference's own kernel run on a GB300:
 reduce(mode=2) reproduces its pings, tests/golden/ref_pings_2d.npz); the 1D
 reduction is a restatement.
 """
@@ -223,3 +224,61 @@ def rasterize(vertices, normals, triangles, world_to_local, world_to_screen, ori
                                   L.ctypes.data, S.ctypes.data, o.ctypes.data, width, height, carrier_hz, c,
                                   out.ctypes.data, win.ctypes.data)
     return out, win
+
+
+def directivity_table(kind: str, params, baffle: str = "none", oversampling: int = 1) -> np.ndarray:
+    """Receiver directivity table (float32 [height][width]) as the reference
+    builds it on the host: kind "RECT" (params width, height, wavelength;
+    Directivity::rectangle_antenna, src/Directivity.cpp:59-101) or "DISK"
+    (params diameter, wavelength; Directivity::disk_antenna,
+    src/Directivity.cpp:109-166). Table sizes, the float / double mix and the
+    single-sided baffle follow those lines. Where disk_antenna's
+    sqrt(1 - y2 - z2) cancels the reference's result depends on its libm's
+    last bit (a NaN or a tiny x, both below the 1e-2 cut-off); the exact-math
+    limit is taken here, x = 0 and a value of 0."""
+    from scipy.special import j1
+
+    f32 = np.float32
+    os_ = int(oversampling)
+    if kind == "RECT":
+        width, height, wl = (f32(p) for p in params)
+        half_os = float(f32(f32(0.5) * f32(os_)) * f32(2))          # 0.5f * oversampling * 2 in float
+        Nw = 2 * int(half_os * np.pi * float(width) / float(wl) + 1)
+        Nh = 2 * int(half_os * np.pi * float(height) / float(wl) + 1)
+        elev = np.pi * np.arange(Nh, dtype=np.float64) / Nh
+        bear = np.pi * np.arange(Nw, dtype=np.float64) / Nw
+        ke = np.pi * float(height) / float(wl)
+        kb = np.pi * float(width) / float(wl)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            e = (np.sin(ke * np.sin(elev)) / (ke * np.sin(elev))).astype(f32)
+            b = (np.sin(kb * np.sin(bear)) / (kb * np.sin(bear))).astype(f32)
+        e[0] = f32(1)
+        b[0] = f32(1)
+        data = (e[:, None] * b[None, :]).astype(f32)
+    elif kind == "DISK":
+        dia, wl = (f32(p) for p in params)
+        period = f32(f32(f32(2) * wl) / dia)
+        N = max(64, 8 * int(os_ * np.pi / float(period)))
+        elev = (np.pi * np.arange(N, dtype=np.float64) / N)[:, None]
+        bear = (np.pi * np.arange(N, dtype=np.float64) / N)[None, :]
+        cose2, sine2 = np.cos(elev) ** 2, np.sin(elev) ** 2
+        cosb2, sinb2 = np.cos(bear) ** 2, np.sin(bear) ** 2
+        with np.errstate(divide="ignore", invalid="ignore"):
+            denom = 1.0 - sine2 * sinb2
+            y2 = cose2 * sinb2 / denom
+            z2 = sine2 * cosb2 / denom
+            s = 1.0 - y2 - z2
+            x = np.where((denom > 0.0) & (s > 0.0), np.sqrt(np.where(s > 0.0, s, 0.0)), 0.0)
+            x = np.where((elev > 0.5 * np.pi) | (bear > 0.5 * np.pi), -x, x)
+            a = (np.pi * float(dia) / float(wl)) * np.sin(np.arctan2(np.sqrt(y2 + z2), x))
+            v = np.where(np.abs(a) < 1.0e-3, 1.0, 2.0 * j1(a) / a)
+        data = np.where(np.abs(x) < 1.0e-2, 0.0, v).astype(f32)
+    else:
+        raise ValueError(f"unknown directivity kind {kind!r}")
+    if baffle == "single-sided":
+        H, W = data.shape
+        data[H // 2 + 1:, :] = 0
+        data[:, W // 2 + 1:] = 0
+    elif baffle != "none":
+        raise ValueError(f"unsupported baffle mode {baffle!r}")
+    return data

@@ -1,8 +1,9 @@
 """Pin the oracle against the reference's own arithmetic (tests/golden/).
 
-The golden vectors come from compiling the reference's Binner::Key and
-Waveform_Sine (tests/golden/make_golden.py); the oracle's range key and the
-package's Waveform_Sine restatement must reproduce them bit for bit.
+The golden vectors come from compiling the reference's Binner::Key,
+Waveform_Sine and receiver directivity builders (tests/golden/make_golden.py);
+the oracle's range key and directivity tables and the package's Waveform_Sine
+restatement must reproduce them bit for bit.
 """
 import json
 from pathlib import Path
@@ -50,6 +51,29 @@ def test_key_outside_int_range_saturates(oracle):
     assert list(keys[:4]) == [0xFFFFFFFF] * 4
     assert list(side[:4]) == [1, -1, 1, -1]
     assert keys[4] == 0 and side[4] == 0
+
+
+def test_directivity_tables_bit_exact(oracle):
+    # src/Directivity.cpp rectangle_antenna / disk_antenna, single-sided and
+    # unbaffled, several oversamplings. The reference's disk tables hold NaNs
+    # where sqrt(1 - y2 - z2) cancels (its libm's last bit decides); the
+    # oracle keeps the exact-math limit there, 0, like the device builder.
+    cases = json.loads((GOLDEN / "ref_directivity.json").read_text())["cases"]
+    assert {c["kind"] for c in cases} == {"RECT", "DISK"}
+    for c in cases:
+        par = [float.fromhex(x) for x in c["params"]]
+        got = oracle.directivity_table(c["kind"], par, c["baffle"], c["oversampling"])
+        want = np.array([float.fromhex(x) for x in c["values"]], np.float32).reshape(c["height"], c["width"])
+        assert got.shape == want.shape
+        assert np.isfinite(got).all()
+        np.testing.assert_array_equal(got, np.where(np.isnan(want), np.float32(0), want))
+
+
+def test_directivity_table_rejects_unknown_modes(oracle):
+    with pytest.raises(ValueError):
+        oracle.directivity_table("RECT", [0.01, 0.01, 0.00125], "cardioid", 1)
+    with pytest.raises(ValueError):
+        oracle.directivity_table("HEX", [0.01, 0.00125])
 
 
 def test_waveform_sine_matches_reference():
