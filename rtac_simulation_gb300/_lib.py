@@ -112,6 +112,18 @@ class Receiver(ctypes.Structure):
                 ("directivity_height", _U32), ("carrier_hz", ctypes.c_double), ("flags", _U32)]
 
 
+def directivity_table_size(kind: int, params):
+    """(height, width) of the table rtacx_directivity_table builds for these
+    parameters (a host-only query, no device work)."""
+    lib = load()
+    p = (ctypes.c_float * len(params))(*params)
+    w, h = _U32(), _U32()
+    st = lib.rtacx_directivity_table(kind, p, None, ctypes.byref(w), ctypes.byref(h), None)
+    if st != RTACX_OK:
+        raise RtacxError(st, "rtacx_directivity_table (size) failed")
+    return h.value, w.value
+
+
 def directivity_table(kind: int, params, stream=None):
     """Device directivity table (torch tensor [height][width]) built by
     rtacx_directivity_table."""
@@ -119,10 +131,8 @@ def directivity_table(kind: int, params, stream=None):
     lib = load()
     p = (ctypes.c_float * len(params))(*params)
     w, h = _U32(), _U32()
-    st = lib.rtacx_directivity_table(kind, p, None, ctypes.byref(w), ctypes.byref(h), None)
-    if st != RTACX_OK:
-        raise RtacxError(st, "rtacx_directivity_table (size) failed")
-    out = torch.empty((h.value, w.value), dtype=torch.float32, device="cuda")
+    rows, cols = directivity_table_size(kind, params)
+    out = torch.empty((rows, cols), dtype=torch.float32, device="cuda")
     st = lib.rtacx_directivity_table(kind, p, out.data_ptr(), ctypes.byref(w), ctypes.byref(h), _stream(stream))
     if st != RTACX_OK:
         raise RtacxError(st, "rtacx_directivity_table failed")

@@ -226,20 +226,29 @@ extern "C" rtacx_status rtacx_directivity_table(int kind, const float* params, f
                                                 uint32_t* height, void* stream)
 {
     if(!params || !width || !height) return RTACX_ERR_INVALID_ARGUMENT;
+    // Table sides are formed in double and bounded before the conversion to
+    // unsigned (an out-of-range conversion is undefined): at most 2^26 texels.
+    constexpr double kMaxSide = (double)(1u << 26);
     uint32_t W, H;
     if(kind == RTACX_DIRECTIVITY_RECTANGLE) {
         const float w = params[0], h = params[1], l = params[2], os = params[4];
         if(!(w > 0.0f && h > 0.0f && l > 0.0f && os >= 1.0f)) return RTACX_ERR_INVALID_ARGUMENT;
+        if(!(os < 65536.0f)) return RTACX_ERR_UNSUPPORTED;
         const unsigned int o = (unsigned int)os;
         // Nw = 2 * (unsigned)(0.5f * oversampling * 2 * M_PI * width / wavelength + 1)
-        W = 2u * (unsigned int)((double)(0.5f * o * 2) * kPi * w / l + 1);
-        H = 2u * (unsigned int)((double)(0.5f * o * 2) * kPi * h / l + 1);
+        const double hw = (double)(0.5f * o * 2) * kPi * w / l + 1, hh = (double)(0.5f * o * 2) * kPi * h / l + 1;
+        if(!(hw < kMaxSide && hh < kMaxSide)) return RTACX_ERR_UNSUPPORTED;
+        W = 2u * (unsigned int)hw;
+        H = 2u * (unsigned int)hh;
     }
     else if(kind == RTACX_DIRECTIVITY_DISK) {
         const float dia = params[0], l = params[1], os = params[3];
         if(!(dia > 0.0f && l > 0.0f && os >= 1.0f)) return RTACX_ERR_INVALID_ARGUMENT;
+        if(!(os < 65536.0f)) return RTACX_ERR_UNSUPPORTED;
         const float period = 2.0f * l / dia;
-        W = H = std::max(64u, 8u * (unsigned int)((unsigned int)os * kPi / period));
+        const double q = (unsigned int)os * kPi / period;
+        if(!(q < kMaxSide)) return RTACX_ERR_UNSUPPORTED;
+        W = H = std::max(64u, 8u * (unsigned int)q);
     }
     else return RTACX_ERR_INVALID_ARGUMENT;
     if((uint64_t)W * H > (1u << 26)) return RTACX_ERR_UNSUPPORTED;

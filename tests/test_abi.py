@@ -80,3 +80,36 @@ def test_create_without_gpu_fails_cleanly(lib):
     h = ctypes.c_void_p()
     assert so.rtacx_create(ctypes.byref(h), 0) != lib.RTACX_OK
     assert not h.value
+
+
+def test_directivity_table_sizes_without_a_gpu(lib):
+    # The size query does no device work: the table sides follow the
+    # reference builders (src/Directivity.cpp:63-64, 113-114), checked against
+    # the tables the reference's own code produced.
+    import json
+    from pathlib import Path
+    cases = json.loads((Path(__file__).resolve().parent / "golden" / "ref_directivity.json").read_text())["cases"]
+    for c in cases:
+        par = [float.fromhex(x) for x in c["params"]]
+        baffle = 1.0 if c["baffle"] == "single-sided" else 0.0
+        kind = lib.RTACX_DIRECTIVITY_RECTANGLE if c["kind"] == "RECT" else lib.RTACX_DIRECTIVITY_DISK
+        assert lib.directivity_table_size(kind, par + [baffle, float(c["oversampling"])]) == (c["height"], c["width"])
+
+
+def test_directivity_table_rejects_bad_parameters(lib):
+    rect, disk = lib.RTACX_DIRECTIVITY_RECTANGLE, lib.RTACX_DIRECTIVITY_DISK
+    for kind, par, status in [
+        (rect, [0.0, 0.01, 0.00125, 0.0, 1.0], lib.RTACX_ERR_INVALID_ARGUMENT),
+        (rect, [0.01, 0.01, 0.00125, 0.0, 0.5], lib.RTACX_ERR_INVALID_ARGUMENT),
+        (rect, [float("nan"), 0.01, 0.00125, 0.0, 1.0], lib.RTACX_ERR_INVALID_ARGUMENT),
+        (rect, [1e30, 0.01, 0.00125, 0.0, 1.0], lib.RTACX_ERR_UNSUPPORTED),
+        (rect, [0.01, 0.01, 0.00125, 0.0, 1e30], lib.RTACX_ERR_UNSUPPORTED),
+        (rect, [3.0, 3.0, 0.00125, 0.0, 1.0], lib.RTACX_ERR_UNSUPPORTED),
+        (disk, [1e30, 0.00125, 0.0, 1.0], lib.RTACX_ERR_UNSUPPORTED),
+        (disk, [0.1, 0.00125, 0.0, float("inf")], lib.RTACX_ERR_UNSUPPORTED),
+        (disk, [0.1, -1.0, 0.0, 1.0], lib.RTACX_ERR_INVALID_ARGUMENT),
+        (7, [0.1, 0.00125, 0.0, 1.0], lib.RTACX_ERR_INVALID_ARGUMENT),
+    ]:
+        with pytest.raises(lib.RtacxError) as e:
+            lib.directivity_table_size(kind, par)
+        assert e.value.status == status, (kind, par)
