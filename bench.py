@@ -443,13 +443,16 @@ def time_next_rows(torch, local, peaks, reps=20, warmup=3):
     rect = [1.56e-3, 8e-3, 1.25e-3, 1.0, 8.0]
     disk = [6e-3, 1.25e-3, 1.0, 8.0]
     tabs = {}
+    # The call includes the host size query and the output allocation.
+    bounds = {"rectangle": "launch (size query, allocation and one short kernel)",
+              "disk": "FP64 pipe (double sin, cos, atan2, sqrt and j1 per entry, as the reference builder; not profiled)"}
     for name, kind, par in (("rectangle", _lib.RTACX_DIRECTIVITY_RECTANGLE, rect),
                             ("disk", _lib.RTACX_DIRECTIVITY_DISK, disk)):
         t = timed(lambda: _lib.directivity_table(kind, par, stream=stream))
         tabs[name] = _lib.directivity_table(kind, par, stream=stream)
         e = tabs[name].numel()
         res[f"directivity_{name}"] = {"entries": e, "us_per_table": 1e6 * t, "entries_per_s": e / t,
-                                      "params": par, "bound": "launch (host size query + one kernel)"}
+                                      "params": par, "bound": bounds[name]}
 
     # Echo-sample epilogue on 2^24 hits.
     wk = workloads.oculus_reference_2d(n_samples=16)

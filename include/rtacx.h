@@ -255,7 +255,7 @@ rtacx_status rtacx_configure_receiver(rtacx_ctx* ctx, const rtacx_receiver* rece
 rtacx_status rtacx_make_samples(rtacx_ctx* ctx, const rtacx_echo* hits, uint64_t n, void* samples, void* stream);
 
 /* Receiver directivity tables of Directivity::rectangle_antenna and
- * Directivity::disk_antenna (src/Directivity.cpp:147-254), built on the
+ * Directivity::disk_antenna (src/Directivity.cpp:59-101, 109-166), built on the
  * device. params: rectangle {width, height, wavelength, baffle, oversampling},
  * disk {diameter, wavelength, baffle, oversampling} (baffle 0 none, 1
  * single-sided; lengths in one unit). Writes the table size; with out != NULL

@@ -12,12 +12,12 @@
 //   bearing = atan2(-ly, lx)
 // The directivity lookup is the reference's float texture with normalized
 // coordinates, linear filtering and mirror addressing
-// (src/Directivity.cpp:109-118, include/rtac_simulation/Directivity.h:30-34),
+// (src/Directivity.cpp:21-25, include/rtac_simulation/Directivity.h:30-34),
 // evaluated with exact bilinear weights.
 //
 // k_directivity_rect / k_directivity_disk build the receiver directivity
 // tables of Directivity::rectangle_antenna / disk_antenna
-// (src/Directivity.cpp:147-254) on the device, with the reference's float /
+// (src/Directivity.cpp:59-101, 109-166) on the device, with the reference's float /
 // double arithmetic.
 #include "rtacx_internal.cuh"
 

@@ -124,7 +124,7 @@ def main():
         dirs.append(dict(kind=kind, params=[f32hex(x) for x in par], baffle=baffle, oversampling=os_,
                          width=w, height=h, values=tok[3:]))
     (HERE / "ref_directivity.json").write_text(json.dumps(dict(
-        source="rtac_simulation src/Directivity.cpp:147-254 compiled by oracle/ref_build.sh", cases=dirs)))
+        source="rtac_simulation src/Directivity.cpp:59-166 compiled by oracle/ref_build.sh", cases=dirs)))
     print(f"wrote {len(key_cases)} key cases, {len(waves)} waveform cases, {len(dirs)} directivity tables")
 
 
