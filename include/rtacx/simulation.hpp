@@ -5,13 +5,13 @@
 // for the receiver path, so code written against the reference's
 // SensorInstance reads the same:
 //   Waveform_Sine        include/rtac_simulation/Waveform.h:96-138
-//   BeamDirectivity      include/rtac_simulation/BeamDirectivity.h:205-224
+//   BeamDirectivity      include/rtac_simulation/BeamDirectivity.h:52-104
 //                        (a table + span; the reference's SincFunction table
 //                        lives in non-vendored rtac_base)
-//   SensorInfo(2D)       include/rtac_simulation/SensorInfo.h:291-378
+//   SensorInfo(2D)       include/rtac_simulation/SensorInfo.h:18-104
 //   SensorInstance1D_Complex / SensorInstance2D_Complex
 //                        include/rtac_simulation/SensorInstance1D.h:72-110,
-//                        include/rtac_simulation/SensorInstance2D.h:312-364
+//                        include/rtac_simulation/SensorInstance2D.h:153-205
 // set_ranges() re-derives the adaptive pulse duration, the Binner margin
 // (c * duration) and the PSF tables exactly as SensorInstance::set_ranges
 // (src/SensorInstance.cu:23-34); compute_output() runs sort + bin + reduce in
@@ -221,7 +221,7 @@ public:
         soundCelerity_ = soundCelerity;
         this->set_ranges(ranges);
     }
-    void set_ranges(const Linspace& ranges)       // src/SensorInstance.cu:29-40
+    void set_ranges(const Linspace& ranges)       // src/SensorInstance.cu:23-34
     {
         ranges_ = ranges;
         if(!waveform_->fixed()) waveform_->set_duration(ranges.resolution() / soundCelerity_);
@@ -415,7 +415,7 @@ public:
     Ping2D get_ping() const { return Ping2D(this->ranges(), this->bearings(), this->output().data()); }
 };
 
-// Ping file sink (include/rtac_simulation/sinks/FileSink.h:12-31,
+// Ping file sink (include/rtac_simulation/sinks/FileSink.h:15-37,
 // src/sinks/FileSink.cpp:14-42): appends one record per set_output() call.
 // The reference serialises rtac_base's CudaPing2D, whose wire format lives in
 // the non-vendored rtac_base serialization; this sink writes its own

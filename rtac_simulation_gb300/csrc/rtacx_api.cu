@@ -116,7 +116,7 @@ struct Common {
 };
 
 // Validation and the parts shared by the 1D and 2D configurations: Binner
-// reconfiguration (src/SensorInstance.cu:32, src/Binner.cu:169-176), Key
+// reconfiguration (src/SensorInstance.cu:32, src/Binner.cu:15-22), Key
 // parameters, overlap, output range table, pulse table and per-row support.
 bool configure_common(Context& c, const Common& s, float pulse_scale)
 {

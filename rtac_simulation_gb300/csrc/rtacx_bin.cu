@@ -402,7 +402,7 @@ __device__ __forceinline__ uint32_t bin_count(const uint32_t* off, uint32_t nBB,
 
 // First / last non-empty range bin of row r's reference window
 // [max(0, r - ov), min(nR - 1, r + ov)]; returns false for the empty view
-// (no non-empty bin, or istart >= iend: src/Binner.cu:95-104).
+// (no non-empty bin, or istart >= iend: src/Binner.cu:90-102).
 __device__ __forceinline__ bool ref_window(const uint32_t* off, uint32_t nBB, uint32_t nR, int ov, int r,
                                            int& f, int& l)
 {

@@ -9,7 +9,7 @@
 //                      float atomic (red.global.add.v4.f32) into the pair
 //                      cell P[j][k]; non-empty range bins in a bitmap. No sort.
 //   k_prec_filter      row r's window by the reference rule
-//                      (src/Binner.cu:95-104) on the non-empty bitmap, then
+//                      (src/Binner.cu:90-102) on the non-empty bitmap, then
 //                      G'[r][k] = sum_t taps[t] G[r + t - c][k] over that
 //                      window, written as the bf16 A operand [hi | hi | lo]
 //                      of the three-term split product.
@@ -450,7 +450,7 @@ __device__ __forceinline__ bool bit_set(const uint32_t* bits, long long j)
     return (bits[j >> 5] >> (j & 31)) & 1u;
 }
 
-// Window of range row r by the reference rule (src/Binner.cu:95-104) on the
+// Window of range row r by the reference rule (src/Binner.cu:90-102) on the
 // non-empty bitmap: [max(0, r - ov), min(nR - 1, r + ov)] shrunk to its first
 // and last non-empty bins; {1, 0} (empty) when fewer than two are non-empty.
 __device__ __noinline__ int2 row_window(const uint32_t* __restrict__ nonempty, uint32_t nR, int ov, int r)

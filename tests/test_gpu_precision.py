@@ -283,7 +283,7 @@ def _bin_travel(oracle, sensor, r):
 
 def test_precision_all_out_of_range_and_single_bin_are_zero(oracle):
     """No in-range sample, or samples in one range bin only: every window is
-    the reference's empty view, so the ping is zero (src/Binner.cu:95-104)."""
+    the reference's empty view, so the ping is zero (src/Binner.cu:90-102)."""
     wk = _small_precision()
     ctx = precision_context(wk)
     smp = wk.samples.copy()

@@ -52,7 +52,7 @@ def test_segments_follow_sorted_keys(oracle):
 
 def test_single_nonempty_bin_gives_empty_windows(oracle):
     # do_make_bins: a window with exactly one non-empty bin shrinks to
-    # istart == iend and yields an empty view (src/Binner.cu:95-104).
+    # istart == iend and yields an empty view (src/Binner.cu:90-102).
     s = small_sensor()
     R = wl.linspace(s["range_min"], s["range_max"], s["range_count"])
     smp = samples2d([R[20]] * 3, 0.0, 1.0 + 1.0j)
