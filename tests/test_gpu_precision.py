@@ -375,9 +375,9 @@ def test_precision_partial_stage_and_unaligned_records(oracle, n):
 
 
 def test_precision_consecutive_pings_start_from_a_zero_grid(oracle):
-    """Each ping zeroes the binned grid for the next one beside its GEMM: pings
-    of different samples on one context, on the caller's stream and on a
-    second stream, each match their own oracle."""
+    """Each ping starts from a zeroed binned grid: pings of different samples
+    on one context, on the caller's stream and on a second stream, each match
+    their own oracle."""
     wk_a = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512, seed=5)
     wk_b = wl.precision_2d(n_samples=1 << 14, n_bearings=128, n_ranges=512, seed=6)
     ctx = precision_context(wk_a)
