@@ -22,6 +22,9 @@
 // f32 rmin, rmax, xscale, yscale; f32 bearings[nB]; float2 psf[H][W];
 // f32 samples[n][4] (travel-sorted); u64 views[nR][2] {start, size}.
 // Output file: float2 ping[nR][nB].
+// With a repetition count REPS > 0 it also times the kernel: one untimed
+// launch, then REPS launches between two CUDA events on the launching
+// stream; it prints "ref_kernel_ms <mean per launch>".
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -34,6 +37,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -62,7 +66,7 @@ bool rt_ok(cudaError_t e, const char* what)
 
 template <typename T> bool get(FILE* f, T* p, size_t n) { return std::fread(p, sizeof(T), n, f) == n; }
 
-bool run(const char* cubin, const char* in_path, const char* out_path)
+bool run(const char* cubin, const char* in_path, const char* out_path, int reps)
 {
     FILE* f = std::fopen(in_path, "rb");
     if(!f) return fail("cannot open input");
@@ -167,6 +171,21 @@ bool run(const char* cubin, const char* in_path, const char* out_path)
     std::vector<float2> out((size_t)nR * nB);
     if(!rt_ok(cudaMemcpy(out.data(), d_out, out.size() * sizeof(float2), cudaMemcpyDeviceToHost), "copy back"))
         return false;
+    if(reps > 0) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if(!rt_ok(cudaEventCreate(&e0), "event") || !rt_ok(cudaEventCreate(&e1), "event")) return false;
+        bool ok = cu_ok(cuLaunchKernel(fn, nB, nR, 1, 512, 1, 1, 512 * sizeof(float), nullptr, args, nullptr), "launch") &&
+                  rt_ok(cudaEventRecord(e0, nullptr), "record");
+        for(int i = 0; ok && i < reps; i++)
+            ok = cu_ok(cuLaunchKernel(fn, nB, nR, 1, 512, 1, 1, 512 * sizeof(float), nullptr, args, nullptr), "launch");
+        float ms = 0.0f;
+        ok = ok && rt_ok(cudaEventRecord(e1, nullptr), "record") && rt_ok(cudaEventSynchronize(e1), "kernel") &&
+             rt_ok(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if(!ok) return false;
+        std::printf("ref_kernel_ms %.6f\n", ms / reps);
+    }
     FILE* o = std::fopen(out_path, "wb");
     if(!o) return fail("cannot open output");
     const bool wrote = std::fwrite(out.data(), sizeof(float2), out.size(), o) == out.size();
@@ -182,9 +201,14 @@ bool run(const char* cubin, const char* in_path, const char* out_path)
 
 int main(int argc, char** argv)
 {
-    if(argc != 4) {
-        std::fprintf(stderr, "usage: %s REF_SPARSE2D.cubin INPUT OUTPUT\n", argv[0]);
+    if(argc != 4 && argc != 5) {
+        std::fprintf(stderr, "usage: %s REF_SPARSE2D.cubin INPUT OUTPUT [REPS]\n", argv[0]);
         return 2;
     }
-    return run(argv[1], argv[2], argv[3]) ? 0 : 1;
+    const int reps = argc == 5 ? std::atoi(argv[4]) : 0;
+    if(reps < 0 || reps > 1000) {
+        std::fprintf(stderr, "REPS must be in [0, 1000]\n");
+        return 2;
+    }
+    return run(argv[1], argv[2], argv[3], reps) ? 0 : 1;
 }
