@@ -57,3 +57,22 @@ def test_texture_psf_flag_rejected_where_unsupported():
     with pytest.raises(_lib.RtacxError):
         ctx2 = _lib.Context(0)
         ctx2.configure_2d(**wk.sensor, flags=4)
+
+
+def test_full_size_ping_against_the_live_reference_kernel(tmp_path):
+    """The reference's own kernel (oracle/_ref/ref_sparse2d.cubin, compiled
+    from the reference's source by oracle/ref_build.sh) run live on the full
+    oculus_2d ping (2^20 samples, 512 x 1024): the texture-PSF path matches it
+    to float round-off, the exact plain form to the texture quantization.
+    Skipped where the cubin was not built (it needs the reference tree)."""
+    from oracle import ref_kernel
+    from rtac_simulation_gb300 import _lib
+    if not ref_kernel.CUBIN.exists():
+        pytest.skip("oracle/_ref/ref_sparse2d.cubin not built here")
+    exe = ref_kernel.build_harness(tmp_path)
+    ref, _, wk = ref_kernel.run_case(exe, tmp_path, "oculus_2d", "oculus_2d", {})
+    assert np.isfinite(ref).all()
+    tex = gpu_reduce(make_context(wk, flags=_lib.RTACX_FLAG_TEXTURE_PSF), wk.samples, wk.out_shape)
+    assert rel_l2(tex, ref) <= 1e-6
+    exact = gpu_reduce(make_context(wk), wk.samples, wk.out_shape)
+    assert rel_l2(exact, ref) <= REF_PINGS_TOL_EXACT
