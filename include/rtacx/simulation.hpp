@@ -239,11 +239,16 @@ protected:
     SensorInstance(const Linspace& ranges, const Waveform::ConstPtr& waveform, float soundCelerity)
         : ranges_(ranges), waveform_(waveform->copy()), soundCelerity_(soundCelerity)
     {
-        check(rtacx_create(&ctx_, 0));
+        const rtacx_status st = rtacx_create(&ctx_, 0);
+        if(st != RTACX_OK)
+            throw std::runtime_error("rtacx: cannot create a context on CUDA device 0 (status " +
+                                     std::to_string((int)st) + ")");
     }
     void check(rtacx_status st) const
     {
-        if(st != RTACX_OK) throw std::runtime_error(std::string("rtacx: ") + rtacx_last_error(ctx_));
+        if(st != RTACX_OK)
+            throw std::runtime_error(std::string("rtacx: ") + rtacx_last_error(ctx_) + " (status " +
+                                     std::to_string((int)st) + ")");
     }
     std::vector<Complex> pulse_table() const
     {

@@ -113,3 +113,26 @@ def test_directivity_table_rejects_bad_parameters(lib):
         with pytest.raises(lib.RtacxError) as e:
             lib.directivity_table_size(kind, par)
         assert e.value.status == status, (kind, par)
+
+
+def test_cpp_mirror_without_a_gpu_reports_the_failure(lib, tmp_path):
+    # The C++ mirror (include/rtacx/simulation.hpp) turns a failing status
+    # into std::runtime_error, as the reference's API throws: without a GPU
+    # the sensor's constructor cannot create its context, and the demo
+    # program written against the mirror exits with that message.
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from rtac_simulation_gb300 import build
+    srcs = build.sources() + [build.DEMO_SRC, ROOT / "include" / "rtacx" / "simulation.hpp"]
+    if not build.DEMO_BIN.exists() or any(s.stat().st_mtime > build.DEMO_BIN.stat().st_mtime for s in srcs):
+        build.build_demo()
+    (tmp_path / "params.txt").write_text("dims 1\nrange_min 0.5\nrange_max 100.0\nrange_count 64\n"
+                                         "celerity 1500.0\nfrequency 38000.0\nduration 0.0001\nfixed 0\n"
+                                         "oversampling 8\ntexture_psf 0\n")
+    (tmp_path / "samples.bin").write_bytes(bytes(48))
+    res = subprocess.run([str(build.DEMO_BIN), str(tmp_path / "params.txt"), str(tmp_path / "samples.bin"),
+                          str(tmp_path / "out.bin")], capture_output=True, text=True, timeout=60)
+    assert res.returncode != 0
+    assert "cannot create a context on CUDA device 0" in res.stderr
+    assert not (tmp_path / "out.bin").exists()
