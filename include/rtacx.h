@@ -148,7 +148,9 @@ rtacx_status rtacx_bin(rtacx_ctx* ctx, const void* samples, uint64_t n, int samp
  * (include/rtac_simulation/SensorInstance1D.h:63-69) and
  * SensorInstance2D::fill_ping / reduce_samples
  * (include/rtac_simulation/SensorInstance2D.h:66-93). `samples` must match
- * the configured sensor (12-byte records for 1D, 16-byte records for 2D). */
+ * the configured sensor (12-byte records for 1D, 16-byte records for 2D) and
+ * be 4-byte aligned; `out` must be 8-byte aligned (whole complex64 cells are
+ * stored): RTACX_ERR_INVALID_ARGUMENT otherwise, before any work is queued. */
 rtacx_status rtacx_reduce(rtacx_ctx* ctx, const void* samples, uint64_t n,
                           float* out, void* stream);
 
@@ -364,14 +366,17 @@ rtacx_status rtacx_gemm_bf16_tn(const void* A, const void* B, float* C, int M, i
  * same kernels as rtacx_reduce without a context: the sensor (a
  * rtacx_sensor_1d* or rtacx_sensor_2d* matching sample_kind, host tables) is
  * uploaded on every call into one fixed file-scope device array that also
- * holds all scratch (about 8.3 MB, kept by every GPU that loads the library
+ * holds all scratch (about 6.6 MB, kept by every GPU that loads the library
  * until exit). Runs on the current device and on `stream`; no cudaMalloc,
  * cudaFree or other allocating call. Sizes above the limits below return
  * RTACX_ERR_UNSUPPORTED. The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress): make it before any stream capture.
  * All calls share the array, so calls whose GPU work overlaps (other streams,
- * other threads) race: serialise them. Status codes only (no context, so no
- * rtacx_last_error message). */
+ * other threads) race: serialise them. `samples` must be 4-byte and `out`
+ * 8-byte aligned (RTACX_ERR_INVALID_ARGUMENT otherwise). Status codes only
+ * (no context, so no rtacx_last_error message); the kernels' device error
+ * word is not read back, so a consistency error on the device (which an
+ * overlapping call can cause) is not reported by the status. */
 #define RTACX_NOALLOC_MAX_SAMPLES  (1u << 18)
 #define RTACX_NOALLOC_MAX_RANGES   4096u
 #define RTACX_NOALLOC_MAX_BEARINGS 1024u

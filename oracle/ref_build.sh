@@ -10,10 +10,18 @@
 #                           device stand-ins of oracle/ref_stubs_cuda; it is
 #                           launched by oracle/ref_sparse_harness.cpp on a
 #                           GPU machine (tests/golden/make_ref_pings.py).
-# Usage: oracle/ref_build.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/ref_build.sh [REFERENCE_ROOT]
+# The tree is REFERENCE_ROOT, else $RTAC_SIMULATION_REFERENCE, else the
+# container's read-only mount /root/reference. Without a reference tree (a
+# GPU machine, which only runs what was built from it) nothing is built and
+# the script exits 0.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${RTAC_SIMULATION_REFERENCE:-/root/reference}}"
+if [ ! -d "$REF/src" ]; then
+    echo "ref_build.sh: no reference tree at $REF; nothing built"
+    exit 0
+fi
 mkdir -p "$HERE/_ref"
 g++ -std=c++17 -O1 -ffp-contract=off -fno-fast-math \
     -I "$HERE/ref_stubs" -I "$REF/include" \

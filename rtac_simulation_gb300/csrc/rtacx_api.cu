@@ -405,6 +405,10 @@ rtacx_status rtacx_reduce(rtacx_ctx* ctx, const void* samples, uint64_t n, float
 {
     if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;
     if(!out) { ctx->impl.error = "null output buffer"; return RTACX_ERR_INVALID_ARGUMENT; }
+    // The gathers store whole complex64 cells (8-byte vector stores and
+    // vector reductions): a ping that is not 8-byte aligned is refused here
+    // rather than faulting on the device.
+    if(reinterpret_cast<uintptr_t>(out) % 8 != 0) { ctx->impl.error = "the ping must be 8-byte aligned"; return RTACX_ERR_INVALID_ARGUMENT; }
     rtacx_status st = prepare(ctx, samples, n, ctx->impl.dims);
     if(st != RTACX_OK) return st;
     Context& c = ctx->impl;

@@ -247,6 +247,7 @@ rtacx_status rtacx_batch_plan(rtacx_batch* b, const rtacx_ping_desc* pings, uint
         if(!seen.insert(p.ctx).second) { B.error = "ping " + std::to_string(i) + ": every ping needs its own context"; return RTACX_ERR_INVALID_ARGUMENT; }
         if(p.n >= (1ull << 32)) { B.error = "at most 2^32 - 1 samples per ping"; return RTACX_ERR_UNSUPPORTED; }
         if(reinterpret_cast<uintptr_t>(p.samples) % 4 != 0) { B.error = "sample buffers must be 4-byte aligned"; return RTACX_ERR_INVALID_ARGUMENT; }
+        if(reinterpret_cast<uintptr_t>(p.out) % 8 != 0) { B.error = "pings must be 8-byte aligned"; return RTACX_ERR_INVALID_ARGUMENT; }
         if(!ensure_capacity(c, p.n)) { B.error = c.error; return RTACX_ERR_OUT_OF_MEMORY; }
     }
     B.pings.assign(pings, pings + count);

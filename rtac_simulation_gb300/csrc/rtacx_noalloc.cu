@@ -11,7 +11,7 @@
 // device ping; no context is created.
 //
 // Limits (the array is sized for them and every GPU that loads the library
-// keeps it until the process exits, about 8.3 MB):
+// keeps it until the process exits, about 6.6 MB):
 //   samples <= RTACX_NOALLOC_MAX_SAMPLES, range bins <= RTACX_NOALLOC_MAX_RANGES,
 //   bearings <= RTACX_NOALLOC_MAX_BEARINGS, pulse taps <= RTACX_NOALLOC_MAX_PULSE,
 //   beam taps <= RTACX_NOALLOC_MAX_BEAM. Larger requests return
@@ -52,8 +52,9 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // Byte offsets of the scratch regions.
 constexpr size_t kOffSorted  = 0;
 constexpr size_t kOffHist    = align256(kOffSorted + kMaxSamples * sizeof(float4));
-constexpr size_t kOffOffsets = align256(kOffHist + (size_t)kMaxHistCtas * kMaxBins * 4);
-static_assert(kMaxHistCtas >= kCursorStride, "cursor region of the static scratch");
+// The scatter's per-bin write cursors: kCursorStride words per bin.
+constexpr size_t kHistBytes  = (size_t)kMaxBins * kCursorStride * sizeof(uint32_t);
+constexpr size_t kOffOffsets = align256(kOffHist + kHistBytes);
 constexpr size_t kOffTotals  = align256(kOffOffsets + (kMaxBins + 1) * 4);
 constexpr size_t kOffWin     = align256(kOffTotals + (kMaxBins + kMaxBins / 1024 + 1) * 4);   // + block sums
 constexpr size_t kOffOor     = align256(kOffWin + kMaxRanges * sizeof(int2));
@@ -116,6 +117,7 @@ extern "C" rtacx_status rtacx_reduce_noalloc(int sample_kind, const void* sensor
     if(!sensor || !out || (n && !samples)) return RTACX_ERR_INVALID_ARGUMENT;
     if(sample_kind != RTACX_SAMPLE_1D && sample_kind != RTACX_SAMPLE_2D) return RTACX_ERR_INVALID_ARGUMENT;
     if(reinterpret_cast<uintptr_t>(samples) % 4 != 0) return RTACX_ERR_INVALID_ARGUMENT;
+    if(reinterpret_cast<uintptr_t>(out) % 8 != 0) return RTACX_ERR_INVALID_ARGUMENT;   // complex64 vector stores
     if(n > kMaxSamples) return RTACX_ERR_UNSUPPORTED;
 
     // Sensor fields of either layout.
@@ -249,6 +251,7 @@ extern "C" rtacx_status rtacx_reduce_noalloc(int sample_kind, const void* sensor
     configure_hist_launch(ctx);
     ctx.hist_ctas = std::min(ctx.hist_ctas, kMaxHistCtas);
     ctx.hist_cols = (size_t)ctx.bin.nBins * kCursorStride;
+    if(ctx.hist_cols * sizeof(uint32_t) > kHistBytes) return RTACX_ERR_UNSUPPORTED;
 
     // Upload this call's tables (pageable copies: the staging above may be
     // reused as soon as these return) and clear the error word.

@@ -484,8 +484,13 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
     scan_u32(ctx.d_tile_parts, tiles, ctx.d_tile_first, stream);   // d_tile_first[tiles] = item count
     k_tile_items<<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_tile_parts, ctx.d_tile_first, grid.x, tiles,
                                                           ctx.d_items);
-    cudaMemsetAsync(ctx.d_item_counter, 0, sizeof(uint32_t), stream);
-    cudaMemsetAsync(out, 0, (size_t)ctx.nR * ctx.nB * sizeof(float2), stream);
+    cudaError_t me = cudaMemsetAsync(ctx.d_item_counter, 0, sizeof(uint32_t), stream);
+    if(me == cudaSuccess) me = cudaMemsetAsync(out, 0, (size_t)ctx.nR * ctx.nB * sizeof(float2), stream);
+    if(me != cudaSuccess) {
+        cudaGetLastError();
+        ctx.error = std::string("clearing the split gather's ping: ") + cudaGetErrorString(me);
+        return RTACX_ERR_CUDA;
+    }
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather_split<TR, TB>, kThreads, smem);
     per_sm = std::max(1, per_sm);

@@ -104,6 +104,38 @@ def beam_sinc(span: float, resolution: float, oversampling: int = 8) -> np.ndarr
 ECHO_PHASE = 1
 ECHO_SPREADING = 2
 
+# Receive-array phase reference of the precision workload, 3 mm from the
+# sensor origin along the array: the beam response then carries the phase
+# exp(i kappa (sin theta_k - sin theta_b)), kappa = 2 pi x0 / lambda, and the
+# dense bearing directivity is complex.
+PHASE_CENTRE_M = 3.0e-3
+
+
+def steering_wavenumber(frequency: float, c: float, x0: float) -> float:
+    """kappa = 2 pi x0 / lambda of a phase reference x0 metres off the origin."""
+    return 2.0 * math.pi * x0 * frequency / c
+
+
+def steer_samples(samples: np.ndarray, steer: float) -> np.ndarray:
+    """Copy of 2D samples with each value multiplied by exp(i kappa sin theta_s):
+    with the output rotated by exp(-i kappa sin theta_b) (steer_ping), the
+    per-sample PSF of a real beam becomes the per-sample counterpart of the
+    steered complex directivity of precision_tables."""
+    out = np.array(samples, dtype=np.float32, copy=True)
+    if steer == 0.0:
+        return out
+    ph = np.exp(1j * steer * np.sin(out[:, 3].astype(np.float64)))
+    v = (out[:, 0].astype(np.float64) + 1j * out[:, 1]) * ph
+    out[:, 0], out[:, 1] = v.real, v.imag
+    return out
+
+
+def steer_ping(ping: np.ndarray, bearings, steer: float) -> np.ndarray:
+    """ping[r][b] * exp(-i kappa sin theta_b) (see steer_samples)."""
+    if steer == 0.0:
+        return ping
+    return ping * np.exp(-1j * steer * np.sin(np.asarray(bearings, np.float64)))[None, :]
+
 
 @dataclass
 class Workload:
@@ -113,6 +145,7 @@ class Workload:
     samples: np.ndarray               # (N, 3) SimSample1D or (N, 4) SimSample2D, float32
     meta: dict = field(default_factory=dict)
     echo: dict | None = None          # echo pre-step: {"carrier_hz": f, "flags": ECHO_*}
+    precision: dict = field(default_factory=dict)   # keyword arguments of precision_tables
 
     @property
     def n(self) -> int:
@@ -215,8 +248,9 @@ def precision_2d(n_samples: int = 1 << 24, seed: int = 3, n_bearings: int = 512,
     re, im = _rayleigh_phasor(rng, n_samples)
     return Workload("precision_2d", 2,
                     sensor_2d(rmin, rmax, n_ranges, c, pulse, taps * res, beam, span, bearings),
-                    _pack(re, im, t, th), dict(frequency=f),
-                    echo=dict(carrier_hz=f, flags=ECHO_PHASE | ECHO_SPREADING))
+                    _pack(re, im, t, th), dict(frequency=f, phase_centre_m=PHASE_CENTRE_M),
+                    echo=dict(carrier_hz=f, flags=ECHO_PHASE | ECHO_SPREADING),
+                    precision=dict(steer=steering_wavenumber(f, c, PHASE_CENTRE_M)))
 
 
 def oculus_reference_2d(n_samples: int = 20000, seed: int = 4, n_bearings: int = 256) -> Workload:
@@ -342,19 +376,25 @@ def _lerp(table: np.ndarray, x: np.ndarray) -> np.ndarray:
     return np.where(ok, lo * (1 - a) + hi * a, 0)
 
 
-def precision_tables(sensor: dict):
+def precision_tables(sensor: dict, steer: float = 0.0):
     """Directivity matrix and range taps of the binned precision model,
-    derived from a 2D sensor's tables exactly as rtacx_configure_precision
-    derives them when given NULL tables: D[k][b] = beam(theta_k - theta_b)
-    (float bearing difference, exact lerp) and taps[t] = pulse(t * resolution)
-    for |t| <= overlap, trimmed to the non-zero span. Returns
+    derived from a 2D sensor's tables as rtacx_configure_precision derives
+    them when given NULL tables: D[k][b] = beam(theta_k - theta_b) (float
+    bearing difference, exact lerp) and taps[t] = pulse(t * resolution) for
+    |t| <= overlap, trimmed to the non-zero span. With steer = kappa != 0 the
+    directivity carries the phase of a phase reference off the origin,
+    exp(i kappa (sin theta_k - sin theta_b)) (complex D). Returns
     (D complex64 [nB][nB], taps complex64, centre index)."""
     bear = np.asarray(sensor["bearings"], np.float32)
     beam = np.asarray(sensor["beam"], np.float32).astype(np.float64)
     W = beam.size
     kx = float(np.float32(1.0) / np.float32(sensor["beam_span"])) * W
     e = (bear[:, None] - bear[None, :]).astype(np.float32).astype(np.float64)
-    D = _lerp(beam, e * kx + 0.5 * W - 0.5).astype(np.complex64)
+    D = _lerp(beam, e * kx + 0.5 * W - 0.5)
+    if steer != 0.0:
+        sb = np.sin(bear.astype(np.float64))
+        D = D * np.exp(1j * steer * (sb[:, None] - sb[None, :]))
+    D = D.astype(np.complex64)
     nR = sensor["range_count"]
     res = float(linspace_resolution(sensor["range_min"], sensor["range_max"], nR)) if nR > 1 else 0.0
     mres = np.float32(np.float32(sensor["range_max"]) - np.float32(sensor["range_min"]))

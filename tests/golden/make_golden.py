@@ -5,8 +5,8 @@ header-only Binner::Key and Waveform_Sine against host stand-ins for the
 non-vendored rtac_base headers) and records its answers for a fixed, seeded
 set of inputs into tests/golden/ref_keys.json, ref_waveforms.json and
 ref_directivity.json (the receiver directivity builders of src/Directivity.cpp).
-Needs the reference tree (default /root/reference); the tests only read the
-committed JSON files.
+Needs the reference tree (the argument, else where oracle/ref_build.sh looks
+for it); the tests only read the committed JSON files.
 
 Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
 """
@@ -73,8 +73,9 @@ def run_probe(lines):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    subprocess.run([str(ROOT / "oracle" / "ref_build.sh"), ref], check=True)
+    subprocess.run([str(ROOT / "oracle" / "ref_build.sh"), *sys.argv[1:2]], check=True)
+    if not PROBE.exists():
+        raise SystemExit("no reference tree: pass its path, or set RTAC_SIMULATION_REFERENCE")
     rng = np.random.Generator(np.random.PCG64(2024))
 
     key_cases = []

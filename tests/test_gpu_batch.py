@@ -69,3 +69,35 @@ def test_batch_rejects_shared_context(batch_setup):
     batch = _lib.Batch(0)
     with pytest.raises(_lib.RtacxError):
         batch.plan([(ctxs[0], devs[0], pings[0].n, outs[0]), (ctxs[0], devs[0], pings[0].n, outs[0])])
+
+
+def test_batch_full_size_mix(oracle):
+    """The batched configuration at its size: 64 pings with log-uniform
+    sample counts in [2^14, 2^22] (half 512-bearing 2D, a quarter 256-bearing
+    2D, a quarter 1D). Every ping equals the single-ping path over the whole
+    ping, and the FP64 oracle on a band of 8 rows."""
+    pings = wl.batched_mix()
+    assert len(pings) == 64
+    ctxs, devs, outs = [], [], []
+    for wk in pings:
+        ctxs.append(make_context(wk))
+        devs.append(torch.from_numpy(wk.samples.reshape(-1)).cuda())
+        outs.append(torch.full(wk.out_shape + (2,), float("nan"), device="cuda"))
+    batch = _lib.Batch(0)
+    batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)], autotune=False)
+    batch.run(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    for wk, o, ctx in zip(pings, outs, ctxs):
+        got = _complex(o)
+        assert np.isfinite(got).all(), wk.name
+        ref_ctx = make_context(wk)
+        assert rel_l2(got, gpu_reduce(ref_ctx, wk.samples, wk.out_shape)) <= 1e-6, wk.name
+        ref_ctx.close()
+        nR = wk.sensor["range_count"]
+        rows = (nR // 3, nR // 3 + 8)
+        want = oracle.reduce(wk.samples, wk.sensor, rows=rows)
+        band = got[rows[0]:rows[1]]
+        assert rel_l2(band, want) <= 1e-5, wk.name
+    batch.close()
+    for c in ctxs:
+        c.close()

@@ -394,3 +394,53 @@ def test_precision_consecutive_pings_start_from_a_zero_grid(oracle):
         ctx.stream_status(s)
         o = out.cpu().numpy()
         assert rel_l2(o[..., 0] + 1j * o[..., 1], want[id(w)]) <= TOL
+
+
+def _random_phase(D, seed=21):
+    """D with an independent uniform phase per entry: a complex directivity
+    with no structure the contraction could lean on."""
+    rng = np.random.default_rng(seed)
+    return (D * np.exp(2j * np.pi * rng.random(D.shape))).astype(np.complex64)
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+@pytest.mark.parametrize("kind", ["steered", "random_phase"])
+def test_precision_complex_directivity(oracle, fp16, kind):
+    """Im D != 0 through both contraction forms: the {dr, -di}, {di, dr}
+    layout of the directivity operand (and the FP16 column scales over the
+    imaginary rows) against the FP64 oracle of the binned model."""
+    from rtac_simulation_gb300 import _lib
+    wk = wl.precision_2d(n_samples=1 << 18, n_ranges=1024)
+    D, taps, c = wl.precision_tables(wk.sensor, **wk.precision)
+    if kind == "random_phase":
+        D = _random_phase(D)
+    assert np.abs(D.imag).max() > 0.03
+    ctx = make_context(wk)
+    ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    ctx.configure_precision(D, taps, c, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    assert np.isfinite(got).all()
+    err = rel_l2(got, want)
+    assert err <= TOL, err
+    # The real-directivity ping differs: the imaginary half is really used.
+    Dr = D.real.astype(np.complex64)
+    ctx.configure_precision(Dr, taps, c, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
+    assert rel_l2(gpu_precision(ctx, wk.samples, wk.out_shape), want) > 100 * TOL
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+def test_precision_complex_directivity_full_size_band(oracle, fp16):
+    """The headline ping (2^24 samples, 512 x 4096, steered complex
+    directivity) against the binned FP64 oracle on two bands of rows."""
+    from rtac_simulation_gb300 import _lib
+    wk = wl.precision_2d()
+    D, taps, c = wl.precision_tables(wk.sensor, **wk.precision)
+    ctx = make_context(wk)
+    ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    ctx.configure_precision(D, taps, c, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    smp = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
+    for rows in ((0, 32), (2500, 2532)):
+        want = oracle.reduce_binned(smp, wk.sensor, D, taps, c, rows=rows)
+        assert rel_l2(got[rows[0]:rows[1]], want) <= TOL, rows

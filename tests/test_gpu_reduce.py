@@ -12,7 +12,7 @@ torch = pytest.importorskip("torch")
 if not torch.cuda.is_available():
     pytest.skip("needs a GPU", allow_module_level=True)
 
-from helpers_gpu import gpu_reduce, make_context, rel_l2  # noqa: E402
+from helpers_gpu import to_device, gpu_reduce, make_context, rel_l2  # noqa: E402
 
 TOL = 1e-5
 
@@ -72,6 +72,21 @@ def test_reduce_unaligned_matches_aligned():
     a = gpu_reduce(ctx, wk.samples, wk.out_shape)
     b = gpu_reduce(ctx, wk.samples, wk.out_shape, offset_floats=1)
     assert rel_l2(b, a) <= 1e-6
+
+
+def test_reduce_rejects_misaligned_ping():
+    """A ping pointer that is only 4-byte aligned is refused with a status
+    before any launch (the gathers store whole complex64 cells)."""
+    from rtac_simulation_gb300 import _lib
+    wk = wl.oculus_reference_2d(n_samples=64)
+    ctx = make_context(wk)
+    d = to_device(wk.samples)
+    buf = torch.zeros(2 * wk.out_shape[0] * wk.out_shape[1] + 2, dtype=torch.float32, device="cuda")
+    lib = _lib.load()
+    st = lib.rtacx_reduce(ctx.handle, d.data_ptr(), wk.n, buf.data_ptr() + 4, None)
+    assert st == _lib.RTACX_ERR_INVALID_ARGUMENT
+    assert "aligned" in ctx.last_error()
+    assert torch.count_nonzero(buf).item() == 0
 
 
 def test_full_size_rows_match_oracle(oracle):

@@ -96,3 +96,18 @@ def test_noalloc_rejects_sizes_beyond_limits():
     sensor.range_count = 4097
     assert lib.rtacx_reduce_noalloc(_lib.RTACX_SAMPLE_2D, ctypes.byref(sensor), dev.data_ptr(), 4,
                                     out.data_ptr(), None) == _lib.RTACX_ERR_UNSUPPORTED
+
+
+def test_noalloc_rejects_misaligned_buffers():
+    """Only 4-byte aligned samples and 8-byte aligned pings are accepted; the
+    check comes before any upload or launch."""
+    wk = wl.oculus_reference_2d(n_samples=16)
+    lib = _lib.load()
+    sensor, keep = _sensor_struct(wk)
+    dev = torch.zeros(64 + 4, dtype=torch.float32, device="cuda")
+    out = torch.zeros(2 * wk.out_shape[0] * wk.out_shape[1] + 2, dtype=torch.float32, device="cuda")
+    assert lib.rtacx_reduce_noalloc(_lib.RTACX_SAMPLE_2D, ctypes.byref(sensor), dev.data_ptr(), 16,
+                                    out.data_ptr() + 4, None) == _lib.RTACX_ERR_INVALID_ARGUMENT
+    assert lib.rtacx_reduce_noalloc(_lib.RTACX_SAMPLE_2D, ctypes.byref(sensor), dev.data_ptr() + 2, 16,
+                                    out.data_ptr(), None) == _lib.RTACX_ERR_INVALID_ARGUMENT
+    assert torch.count_nonzero(out).item() == 0
