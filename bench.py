@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import datetime
+import inspect
 import json
 import math
 import os
@@ -50,13 +51,11 @@ DEFAULT_CONFIG = "precision_2d"
 #       python bench.py --steps 2 --warmup 3 --no-cpu-baseline [--no-next-rows]
 # on a GB300. Reported as `traffic` beside the live `achieved` numbers.
 NCU_TRAFFIC_BYTES = {
-    "k_prec_accumulate_staged": 302.126e6 + 3.701e6,
-    "k_gemm_tn": 31.470e6 + 0.003e6,
     "sort_bin": (268.531e6 + 3.186e6) + (274.855e6 + 223.261e6),   # k_count + k_scatter_staged
 }
 
 KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
-PRECISION_KERNELS_PER_PING = 4   # clear, staged accumulate, range filter (with the windows), tensor-core GEMM
+PRECISION_KERNELS_PER_PING = 5   # clear, staged accumulate, operand split, tensor-core GEMM, range filter
 
 
 def parse_args():
@@ -68,6 +67,8 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", default=DEFAULT_CONFIG, choices=sorted(workloads.CONFIGS))
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-reference-kernel", action="store_true",
+                   help="reference arm: skip timing the reference's own CUDA kernel")
     p.add_argument("--no-next-rows", action="store_true",
                    help="skip the timing of the echo-sample epilogue, directivity tables and rasteriser")
     return p.parse_args()
@@ -185,75 +186,133 @@ def useful_pairs(wk) -> float:
     return float((rows * cols).sum())
 
 
-def cpu_reference_step(wk, rows_per_step: int, threads: int) -> tuple[float, int]:
-    """Time the reference algorithm (oracle, FP32 reference arithmetic) on the
-    host: full sort + bin of all samples plus the gather of `rows_per_step`
-    output rows; extrapolate the gather to every row. Returns seconds per
-    ping and the row count actually reduced."""
+# Samples of the bounded ping the host arms reduce per step: the same
+# geometry, tables and sample distributions as the GPU workload, fewer
+# samples (the per-sample cost of the reference algorithm -- the gather over
+# the PSF support -- does not depend on the sample count).
+CPU_PING_SAMPLES = 1 << 17
+
+
+def full_samples(config: str) -> int:
+    """Sample count of a configuration's full ping (its builder's default)."""
+    return int(inspect.signature(workloads.CONFIGS[config]).parameters["n_samples"].default)
+
+
+def cpu_workload(config: str, echo_mode: int = 1):
+    """The bounded host ping of a configuration, with the echo epilogue applied
+    in the reference's float arithmetic (its ray generator does it before
+    this path)."""
     from oracle import oracle
-    nR = wk.sensor["range_count"]
-    r0 = nR // 2 - rows_per_step // 2
+    wk = workloads.CONFIGS[config](n_samples=min(full_samples(config), CPU_PING_SAMPLES))
+    if wk.echo:
+        wk.samples = oracle.apply_echo(wk.samples, wk.sensor, wk.echo, mode=echo_mode)
+    return wk
+
+
+def cpu_reference_step(wk, threads: int) -> float:
+    """Seconds of the reference algorithm (oracle, FP32 reference arithmetic)
+    on the host for one whole ping: travel sort, keys, segments, windows and
+    the per-sample PSF gather of every output cell."""
+    from oracle import oracle
     t0 = time.perf_counter()
-    oracle.reduce(wk.samples, wk.sensor, mode=1, rows=(r0, r0), threads=threads)
-    t_bin = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    oracle.reduce(wk.samples, wk.sensor, mode=1, rows=(r0, r0 + rows_per_step), threads=threads)
-    t_rows = max(time.perf_counter() - t0 - t_bin, 1e-9)
-    return t_bin + t_rows * nR / rows_per_step, rows_per_step
+    oracle.reduce(wk.samples, wk.sensor, mode=1, threads=threads)
+    return time.perf_counter() - t0
 
 
 def cpu_model() -> str:
+    """Host CPU model: lscpu's model name, else /proc/cpuinfo's, else the Arm
+    part number's name."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    arm_parts = {"0xd4f": "Neoverse-V2", "0xd40": "Neoverse-V1", "0xd49": "Neoverse-N2", "0xd0c": "Neoverse-N1"}
     try:
         for line in open("/proc/cpuinfo"):
-            if line.lower().startswith(("model name", "cpu part")):
-                return line.split(":", 1)[1].strip()
+            key, _, val = line.partition(":")
+            if key.strip().lower() == "model name":
+                return val.strip()
+            if key.strip().lower() == "cpu part":
+                return arm_parts.get(val.strip().lower(), f"Arm part {val.strip()}")
     except OSError:
         pass
     return "unknown"
 
 
+def reference_gpu_kernel(config: str) -> dict:
+    """The reference's own 2D reduction kernel (do_sparse_convolve_2d_f,
+    src/SensorInstance2D.cu:44-83), compiled from the reference's source for
+    sm_103a where the reference tree is (oracle/_ref/ref_sparse2d.cubin) and
+    launched as SensorInstance2D::do_reduce does, on this GPU and the full
+    workload: CUDA-event time per launch with the samples already
+    travel-sorted and binned (its Thrust sort and do_make_bins are not
+    included). Reported beside the host arm, not timed as it."""
+    from oracle import ref_kernel
+    if not ref_kernel.CUBIN.exists():
+        return {"unavailable": "oracle/_ref/ref_sparse2d.cubin was not built (no reference tree where it was built)"}
+    if config in ("echosounder_1d", "ea400_reference_1d"):
+        return {"unavailable": "1D: this arm times the reference's 2D kernel only"}
+    with tempfile.TemporaryDirectory() as d:
+        tmp = Path(d)
+        exe = ref_kernel.build_harness(tmp)
+        _, ms, wk = ref_kernel.run_case(exe, tmp, config, config, {}, reps=2)
+    return {"ms_per_launch": ms, "samples": int(wk.n), "samples_per_s": wk.n / (ms / 1e3),
+            "what": "do_sparse_convolve_2d_f from the reference's source, one 512-thread CTA per output cell, "
+                    "PSF texture (linear filter, border); sort and binning excluded; mean of 2 launches after 1"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    from oracle import oracle
     if args.config == "batched_mix":
         return run_reference_batch(args)
-    wk = workloads.CONFIGS[args.config]()
-    if wk.echo:   # the reference applies the echo epilogue in its ray generator, before this path
-        wk.samples = oracle.apply_echo(wk.samples, wk.sensor, wk.echo, mode=1)
+    wk = cpu_workload(args.config)
+    full_desc = wk_desc(wk).replace(f": {wk.n} samples", f": {full_samples(args.config)} samples", 1)
     threads = os.cpu_count() or 1
-    rows = 16 if wk.dims == 2 else max(64, wk.sensor["range_count"] // 8)
     for _ in range(args.warmup):
-        cpu_reference_step(wk, rows, threads)
-    times = [cpu_reference_step(wk, rows, threads)[0] for _ in range(args.steps)]
+        cpu_reference_step(wk, threads)
+    times = [cpu_reference_step(wk, threads) for _ in range(args.steps)]
     t = statistics.median(times)
     value = wk.n / t
-    sample = (f"per step: sort+bin of all {wk.n} samples and the FP32 gather of {rows} of "
-              f"{wk.sensor['range_count']} output rows, extrapolated to the full ping; median of {args.steps}")
-    print(json.dumps({
+    sample = (f"per step: one whole ping of {wk.n} samples with the workload's geometry ({full_desc}): "
+              f"sort, keys, segments, windows and the FP32 per-sample PSF gather of all "
+              f"{int(np.prod(wk.out_shape))} output cells, nothing extrapolated; median of {args.steps}")
+    line = {
         "impl": "reference", "metric": "samples/s", "value": value, "unit": "samples/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t,
         "pings_per_s": 1.0 / t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": wk_desc(wk), "form": "reference algorithm, host CPU"},
+        "config": {"workload": full_desc, "form": "reference algorithm, host CPU",
+                   "host_ping": f"{wk.n} samples per step (same geometry and distributions)"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
                          "sample": sample, "cpu": cpu_model()},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }))
+    }
+    if not args.no_reference_kernel:
+        try:
+            line["reference_cuda_kernel"] = reference_gpu_kernel(args.config)
+        except Exception as e:   # the host arm stands on its own
+            line["reference_cuda_kernel"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    print(json.dumps(line))
 
 
 def run_reference_batch(args):
     """Reference algorithm on the host for the batched mix, bounded: every
-    step takes 8 of the 64 pings, each with a full sort + bin and the gather
-    of a band of rows extrapolated to all rows (as the single-ping arm)."""
+    step reduces 8 of the 64 pings in full (sort, bin and the gather of every
+    output cell), each capped at CPU_PING_SAMPLES samples."""
     pings = workloads.batched_mix()
-    sample = pings[::8]
+    sample = []
+    for wk in pings[::8]:
+        if wk.n > CPU_PING_SAMPLES:
+            wk = workloads.Workload(wk.name, wk.dims, wk.sensor, wk.samples[:CPU_PING_SAMPLES], wk.meta)
+        sample.append(wk)
     threads = os.cpu_count() or 1
     times = []
     for step in range(args.warmup + args.steps):
-        t = 0.0
-        for wk in sample:
-            t += cpu_reference_step(wk, 16 if wk.dims == 2 else 64, threads)[0]
+        t = sum(cpu_reference_step(wk, threads) for wk in sample)
         if step >= args.warmup:
             times.append(t)
     t = statistics.median(times)
@@ -263,9 +322,10 @@ def run_reference_batch(args):
         "impl": "reference", "metric": "samples/s", "value": value, "unit": "samples/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t, "pings_per_s": len(sample) / t,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "batched_mix (8 of 64 pings per step: sort + bin of each, gather of 16 (2D) or 64 (1D) rows extrapolated to all rows)", "form": "reference algorithm, host CPU"},
+        "config": {"workload": "batched_mix (8 of the 64 pings per step, each reduced in full, at most "
+                               f"{CPU_PING_SAMPLES} samples each)", "form": "reference algorithm, host CPU"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": threads, "kind": "port",
-                         "sample": f"8 of the 64 pings ({n} samples) fully reduced per step"},
+                         "sample": f"8 of the 64 pings ({n} samples) fully reduced per step", "cpu": cpu_model()},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
@@ -548,22 +608,32 @@ def run_ours(args, world, rank, local):
     if wk.echo:
         ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
     forms = ["plain"]
+    steer = wk.precision.get("steer", 0.0)
     if wk.dims == 2 and wk.echo:
-        D, taps, center = workloads.precision_tables(wk.sensor)
-        ctx.configure_precision(D, taps, center)
+        tab = workloads.precision_tables(wk.sensor, **wk.precision)
+        ctx.configure_precision(**tab)
         forms = ["precision", "precision_compensated", "precision_fp16", "plain"]
         if args.config == "stress_2d":   # the clustered ping: also with the hot-range replicas
             forms.insert(3, "precision_hot")
     ctx.reserve(n)
     host_in = torch.from_numpy(wk.samples.reshape(-1)).pin_memory()
     d_in = host_in.to("cuda")
+    # The plain form reads the samples rotated by exp(i kappa sin theta_s):
+    # its ping rotated by exp(-i kappa sin theta_b) is then the per-sample
+    # counterpart of the precision form's steered complex directivity (the
+    # work per ping does not depend on the values).
+    if steer:
+        plain_host = torch.from_numpy(workloads.steer_samples(wk.samples, steer).reshape(-1)).pin_memory()
+        plain_dev = plain_host.to("cuda")
+    else:
+        plain_host, plain_dev = host_in, d_in
     outs = {f: torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda") for f in forms}
     host_out = torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory()
     alt = None
     if "precision" in forms:   # second context: two pings in flight in the end-to-end loop
         ctx2 = _lib.Context(local)
         ctx2.configure_2d(**wk.sensor)
-        ctx2.configure_precision(D, taps, center)
+        ctx2.configure_precision(**tab)
         alt = (ctx2, torch.empty(wk.out_shape + (2,), dtype=torch.float32).pin_memory(),
                torch.empty(wk.out_shape + (2,), dtype=torch.float32, device="cuda"))
     res = {}
@@ -571,16 +641,17 @@ def run_ours(args, world, rank, local):
         if f in ("precision_fp16", "precision_hot"):   # FP16 contraction / hot-range replicas, FP64 phase
             fl = _lib.RTACX_PRECISION_FP16_ROWSCALE if f == "precision_fp16" else _lib.RTACX_PRECISION_HOT_RANGE
             for c in (ctx, alt[0]):
-                c.configure_precision(D, taps, center, flags=fl)
+                c.configure_precision(**tab, flags=fl)
         # The plain form (~72 ms per ping here) is timed over at most 20 steps
         # when it is not the headline form.
         steps_f = min(args.steps, 20) if (f == "plain" and forms[0] != "plain") else args.steps
-        res[f] = time_form(ctx, f, d_in, n, outs[f], host_in, host_out, steps_f, args.warmup, dist, local, torch,
+        src_dev, src_host = (plain_dev, plain_host) if f == "plain" else (d_in, host_in)
+        res[f] = time_form(ctx, f, src_dev, n, outs[f], src_host, host_out, steps_f, args.warmup, dist, local, torch,
                            wk.echo, alt)
         res[f]["steps"] = steps_f
         if f in ("precision_fp16", "precision_hot"):
             for c in (ctx, alt[0]):
-                c.configure_precision(D, taps, center)
+                c.configure_precision(**tab)
     if rank != 0:
         return
     head = forms[0]
@@ -605,7 +676,8 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": wk_desc(wk),
-                   "form": ("precision: bin-first, BF16x3 tcgen05 complex contraction, FP32 range filter, FP64 carrier phase"
+                   "form": ("precision: bin onto a 4x bearing grid, BF16x3 tcgen05 complex contraction, FP32 range "
+                            "filter, FP64 carrier phase"
                             if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
                    "l2": ("inputs larger than L2 (%.0f MB of samples)" if n * rec_in > 129e6 else
                           "inputs smaller than L2 (%.0f MB of samples): timed warm, not flushed") % (n * rec_in / 1e6),
@@ -643,21 +715,22 @@ def run_ours(args, world, rank, local):
     if "precision" in forms:
         ps = res["precision"]["stage"]
         nR, nB = wk.sensor["range_count"], len(wk.sensor["bearings"])
+        cells, rows_g = tab["grid_count"], nR + len(tab["range_taps"]) + 1
         # Accumulate: one read of every sample (16 B) + the binned grid written once (8 B / cell).
-        acc_bytes = n * rec_in + nR * nB * 8
+        acc_bytes = n * rec_in + rows_g * cells * 8
         acc_gbs = acc_bytes / (ps["accumulate"] / 1e3) / 1e9
-        Mp, Np, Kp = -(-nR // 128) * 128, -(-2 * nB // 256) * 256, -(-6 * nB // 64) * 64
+        Mp, Np, Kp = -(-rows_g // 128) * 128, -(-2 * nB // 256) * 256, -(-6 * cells // 64) * 64
         gemm_tf = 2.0 * Mp * Np * Kp / (ps["gemm"] / 1e3) / 1e12
         roof_acc = {"bound": "hbm", "achieved": acc_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                     "frac": acc_gbs / peaks["hbm_gbs"], "traffic": ncu.get("k_prec_accumulate_staged"),
                     "kernel": "k_prec_accumulate_staged",
                     "peak_source": peaks["source"],
-                    "algorithmic": f"{rec_in} B per sample read + 8 B per binned cell"}
+                    "algorithmic": f"{rec_in} B per sample read + 8 B per grid cell ({rows_g} x {cells})"}
         roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": gemm_tf / peaks["bf16_tflops"], "traffic": ncu.get("k_gemm_tn"), "kernel": "k_gemm_tn",
                      "peak_source": peaks["source"],
                      "algorithmic": f"2*M*N*K with M={Mp} N={Np} K={Kp} (three BF16 split products as one K)"}
-        dominant = max(("accumulate", "gemm", "filter"), key=lambda k: ps[k])
+        dominant = max(("accumulate", "gemm", "filter", "split"), key=lambda k: ps[k])
         line["roofline"] = roof_gemm if dominant == "gemm" else roof_acc
         line["roofline"]["dominant_stage"] = dominant
         line["roofline_gemm"] = roof_gemm
@@ -676,21 +749,13 @@ def run_ours(args, world, rank, local):
     if world == 1 and not args.no_cpu_baseline:
         from oracle import oracle
         threads = os.cpu_count() or 1
-        ref_wk = wk
-        if wk.echo:
-            ref_wk = workloads.Workload(wk.name, wk.dims, wk.sensor,
-                                        oracle.apply_echo(wk.samples, wk.sensor, wk.echo, mode=1), wk.meta)
-        rows = 32 if wk.dims == 2 else max(64, wk.sensor["range_count"] // 8)
-        cap = 1 << 24
-        n_cpu = min(n, cap)
-        if n > cap:   # bound the host sort: time a prefix of the ping
-            ref_wk = workloads.Workload(wk.name, wk.dims, wk.sensor, ref_wk.samples[:cap], wk.meta)
-        t_cpu, rows = cpu_reference_step(ref_wk, rows, threads)
+        cpu_wk = cpu_workload(args.config)
+        t_cpu = statistics.median(cpu_reference_step(cpu_wk, threads) for _ in range(3))
         line["cpu_baseline"] = {
-            "value": n_cpu / t_cpu, "unit": "samples/s", "cores": threads, "kind": "port",
+            "value": cpu_wk.n / t_cpu, "unit": "samples/s", "cores": threads, "kind": "port",
             "sample": (f"oracle FP32 reference arithmetic (per-sample PSF, float carrier phase as the reference): "
-                       f"sort+bin of {n_cpu} samples{' (prefix of the ping)' if n > cap else ''} plus the gather of "
-                       f"{rows} of {wk.sensor['range_count']} rows, extrapolated"),
+                       f"one whole ping of {cpu_wk.n} samples with this workload's geometry, all "
+                       f"{int(np.prod(cpu_wk.out_shape))} output cells, median of 3, nothing extrapolated"),
             "cpu": cpu_model()}
         # Bit-exact bin counts of this ping against the oracle's keys.
         s_ = wk.sensor
@@ -707,24 +772,34 @@ def run_ours(args, world, rank, local):
         # Accuracy of this run's pings against their FP64 oracles on bands of rows.
         nR = wk.sensor["range_count"]
         exact = oracle.apply_echo(wk.samples, wk.sensor, wk.echo) if wk.echo else wk.samples
+        exact_steered = workloads.steer_samples(exact, steer) if steer else exact
         acc = {}
         bands = [(0, 16), (nR // 3, nR // 3 + 16), (nR // 2, nR // 2 + 16)] if wk.dims == 2 else [(0, nR)]
         got_plain = to_complex(outs["plain"])
+        if steer:
+            got_plain = workloads.steer_ping(got_plain, wk.sensor["bearings"], steer)
         for b0, b1 in bands:
-            want = oracle.reduce(exact, wk.sensor, mode=0, rows=(b0, b1), threads=threads)
+            # The per-sample PSF in FP64 (the steered counterpart where the directivity is steered).
+            want = oracle.reduce(exact_steered, wk.sensor, mode=0, rows=(b0, b1), threads=threads)
+            if steer:
+                want = workloads.steer_ping(want, wk.sensor["bearings"], steer)
             if not np.linalg.norm(want) > 0:      # no echo in this band
                 continue
-            acc.setdefault("plain_rel_l2_vs_fp64", []).append(
-                float(np.linalg.norm(got_plain[b0:b1] - want) / np.linalg.norm(want)))
+            rel = lambda a_, b_: float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_))
+            acc.setdefault("plain_rel_l2_vs_fp64", []).append(rel(got_plain[b0:b1], want))
             if "precision" in forms:
-                want_b = oracle.reduce_binned(exact, wk.sensor, D, taps, center, rows=(b0, b1), threads=threads)
+                want_b = oracle.reduce_binned(exact, wk.sensor, tab, rows=(b0, b1), threads=threads)
                 for f in [f_ for f_ in forms if f_.startswith("precision")]:
                     got_p = to_complex(outs[f])
-                    acc.setdefault(f"{f}_rel_l2_vs_fp64_binned", []).append(
-                        float(np.linalg.norm(got_p[b0:b1] - want_b) / np.linalg.norm(want_b)))
-                acc.setdefault("binned_vs_per_sample_model_rel_l2", []).append(
-                    float(np.linalg.norm(want_b - want) / np.linalg.norm(want)))
+                    acc.setdefault(f"{f}_rel_l2_vs_fp64_binned", []).append(rel(got_p[b0:b1], want_b))
+                acc.setdefault("precision_rel_l2_vs_fp64_per_sample", []).append(
+                    rel(to_complex(outs["precision"])[b0:b1], want))
+                acc.setdefault("precision_rel_l2_vs_plain_fp32_path", []).append(
+                    rel(to_complex(outs["precision"])[b0:b1], got_plain[b0:b1]))
+                acc.setdefault("binned_vs_per_sample_model_rel_l2", []).append(rel(want_b, want))
         acc["rows_checked"] = bands
+        acc["note"] = ("fp64_binned: the FP64 oracle of the binned model the precision form computes; "
+                       "fp64_per_sample / binned_vs_per_sample: against the reference's per-sample PSF in FP64")
         line["accuracy"] = acc
     print(json.dumps(line))
 

@@ -173,29 +173,49 @@ typedef struct {
 } rtacx_echo_model;
 rtacx_status rtacx_set_echo_model(rtacx_ctx* ctx, const rtacx_echo_model* model);
 
-/* Precision (tensor-core) form of a configured 2D sensor. Bins first, then
- * contracts over bearings on the tensor cores, then filters in range:
- *   G[j][k]  = sum over samples s in range bin j (Binner::Key) of v_s, split
- *              linearly between the two table bearings k, k+1 around theta_s
- *              (clamped to the first / last bearing outside the table);
- *   G'[r][k] = sum_t taps[t] G[r + t - tap_center][k] over the bins j of
- *              row r's reference window (do_make_bins rule, range bins whose
- *              G row received a sample count as non-empty);
- *   out      = G' x D, D the dense complex [bearing_count][bearing_count]
- *              directivity (D[k][b]: response of beam b to bearing k).
- * The contraction runs in BF16 with three split products (hi*hi + hi*lo +
+/* Precision (tensor-core) form of a configured 2D sensor. Bins onto a fine
+ * grid first, then contracts over bearings on the tensor cores, then filters
+ * in range. Per sample s (reference range key in range, finite travel t and
+ * bearing theta; float arithmetic, every operation rounded on its own):
+ *   range    res = (range_max - range_min) / (range_count - 1) (the output
+ *            ranges' Linspace resolution), j = floor((t - range_min) / res),
+ *            alpha = (t - (range_min + j res)) / res: the value goes to grid
+ *            rows j and j + 1 with weights 1 - alpha and alpha;
+ *   bearing  a uniform grid of grid_count bearings from grid_first to
+ *            grid_last, step = (grid_last - grid_first) / (grid_count - 1),
+ *            q = clamp(floor((theta - grid_first) / step), 0, grid_count - 2),
+ *            w = clamp((theta - (grid_first + q step)) / step, 0, 1): grid
+ *            bearings q and q + 1 with weights 1 - w and w
+ *            (divisions as products with the float reciprocals);
+ *   G[j][q] += v_s times the product of the two weights (four cells);
+ *   out(r, b) = sum_t taps[t] sum_q G[r + t - tap_center][q] D[q][b],
+ *            D the dense complex [grid_count][bearing_count] directivity
+ *            (D[q][b]: response of beam b to grid bearing q); a row whose
+ *            reference window (do_make_bins rule, src/Binner.cu:90-102, on
+ *            the keyed non-empty range bins) is empty is zero.
+ * For a pulse sampled at bin spacing the range part is the per-sample PSF's
+ * own interpolation (the taps at whole-bin offsets, linearly interpolated),
+ * so the model differs from rtacx_reduce only by the bearing grid. The
+ * contraction runs in BF16 with three split products (hi*hi + hi*lo +
  * lo*hi) and FP32 accumulation on tcgen05 tensor cores; the rest is FP32.
- * This is a binned model: samples sit on the table bearings and at their
- * range-bin offsets, unlike the per-sample PSF of rtacx_reduce. Bearings
- * must be strictly increasing. NULL tables are derived from the 2D sensor:
- * D[k][b] = beam(theta_k - theta_b) and taps[t] = pulse((t - tap_center) *
- * resolution) with the same texture-equivalent lerp as rtacx_reduce. */
+ * NULL tables are derived from the 2D sensor: taps[t] = pulse((t -
+ * tap_center) * resolution) (texture-equivalent lerp, |t - tap_center| <=
+ * the reference's bin overlap, trimmed to the non-zero span), and D[.][b] the
+ * least-squares projection of beam(theta - theta_b) onto the grid's hat
+ * functions (the coefficients whose linear interpolation between grid
+ * bearings is closest in mean square to the per-sample response). grid_count
+ * 0 selects four grid bearings per output bearing (rounded up to a multiple
+ * of 32); grid_first == grid_last selects the first and last table bearings.
+ * Samples outside the grid's bearings take its end bearing. */
 typedef struct {
-    const float* directivity;   /* host complex [bearing_count][bearing_count] or NULL */
-    const float* range_taps;    /* host complex [tap_count] or NULL                    */
+    const float* directivity;   /* host complex [grid_count][bearing_count] or NULL */
+    const float* range_taps;    /* host complex [tap_count] or NULL                 */
     uint32_t tap_count;
     uint32_t tap_center;
-    uint32_t flags;             /* 0 or RTACX_PRECISION_FP16_ROWSCALE */
+    uint32_t flags;             /* 0 or RTACX_PRECISION_* below                     */
+    uint32_t grid_count;        /* bearing grid size (even, <= 16384), 0: default   */
+    float grid_first;           /* first and last grid bearing (rad)                */
+    float grid_last;
 } rtacx_precision_desc;
 /* Contract in FP16 instead of BF16: each row of the filtered grid and each
  * column of the directivity is scaled by a power of two to [2^14, 2^15)
@@ -206,11 +226,11 @@ typedef struct {
 /* Contention relief for clustered scenes (a strong target concentrating many
  * samples in few range bins): a strided subsample of each ping (1/128 of the
  * samples, or of the first 2^21-record chunk of rtacx_reduce_precision_host)
- * finds the densest 256-row range interval; if it holds at least a tenth of
- * the samples and four times its uniform share, those rows are accumulated
- * into eight replicas (chosen by CTA and warp), added back into the grid
- * before the range filter, so vector reductions to the same cells no longer
- * serialise. Same result up to the order of float additions. */
+ * finds the densest 256-row interval of grid rows; if it holds at least a
+ * tenth of the samples and four times its uniform share, those rows are
+ * accumulated into eight replicas (chosen by CTA and warp), added back into
+ * the grid before the contraction, so vector reductions to the same cells no
+ * longer serialise. Same result up to the order of float additions. */
 #define RTACX_PRECISION_HOT_RANGE 2u
 rtacx_status rtacx_configure_precision(rtacx_ctx* ctx, const rtacx_precision_desc* desc);
 rtacx_status rtacx_reduce_precision(rtacx_ctx* ctx, const void* samples, uint64_t n,
@@ -336,10 +356,10 @@ rtacx_status rtacx_stream_status(rtacx_ctx* ctx, void* stream);
  * the caller's stream. rtacx_stage_times waits for the last traced call and
  * writes up to `max` stage durations in milliseconds (0 for stages the last
  * call did not run): for rtacx_reduce count, reset of the bin totals, bin
- * scan, scatter, windows, reduce; for rtacx_reduce_precision accumulate, windows (0: the
- * range filter forms each row's window itself), range filter, tensor-core
- * GEMM, copy-out, and the zeroing of the binned grid before the
- * accumulation. Returns the number of stages written (negative on error). */
+ * scan, scatter, windows, reduce; for rtacx_reduce_precision accumulate,
+ * operand split, range filter, tensor-core GEMM, (unused), and the zeroing
+ * of the grid before the accumulation. Returns the number of stages written
+ * (negative on error). */
 #define RTACX_STAGE_COUNT 6
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
 

@@ -61,7 +61,7 @@ def load() -> ctypes.CDLL:
     lib.rtacx_oracle_reduce.restype = None
     lib.rtacx_oracle_apply_echo.argtypes = [_P, _U64, _U32, ctypes.c_double, _F, _U32, _I]
     lib.rtacx_oracle_apply_echo.restype = None
-    lib.rtacx_oracle_reduce_binned.argtypes = [_P, _U64, _F, _F, _U32, _F, _P, _U32, _P, _P, _U32, _U32,
+    lib.rtacx_oracle_reduce_binned.argtypes = [_P, _U64, _F, _F, _U32, _F, _U32, _F, _F, _U32, _P, _P, _U32, _U32,
                                                _U32, _U32, _I, _P]
     lib.rtacx_oracle_reduce_binned.restype = None
     lib.rtacx_oracle_make_samples.argtypes = [_P, _U64, _P, _P, _U32, _U32, ctypes.c_double, _F, _U32, _U32, _P]
@@ -134,10 +134,11 @@ def pulse_scale(sensor: dict, literal_1d: bool = False) -> np.float32:
 def reduce(samples: np.ndarray, sensor: dict, mode: int = 0, rows=None, threads: int = 0,
            literal_1d: bool = False) -> np.ndarray:
     """Oracle ping. mode 0: FP64 (complex128), mode 1: FP32 reference
-    arithmetic (complex64), mode 2 (2D): the PSF fetched as the reference's
+    arithmetic (complex64), mode 2: the PSF fetched as the reference's
     texture does on the GPU (coordinate truncated to 21 fractional bits,
-    weights rounded to 1/256), accumulated in FP64 (complex128). rows =
-    (begin, end) restricts the output rows."""
+    weights rounded to 1/256; border addressing), accumulated in FP64
+    (complex128); mode 3 (1D): mode 2 with clamp addressing. rows = (begin,
+    end) restricts the output rows."""
     lib = load()
     s = np.ascontiguousarray(samples, dtype=np.float32)
     n, stride = s.shape
@@ -154,8 +155,8 @@ def reduce(samples: np.ndarray, sensor: dict, mode: int = 0, rows=None, threads:
         beam = np.zeros(1, dtype=np.float32)
         bearings = np.zeros(1, dtype=np.float32)
         bscale, nB = np.float32(0.0), 1
-    if mode == 2 and dims != 2:
-        raise ValueError("the texture-unit mode is 2D only")
+    if mode == 3 and dims != 1:
+        raise ValueError("the clamp-addressed texture mode is 1D only")
     out = np.zeros((r1 - r0, nB), dtype=np.complex64 if mode == 1 else np.complex128)
     threads = threads or (os.cpu_count() or 1)
     lib.rtacx_oracle_reduce(dims, s.ctypes.data, n, sensor["range_min"], sensor["range_max"], nR,
@@ -177,21 +178,25 @@ def apply_echo(samples: np.ndarray, sensor: dict, echo: dict | None, mode: int =
     return out
 
 
-def reduce_binned(samples: np.ndarray, sensor: dict, directivity: np.ndarray, taps: np.ndarray,
-                  tap_center: int, rows=None, threads: int = 0) -> np.ndarray:
-    """FP64 oracle of the binned precision model (complex128 [rows][nB])."""
+def reduce_binned(samples: np.ndarray, sensor: dict, tables: dict, rows=None, threads: int = 0) -> np.ndarray:
+    """FP64 oracle of the binned precision model (complex128 [rows][nB]).
+    `tables` holds the precision configuration (workloads.precision_tables):
+    directivity [grid_count][nB], range_taps, tap_center, grid_count,
+    grid_first, grid_last."""
     lib = load()
     s = np.ascontiguousarray(samples, dtype=np.float32)
     n = s.shape[0]
     nR = sensor["range_count"]
-    bear = np.ascontiguousarray(sensor["bearings"], dtype=np.float32)
-    D = np.ascontiguousarray(directivity, dtype=np.complex64)
-    t = np.ascontiguousarray(taps, dtype=np.complex64)
+    nB = len(sensor["bearings"])
+    D = np.ascontiguousarray(tables["directivity"], dtype=np.complex64)
+    t = np.ascontiguousarray(tables["range_taps"], dtype=np.complex64)
+    cells = int(tables["grid_count"])
+    assert D.shape == (cells, nB)
     r0, r1 = rows if rows is not None else (0, nR)
-    out = np.zeros((r1 - r0, bear.size), dtype=np.complex128)
+    out = np.zeros((r1 - r0, nB), dtype=np.complex128)
     lib.rtacx_oracle_reduce_binned(s.ctypes.data, n, sensor["range_min"], sensor["range_max"], nR,
-                                   sensor["margin"], bear.ctypes.data, bear.size, D.ctypes.data,
-                                   t.ctypes.data, t.size, tap_center, r0, r1,
+                                   sensor["margin"], nB, tables["grid_first"], tables["grid_last"], cells,
+                                   D.ctypes.data, t.ctypes.data, t.size, int(tables["tap_center"]), r0, r1,
                                    threads or (os.cpu_count() or 1), out.ctypes.data)
     return out
 

@@ -9,7 +9,9 @@
 #                           texture lookup) for sm_103a (nvcc), with the
 #                           device stand-ins of oracle/ref_stubs_cuda; it is
 #                           launched by oracle/ref_sparse_harness.cpp on a
-#                           GPU machine (tests/golden/make_ref_pings.py).
+#                           GPU machine (tests/golden/make_ref_pings.py);
+#   _ref/ref_sparse1d.cubin the same for src/SensorInstance1D.cu
+#                           (do_sparse_convolve_1d_f, KernelView1D).
 # Usage: oracle/ref_build.sh [REFERENCE_ROOT]
 # The tree is REFERENCE_ROOT, else $RTAC_SIMULATION_REFERENCE, else the
 # container's read-only mount /root/reference. Without a reference tree (a
@@ -30,3 +32,6 @@ NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
 "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -diag-suppress 20012 \
     -I "$HERE/ref_stubs_cuda" -I "$REF/include" \
     "$REF/src/SensorInstance2D.cu" -o "$HERE/_ref/ref_sparse2d.cubin"
+"$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -diag-suppress 20012 \
+    -I "$HERE/ref_stubs_cuda" -I "$REF/include" \
+    "$REF/src/SensorInstance1D.cu" -o "$HERE/_ref/ref_sparse1d.cubin"

@@ -22,6 +22,7 @@ template <typename T> struct CudaVector {
     const T* data() const { return data_; }
     std::size_t size() const { return size_; }
     void resize(std::size_t n) { size_ = n; }
+    VectorView<T> view() { return VectorView<T>{size_, data_}; }
 };
 }
 }

@@ -2,7 +2,8 @@
 // before the reference's include directory so that src/SensorInstance2D.cu
 // compiles without the rest of the sensor class hierarchy (SensorInfo
 // factories, poses, receivers, pings), which needs the non-vendored
-// rtac_base. It declares only what that file's definitions use; the sample
+// rtac_base. It declares only what that file's definitions use (and what
+// src/SensorInstance1D.cu uses, through the SensorInstance1D stand-in); the sample
 // records (rtac_simulation/Sample.h) and the PSF lookup KernelView2D
 // (rtac_simulation/ReductionKernel.h) are the reference's own headers.
 // Nothing here runs: the harness launches do_sparse_convolve_2d_f itself.
@@ -42,6 +43,11 @@ struct BeamDirectivity {
     float span() const { return span_; }
 };
 
+// The 1D sensor's info: only the type is used by src/SensorInstance1D.cu.
+struct SensorInfo {
+    using ConstPtr = std::shared_ptr<const SensorInfo>;
+};
+
 struct SensorInfo2D {
     using ConstPtr = std::shared_ptr<const SensorInfo2D>;
     BeamDirectivity::ConstPtr beam_;
@@ -59,6 +65,7 @@ protected:
     Linspace<float> ranges_{};
 public:
     SensorInstance(const SensorInfo2D::ConstPtr&, const Pose&, float c) : soundCelerity_(c) {}
+    SensorInstance(const SensorInfo::ConstPtr&, const Pose&, float c) : soundCelerity_(c) {}
     const Linspace<float>& ranges() const { return ranges_; }
 };
 

@@ -318,6 +318,31 @@ void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void*
             }
         }
     }
+    else if((mode == 2 || mode == 3) && S.dims == 1) {
+        // Texture-unit emulation (1D): the linear fetch of the pulse table
+        // with the texture unit's per-axis weight (texel_weight) at the
+        // kernel's coordinate fmaf(scale, delta, 0.5)
+        // (include/rtac_simulation/ReductionKernel.h:44-55), border (mode 2)
+        // or clamp (mode 3) addressing -- the reference's 1D texture takes
+        // rtac_base's defaults (src/SensorInstance1D.cu:15-25), which are not
+        // vendored; accumulation in double.
+        std::complex<double>* o = static_cast<std::complex<double>*>(out_row);
+        auto texel = [&](int j) -> std::complex<double> {
+            if(mode == 3) j = std::min(std::max(j, 0), H - 1);
+            else if(j < 0 || j >= H) return std::complex<double>(0.0, 0.0);
+            return std::complex<double>(pulse_f[j].real(), pulse_f[j].imag());
+        };
+        std::complex<double> acc(0.0, 0.0);
+        for(uint32_t k = 0; k < size; k++) {
+            const SortedSample& s = B.sorted[off + k];
+            const float uy = std::fmaf(S.pulse_scale, s.travel - R, 0.5f);
+            int c;
+            const int j = texel_weight(uy, H, c);
+            const std::complex<double> w = ((double)(256 - c) * texel(j) + (double)c * texel(j + 1)) / 256.0;
+            acc += std::complex<double>(s.re, s.im) * w;
+        }
+        o[0] = acc;
+    }
     else if(mode == 2) {
         // Texture-unit emulation (2D): the bilinear fetch of the W x H table
         // PSF[h][w] = pulse[h] * beam[w] (rounded to float, as
@@ -373,6 +398,46 @@ void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void*
             o[b] = acc;
         }
     }
+}
+
+struct GridAxes {
+    float rmin, res, inv_res;
+    float first, step, inv_step;
+    uint32_t cells;
+    int row_lo, row_hi;        // accepted absolute rows j: [row_lo, row_hi]
+};
+
+GridAxes make_grid_axes(float rmin, float rmax, uint32_t nR, float first, float last, uint32_t cells,
+                        uint32_t ntaps, uint32_t center)
+{
+    GridAxes g;
+    g.rmin = rmin;
+    g.res = (rmax - rmin) / (float)(nR - 1u);
+    g.inv_res = 1.0f / g.res;
+    g.first = first;
+    g.step = (last - first) / (float)(cells - 1u);
+    g.inv_step = 1.0f / g.step;
+    g.cells = cells;
+    g.row_lo = -(int)center - 1;
+    g.row_hi = (int)nR + (int)ntaps - (int)center - 2;
+    return g;
+}
+
+// Grid coordinates of one sample; false when it contributes nothing.
+inline bool grid_coords(const GridAxes& g, float t, float th, int& jg, float& alpha, int& q, float& w, int center)
+{
+    if(!std::isfinite(t) || !std::isfinite(th)) return false;
+    const float jf = std::floor((t - g.rmin) * g.inv_res);
+    if(!(jf >= (float)g.row_lo && jf <= (float)g.row_hi)) return false;
+    const int j = (int)jf;
+    const float rj = g.rmin + (float)j * g.res;
+    alpha = (t - rj) * g.inv_res;
+    jg = j + center + 1;
+    const float qf = std::fmin(std::fmax(std::floor((th - g.first) * g.inv_step), 0.0f), (float)(g.cells - 2u));
+    q = (int)qf;
+    const float gq = g.first + (float)q * g.step;
+    w = std::fmin(std::fmax((th - gq) * g.inv_step, 0.0f), 1.0f);
+    return true;
 }
 
 } // namespace
@@ -521,66 +586,77 @@ void rtacx_oracle_apply_echo(float* samples, uint64_t n, uint32_t stride, double
 }
 
 // FP64 oracle of the binned (precision) model -- see rtacx_reduce_precision
-// in include/rtacx.h: G[j][k] by range key and linear bearing split, window
-// rule on non-empty bins, range taps within each row's window, then the dense
-// complex directivity. Rows [row_begin, row_end) into out (complex double).
+// in include/rtacx.h. Per sample (in-range reference key, finite travel and
+// bearing), with the float arithmetic of the device spelled out so that the
+// grid coordinates agree bit for bit:
+//   range    res = (rmax - rmin) / (nR - 1), inv_res = 1 / res (the Linspace
+//            resolution of the output ranges); j = floor((t - rmin) * inv_res),
+//            alpha = (t - (rmin + j * res)) * inv_res: weight 1 - alpha on
+//            grid row j, alpha on row j + 1. The per-sample PSF evaluates a
+//            pulse sampled at bin spacing at t - R_r, which is exactly this
+//            linear split followed by the taps at whole-bin offsets.
+//   bearing  step = (last - first) / (cells - 1), inv_step = 1 / step;
+//            q = clamp(floor((theta - first) * inv_step), 0, cells - 2),
+//            w = clamp((theta - (first + q * step)) * inv_step, 0, 1): weight
+//            1 - w on grid bearing q, w on q + 1.
+// Grid row j is stored at jg = j + center + 1 of nR + ntaps + 1 rows; samples
+// whose rows fall outside reach no output row and are dropped. Output row r
+// is zero when its reference window (do_make_bins rule on the keyed
+// non-empty bins) is empty, else out(r, b) = sum_t taps[t] sum_q
+// G[r + t + 1][q] D[q][b]. Rows [row_begin, row_end) into out (complex
+// double).
 void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, float rmax, uint32_t nR,
-                                float margin, const float* bearings, uint32_t nB, const float* D,
-                                const float* taps, uint32_t ntaps, uint32_t center,
+                                float margin, uint32_t nB, float grid_first, float grid_last, uint32_t cells,
+                                const float* D, const float* taps, uint32_t ntaps, uint32_t center,
                                 uint32_t row_begin, uint32_t row_end, int nthreads, void* out)
 {
     using cd = std::complex<double>;
+    if(nR < 2 || cells < 2 || ntaps == 0) return;
     KeyParams key = make_key(nR, rmin, rmax, margin);
-    std::vector<cd> G((size_t)nR * nB, cd(0.0, 0.0));
+    const GridAxes ax = make_grid_axes(rmin, rmax, nR, grid_first, grid_last, cells, ntaps, center);
+    const size_t rows = (size_t)nR + ntaps + 1;
+    std::vector<cd> G(rows * cells, cd(0.0, 0.0));
     std::vector<uint8_t> nonempty(nR, 0);
     for(uint64_t i = 0; i < n; i++) {
         const float* s = samples + i * 4;
-        const uint32_t j = range_key(key, s[2]);
-        if(j == kOutOfRange) continue;
-        nonempty[j] = 1;
+        const uint32_t k = range_key(key, s[2]);
+        if(k == kOutOfRange) continue;
+        nonempty[k] = 1;
+        int jg, q;
+        float alpha, w;
+        if(!grid_coords(ax, s[2], s[3], jg, alpha, q, w, (int)center)) continue;
         const cd v(s[0], s[1]);
-        cd* row = G.data() + (size_t)j * nB;
-        if(nB == 1) { row[0] += v; continue; }
-        const float th = s[3];
-        int lo = 0, hi = (int)nB - 2;
-        while(lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if(bearings[mid] <= th) lo = mid; else hi = mid - 1;
-        }
-        double w = ((double)th - (double)bearings[lo]) / ((double)bearings[lo + 1] - (double)bearings[lo]);
-        w = std::fmin(std::fmax(w, 0.0), 1.0);
-        row[lo] += (1.0 - w) * v;
-        row[lo + 1] += w * v;
+        const double a = alpha, b = w;
+        cd* r0 = G.data() + (size_t)jg * cells + q;
+        cd* r1 = r0 + cells;
+        r0[0] += (1.0 - a) * (1.0 - b) * v;
+        r0[1] += (1.0 - a) * b * v;
+        r1[0] += a * (1.0 - b) * v;
+        r1[1] += a * b * v;
     }
-    const int ov = (nR > 1) ? bin_overlap(rmin, rmax, nR, margin) : 0;
-    const cd* tp = nullptr;
+    const int ov = bin_overlap(rmin, rmax, nR, margin);
     std::vector<cd> tv(ntaps);
     for(uint32_t t = 0; t < ntaps; t++) tv[t] = cd(taps[2 * t], taps[2 * t + 1]);
-    tp = tv.data();
-    std::vector<cd> Dd((size_t)nB * nB);
-    for(size_t q = 0; q < Dd.size(); q++) Dd[q] = cd(D[2 * q], D[2 * q + 1]);
+    std::vector<cd> Dd((size_t)cells * nB);
+    for(size_t e = 0; e < Dd.size(); e++) Dd[e] = cd(D[2 * e], D[2 * e + 1]);
     row_end = std::min(row_end, nR);
     parallel_rows(row_begin, row_end, nthreads, [&](uint32_t r) {
         cd* o = static_cast<cd*>(out) + (size_t)(r - row_begin) * nB;
         for(uint32_t b = 0; b < nB; b++) o[b] = cd(0.0, 0.0);
+        if(ov < 0) return;
         const long long lo = std::max(0ll, (long long)r - ov), hi = std::min((long long)nR - 1, (long long)r + ov);
-        long long a = lo;
-        while(a <= hi && !nonempty[a]) a++;
-        if(a >= hi) return;
-        long long z = hi;
-        while(z > a && !nonempty[z]) z--;
-        if(a >= z) return;
-        std::vector<cd> g(nB, cd(0.0, 0.0));
+        int nonempty_bins = 0;
+        for(long long jj = lo; jj <= hi && nonempty_bins < 2; jj++) nonempty_bins += nonempty[jj];
+        if(nonempty_bins < 2) return;          // the reference's empty view (src/Binner.cu:90-102)
+        std::vector<cd> g(cells, cd(0.0, 0.0));
         for(uint32_t t = 0; t < ntaps; t++) {
-            const long long jj = (long long)r + t - (long long)center;
-            if(jj < a || jj > z) continue;
-            const cd* row = G.data() + (size_t)jj * nB;
-            for(uint32_t k = 0; k < nB; k++) g[k] += tp[t] * row[k];
+            const cd* row = G.data() + ((size_t)r + t + 1) * cells;
+            for(uint32_t q = 0; q < cells; q++) g[q] += tv[t] * row[q];
         }
-        for(uint32_t k = 0; k < nB; k++) {
-            if(g[k] == cd(0.0, 0.0)) continue;
-            const cd* dk = Dd.data() + (size_t)k * nB;
-            for(uint32_t b = 0; b < nB; b++) o[b] += g[k] * dk[b];
+        for(uint32_t q = 0; q < cells; q++) {
+            if(g[q] == cd(0.0, 0.0)) continue;
+            const cd* dq = Dd.data() + (size_t)q * nB;
+            for(uint32_t b = 0; b < nB; b++) o[b] += g[q] * dq[b];
         }
     });
 }

@@ -147,7 +147,7 @@ RTACX_ECHO_SPREADING = 2
 RTACX_ECHO_PHASE_COMPENSATED = 4
 RTACX_PRECISION_FP16_ROWSCALE = 1
 RTACX_PRECISION_HOT_RANGE = 2
-PRECISION_STAGES = ("accumulate", "windows", "filter", "gemm", "copy", "clear")
+PRECISION_STAGES = ("accumulate", "split", "filter", "gemm", "unused", "clear")
 
 
 class EchoModel(ctypes.Structure):
@@ -156,7 +156,7 @@ class EchoModel(ctypes.Structure):
 
 class PrecisionDesc(ctypes.Structure):
     _fields_ = [("directivity", _P), ("range_taps", _P), ("tap_count", _U32), ("tap_center", _U32),
-                ("flags", _U32)]
+                ("flags", _U32), ("grid_count", _U32), ("grid_first", ctypes.c_float), ("grid_last", ctypes.c_float)]
 
 STAGES = ("count", "reset", "binscan", "scatter", "windows", "reduce")
 
@@ -279,11 +279,14 @@ class Context:
         m = EchoModel(carrier_hz, flags)
         self._check(self._lib.rtacx_set_echo_model(self._h, ctypes.byref(m)))
 
-    def configure_precision(self, directivity=None, range_taps=None, tap_center: int = 0, flags: int = 0) -> None:
+    def configure_precision(self, directivity=None, range_taps=None, tap_center: int = 0, flags: int = 0,
+                            grid_count: int = 0, grid_first: float = 0.0, grid_last: float = 0.0) -> None:
+        """rtacx_configure_precision; the keyword arguments are those of
+        workloads.precision_tables (directivity [grid_count][nB] complex)."""
         d = None if directivity is None else np.ascontiguousarray(np.asarray(directivity, dtype=np.complex64))
         t = None if range_taps is None else np.ascontiguousarray(np.asarray(range_taps, dtype=np.complex64))
         desc = PrecisionDesc(None if d is None else d.ctypes.data, None if t is None else t.ctypes.data,
-                             0 if t is None else t.size, tap_center, flags)
+                             0 if t is None else t.size, tap_center, flags, grid_count, grid_first, grid_last)
         self._check(self._lib.rtacx_configure_precision(self._h, ctypes.byref(desc)))
 
     def reduce_precision(self, samples, n: int, out, stream=None) -> None:

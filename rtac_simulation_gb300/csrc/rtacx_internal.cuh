@@ -236,6 +236,39 @@ __device__ __forceinline__ float4 load_record(const float* base, uint64_t i, con
     return make_float4(__ldg(s), __ldg(s + 1), __ldg(s + 2), p.stride == 4 ? __ldg(s + 3) : 0.0f);
 }
 
+// Grid of the binned precision model (see rtacx_reduce_precision in
+// include/rtacx.h): range rows at the output-range resolution, a uniform
+// bearing grid of `cells` bearings. Absolute range row j (row 0 at
+// range_min) is stored at grid row j + row_shift; rows outside [row_lo,
+// row_hi] reach no output row.
+struct GridParams {
+    float rmin, res, inv_res;
+    float first, step, inv_step;
+    uint32_t cells;
+    int row_lo, row_hi, row_shift;
+};
+
+// Grid coordinates of one sample with the model's float arithmetic, each
+// operation rounded on its own (no contraction), as the oracle computes
+// them: j = floor((t - rmin) / res), alpha = (t - (rmin + j res)) / res;
+// q = clamp(floor((theta - first) / step), 0, cells - 2), w = clamp((theta -
+// (first + q step)) / step, 0, 1) (divisions as products with the float
+// reciprocals). Returns false for samples that reach no output row or carry
+// a non-finite travel or bearing.
+__device__ __forceinline__ bool grid_coords(const GridParams& g, float t, float th, int& jg, float& alpha, int& q,
+                                            float& w)
+{
+    const float jf = floorf(__fmul_rn(__fsub_rn(t, g.rmin), g.inv_res));
+    const bool ok = fabsf(t) < INFINITY && fabsf(th) < INFINITY && jf >= (float)g.row_lo && jf <= (float)g.row_hi;
+    const int j = ok ? (int)jf : 0;
+    alpha = __fmul_rn(__fsub_rn(t, __fadd_rn(g.rmin, __fmul_rn((float)j, g.res))), g.inv_res);
+    jg = j + g.row_shift;
+    const float qf = fminf(fmaxf(floorf(__fmul_rn(__fsub_rn(th, g.first), g.inv_step)), 0.0f), (float)(g.cells - 2u));
+    q = (int)qf;
+    w = fminf(fmaxf(__fmul_rn(__fsub_rn(th, __fadd_rn(g.first, __fmul_rn(qf, g.step))), g.inv_step), 0.0f), 1.0f);
+    return ok;
+}
+
 // Reduction parameters of a configured sensor.
 struct ReduceParams {
     int dims;
@@ -347,31 +380,27 @@ struct Context {
     bool prec_configured = false;
     uint32_t taps = 0, tap_center = 0;
     uint32_t Mpad = 0, Npad = 0, Kp = 0;
-    float4* d_G = nullptr;              // [nR][nB] binned pair cells {to bearing k, to bearing k+1}
-    uint32_t* d_flags = nullptr;        // [(nR + 31) / 32] bitmap of non-empty range bins
-    float2* d_lut = nullptr;            // bearing lookup grid {count below, bearing in the cell}
-    uint32_t lut_cells = 0;
-    int lut_exact = 0;                  // no grid cell holds two interior bearings
+    GridParams grid{};                  // range rows and uniform bearing grid of the binned model
+    uint32_t grid_rows = 0;             // nR + taps + 1 rows of the binned grid
+    float2* d_G = nullptr;              // [grid_rows][grid.cells] binned grid (complex)
+    uint32_t* d_flags = nullptr;        // [(nR + 31) / 32] bitmap of non-empty range bins (reference keys)
     uint32_t acc_staged_blocks[6] = {}; // resident CTAs per SM of each staged accumulation (0: not used)
     size_t acc_staged_smem = 0;
     uint32_t diag_drop_stage = 0xFFFFFFFFu; // failure-path test: stage whose copy the staged accumulation skips
-    float lut_origin = 0.0f, lut_scale = 0.0f;
-    uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the filtered grid
+    uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the binned grid
     uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity
-    float* d_C = nullptr;               // [Mpad][Npad] GEMM output when the ping shape is not tile-aligned
+    float* d_C = nullptr;               // [Mpad][Npad] GEMM output: the grid contracted over bearings
     float2* d_taps = nullptr;           // [taps] range taps at bin offsets t - tap_center
     // FP16 per-row-scaled contraction (RTACX_PRECISION_FP16_ROWSCALE): A and B
     // hold fp16 splits instead of bf16 ones.
     bool prec_f16 = false;
-    float2* d_Gf = nullptr;             // [nR][nB] filtered grid (fp32) before the scaled split
-    uint32_t* d_rowmax = nullptr;       // [nR] largest |component| of each filtered row (float bits)
-    float* d_row_scale = nullptr;       // [Mpad] 2^-e per row: undoes the row's scaling in the GEMM epilogue
+    float* d_row_scale = nullptr;       // [Mpad] 2^-e per grid row: undoes the row's scaling in the GEMM epilogue
     float* d_col_scale = nullptr;       // [Npad] 2^-e per directivity column
-    // Hot range interval (RTACX_PRECISION_HOT_RANGE).
+    // Hot range interval (RTACX_PRECISION_HOT_RANGE), in grid rows.
     bool prec_hot = false;
-    int2* d_hot = nullptr;              // {first row, length} of the hot interval (length 0: none)
-    uint32_t* d_hotcnt = nullptr;       // [nR] subsample counts (zero between pings)
-    float4* d_rep = nullptr;            // [hot rows][replicas][nB] pair-cell replicas
+    int2* d_hot = nullptr;              // {first grid row, length} of the hot interval (length 0: none)
+    uint32_t* d_hotcnt = nullptr;       // [grid_rows] subsample counts (zero between pings)
+    float2* d_rep = nullptr;            // [hot rows][replicas][grid.cells] grid replicas
 
     // Host-buffer streaming (rtacx_reduce_precision_host): two device staging
     // buffers of RTACX_STREAM_CHUNK records, a copy stream fork-joined to the

@@ -200,6 +200,20 @@ def echosounder_1d(n_samples: int = 65536, seed: int = 1, n_ranges: int = 4096,
                     _pack(re, im, t), dict(frequency=f))
 
 
+def on_range_grid(samples: np.ndarray, sensor: dict, every: int = 8, seed: int = 99) -> np.ndarray:
+    """Copy of `samples` in which every `every`-th travel is set exactly to a
+    (seeded, random) output range R_r = range_min + r * resolution in float:
+    with the reference's literal 1D scaling 1.0f / duration * c, only samples
+    at an exact output range fall inside the pulse table, so these give that
+    ping its non-zero rows."""
+    out = np.array(samples, dtype=np.float32, copy=True)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    idx = np.arange(0, out.shape[0], every)
+    R = linspace(sensor["range_min"], sensor["range_max"], sensor["range_count"])
+    out[idx, 2] = R[rng.integers(0, R.size, idx.size)]
+    return out
+
+
 def oculus_2d(n_samples: int = 1 << 20, seed: int = 2, n_bearings: int = 512, n_ranges: int = 1024,
               rmin: float = 0.3, rmax: float = 40.0, taps: int = 33, half_bearings: int = 16,
               altitude: float = 5.0, clutter: float = 0.01) -> Workload:
@@ -376,25 +390,95 @@ def _lerp(table: np.ndarray, x: np.ndarray) -> np.ndarray:
     return np.where(ok, lo * (1 - a) + hi * a, 0)
 
 
-def precision_tables(sensor: dict, steer: float = 0.0):
-    """Directivity matrix and range taps of the binned precision model,
-    derived from a 2D sensor's tables as rtacx_configure_precision derives
-    them when given NULL tables: D[k][b] = beam(theta_k - theta_b) (float
-    bearing difference, exact lerp) and taps[t] = pulse(t * resolution) for
-    |t| <= overlap, trimmed to the non-zero span. With steer = kappa != 0 the
-    directivity carries the phase of a phase reference off the origin,
-    exp(i kappa (sin theta_k - sin theta_b)) (complex D). Returns
-    (D complex64 [nB][nB], taps complex64, centre index)."""
+# Three-point Gauss-Legendre rule on [-1, 1]: exact for polynomials up to
+# degree 5, so for the (hat function x piecewise-linear beam) products of the
+# projection below.
+_GL3 = ((-math.sqrt(0.6), 5.0 / 9.0), (0.0, 8.0 / 9.0), (math.sqrt(0.6), 5.0 / 9.0))
+
+
+def grid_points(first: float, last: float, cells: int) -> np.ndarray:
+    """Bearings of the precision form's uniform grid, in float as the device
+    forms them: first + q * ((last - first) / (cells - 1))."""
+    step = F32(F32(F32(last) - F32(first)) / F32(cells - 1))
+    q = np.arange(cells, dtype=F32)
+    return (F32(first) + (q * step).astype(F32)).astype(F32)
+
+
+def project_directivity(grid: np.ndarray, bearings, beam, span: float, steer: float = 0.0) -> np.ndarray:
+    """Directivity of the binned model on a bearing grid: for each output
+    bearing b, the least-squares (L2) projection of its response
+    beam(theta - theta_b) * exp(i steer (sin theta - sin theta_b)) onto the
+    hat functions of the grid, i.e. the coefficients whose linear
+    interpolation between grid bearings is closest in mean square to the
+    per-sample response. The beam is the texture-equivalent lerp of the table
+    (border addressing); its knots split every grid interval, and each piece
+    is integrated with the three-point Gauss-Legendre rule (exact when steer
+    is 0). Returns complex128 [cells][nB]."""
+    g = np.asarray(grid, np.float64)
+    tb = np.asarray(bearings, np.float32).astype(np.float64)
+    tab = np.asarray(beam, np.float32).astype(np.float64)
+    W = tab.size
+    kx = float(np.float32(1.0) / np.float32(span)) * W
+    cx = 0.5 * W - 0.5
+    h = np.diff(g)                                        # [cells - 1]
+    xa = (g[:-1, None] - tb[None, :]) * kx + cx           # texel coordinate at each interval's ends
+    xb = (g[1:, None] - tb[None, :]) * kx + cx
+    k0 = np.floor(xa) + 1.0                               # first knot above xa
+    pieces = int(math.ceil(float(h.max()) * kx)) + 1
+    f = np.zeros((g.size, tb.size), np.complex128 if steer else np.float64)
+    sb = np.sin(tb)[None, :]
+    for m in range(pieces + 1):
+        lo = xa if m == 0 else np.minimum(k0 + (m - 1), xb)
+        hi = np.minimum(k0 + m, xb)
+        half = 0.5 * (hi - lo)
+        if not np.any(half > 0):
+            continue
+        mid = 0.5 * (hi + lo)
+        for node, weight in _GL3:
+            x = mid + half * node
+            th = tb[None, :] + (x - cx) / kx
+            val = _lerp(tab, x.ravel()).reshape(x.shape)
+            if steer:
+                val = val * np.exp(1j * steer * (np.sin(th) - sb))
+            wq = weight * half / kx * val                 # quadrature weight x response (d theta = dx / kx)
+            f[:-1] += wq * (g[1:, None] - th) / h[:, None]
+            f[1:] += wq * (th - g[:-1, None]) / h[:, None]
+    from scipy.linalg import solve_banded
+    ab = np.zeros((3, g.size))
+    ab[0, 1:] = h / 6.0
+    ab[2, :-1] = h / 6.0
+    ab[1, :-1] += h / 3.0
+    ab[1, 1:] += h / 3.0
+    return solve_banded((1, 1), ab, f)
+
+
+def precision_tables(sensor: dict, steer: float = 0.0, grid_count: int = 0, grid_first=None, grid_last=None) -> dict:
+    """Configuration of the binned precision model, derived from a 2D sensor's
+    tables as rtacx_configure_precision derives them when given NULL tables:
+    a uniform grid of `grid_count` bearings (default 4 x bearing_count) from
+    the first to the last table bearing, the directivity projected onto it
+    (project_directivity; with steer = kappa != 0 it carries the phase of a
+    phase reference off the origin and is complex), and the range taps
+    taps[t] = pulse((t - center) * resolution) for |t - center| <= overlap,
+    trimmed to the non-zero span. Returns the keyword arguments of
+    Context.configure_precision: directivity (complex64 [grid_count][nB]),
+    range_taps, tap_center, grid_count, grid_first, grid_last."""
     bear = np.asarray(sensor["bearings"], np.float32)
-    beam = np.asarray(sensor["beam"], np.float32).astype(np.float64)
-    W = beam.size
-    kx = float(np.float32(1.0) / np.float32(sensor["beam_span"])) * W
-    e = (bear[:, None] - bear[None, :]).astype(np.float32).astype(np.float64)
-    D = _lerp(beam, e * kx + 0.5 * W - 0.5)
-    if steer != 0.0:
-        sb = np.sin(bear.astype(np.float64))
-        D = D * np.exp(1j * steer * (sb[:, None] - sb[None, :]))
-    D = D.astype(np.complex64)
+    nB = bear.size
+    cells = int(grid_count) or 4 * nB
+    first = float(bear[0]) if grid_first is None else float(np.float32(grid_first))
+    last = float(bear[-1]) if grid_last is None else float(np.float32(grid_last))
+    g = grid_points(first, last, cells)
+    D = project_directivity(g, bear, sensor["beam"], sensor["beam_span"], steer).astype(np.complex64)
+    taps, center = range_taps(sensor)
+    return dict(directivity=D, range_taps=taps, tap_center=center, grid_count=cells,
+                grid_first=first, grid_last=last)
+
+
+def range_taps(sensor: dict):
+    """Range taps of the binned model: the pulse at whole-bin offsets t *
+    resolution, |t| <= overlap, trimmed to the non-zero span. Returns
+    (taps complex64, index of the zero offset)."""
     nR = sensor["range_count"]
     res = float(linspace_resolution(sensor["range_min"], sensor["range_max"], nR)) if nR > 1 else 0.0
     mres = np.float32(np.float32(sensor["range_max"]) - np.float32(sensor["range_min"]))
@@ -409,6 +493,6 @@ def precision_tables(sensor: dict, steer: float = 0.0):
     full = (_lerp(pulse.real, x) + 1j * _lerp(pulse.imag, x)).astype(np.complex64)
     nz = np.nonzero(full)[0]
     if nz.size == 0:
-        return D, np.zeros(1, np.complex64), 0
+        return np.zeros(1, np.complex64), 0
     first, last = nz[0], nz[-1]
-    return D, full[first:last + 1], int(ov - first)
+    return full[first:last + 1], int(ov - first)

@@ -91,7 +91,9 @@ def test_batch_full_size_mix(oracle):
         got = _complex(o)
         assert np.isfinite(got).all(), wk.name
         ref_ctx = make_context(wk)
-        assert rel_l2(got, gpu_reduce(ref_ctx, wk.samples, wk.out_shape)) <= 1e-6, wk.name
+        # Same arithmetic as the single-ping path up to the order of the float
+        # reductions (the batch splits hot tiles differently).
+        assert rel_l2(got, gpu_reduce(ref_ctx, wk.samples, wk.out_shape)) <= 1e-5, wk.name
         ref_ctx.close()
         nR = wk.sensor["range_count"]
         rows = (nR // 3, nR // 3 + 8)

@@ -23,8 +23,8 @@ def test_dropped_stage_times_out_and_context_recovers(oracle):
     wk = wl.precision_2d(n_samples=1 << 16, n_bearings=128, n_ranges=512)
     ctx = make_context(wk)
     ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
-    D, taps, c = wl.precision_tables(wk.sensor)
-    ctx.configure_precision(D, taps, c)
+    tab = wl.precision_tables(wk.sensor, **wk.precision)
+    ctx.configure_precision(**tab)
     d = to_device(wk.samples)
     out = torch.empty(tuple(wk.out_shape) + (2,), dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
@@ -41,5 +41,5 @@ def test_dropped_stage_times_out_and_context_recovers(oracle):
     ctx.stream_status(stream)
     o = out.cpu().numpy()
     got = o[..., 0].astype(np.float64) + 1j * o[..., 1]
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     assert rel_l2(got, want) <= 1e-4

@@ -1,6 +1,6 @@
 """Precision (tensor-core) form against the FP64 oracle of the binned model
 at <= 1e-4 relative L2, the FP64 echo pre-step of the plain form at 1e-5, and
-the model difference between the two forms (reported, not a parity bar)."""
+the binned model against the per-sample PSF of the plain form at <= 1e-2."""
 import numpy as np
 import pytest
 
@@ -27,13 +27,18 @@ def gpu_precision(ctx, samples, out_shape):
     return o[..., 0].astype(np.float64) + 1j * o[..., 1]
 
 
+def tables(wk, **kw):
+    """The workload's precision configuration (its steered complex
+    directivity where it has one)."""
+    return wl.precision_tables(wk.sensor, **{**wk.precision, **kw})
+
+
 def precision_context(wk, explicit=True, flags=0):
     ctx = make_context(wk)
     if wk.echo:
         ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
     if explicit:
-        D, taps, c = wl.precision_tables(wk.sensor)
-        ctx.configure_precision(D, taps, c, flags=flags)
+        ctx.configure_precision(**tables(wk), flags=flags)
     else:
         ctx.configure_precision(flags=flags)
     return ctx
@@ -49,9 +54,9 @@ def test_precision_matches_binned_fp64_oracle(oracle, maker):
     wk = maker()
     ctx = precision_context(wk)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
-    D, taps, c = wl.precision_tables(wk.sensor)
+    tab = tables(wk)
     smp = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
-    want = oracle.reduce_binned(smp, wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(smp, wk.sensor, tab)
     assert np.isfinite(got).all()
     err = rel_l2(got, want)
     assert err <= TOL, err
@@ -67,24 +72,25 @@ def test_precision_contexts_of_different_shapes_interleave(oracle):
     cs = precision_context(small)
     for wk, ctx in ((small, cs), (big, cb)):
         got = gpu_precision(ctx, wk.samples, wk.out_shape)
-        D, taps, c = wl.precision_tables(wk.sensor)
-        want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+        tab = tables(wk)
+        want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
         assert rel_l2(got, want) <= TOL
 
 def test_precision_full_size_rows(oracle):
     wk = wl.precision_2d()
     ctx = precision_context(wk)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
-    D, taps, c = wl.precision_tables(wk.sensor)
+    tab = tables(wk)
     smp = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
     rows = (1000, 1064)
-    want = oracle.reduce_binned(smp, wk.sensor, D, taps, c, rows=rows)
+    want = oracle.reduce_binned(smp, wk.sensor, tab, rows=rows)
     assert rel_l2(got[rows[0]:rows[1]], want) <= TOL
-    assert rel_l2(got[:64], oracle.reduce_binned(smp, wk.sensor, D, taps, c, rows=(0, 64))) <= TOL
+    assert rel_l2(got[:64], oracle.reduce_binned(smp, wk.sensor, tab, rows=(0, 64))) <= TOL
 
 
 def test_precision_derived_tables_match_explicit():
     wk = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512)
+    wk.precision = {}                  # the library derives the real (unsteered) directivity
     a = gpu_precision(precision_context(wk, explicit=True), wk.samples, wk.out_shape)
     b = gpu_precision(precision_context(wk, explicit=False), wk.samples, wk.out_shape)
     assert rel_l2(b, a) <= 1e-6
@@ -94,8 +100,8 @@ def test_precision_unaligned_shape_uses_copy_out(oracle):
     wk = wl.precision_2d(n_samples=1 << 14, n_bearings=77, n_ranges=130)
     ctx = precision_context(wk)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
-    D, taps, c = wl.precision_tables(wk.sensor)
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    tab = tables(wk)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     assert rel_l2(got, want) <= TOL
 
 
@@ -106,20 +112,6 @@ def test_plain_form_with_fp64_echo(oracle):
     got = gpu_reduce(ctx, wk.samples, wk.out_shape)
     want = oracle.reduce(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor)
     assert rel_l2(got, want) <= 1e-5
-
-
-def test_precision_vs_plain_model_difference(oracle):
-    # The binned model is not the per-sample PSF: report how far apart the
-    # two forms are on the same ping (bounded loosely, not a parity bar).
-    wk = wl.precision_2d(n_samples=1 << 16, n_ranges=1024)
-    ctx = precision_context(wk)
-    prec = gpu_precision(ctx, wk.samples, wk.out_shape)
-    ctx2 = make_context(wk)
-    ctx2.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
-    plain = gpu_reduce(ctx2, wk.samples, wk.out_shape)
-    diff = rel_l2(prec, plain)
-    print(f"binned vs per-sample model: rel-L2 {diff:.3e}")
-    assert diff < 1.5
 
 
 @pytest.mark.parametrize("form", ["plain", "precision"])
@@ -137,10 +129,10 @@ def test_compensated_phase_matches_fp64_oracle(oracle, form):
     else:
         ctx = make_context(wk)
         ctx.set_echo_model(wk.echo["carrier_hz"], flags)
-        D, taps, c = wl.precision_tables(wk.sensor)
-        ctx.configure_precision(D, taps, c)
+        tab = tables(wk)
+        ctx.configure_precision(**tab)
         got = gpu_precision(ctx, wk.samples, wk.out_shape)
-        assert rel_l2(got, oracle.reduce_binned(exact, wk.sensor, D, taps, c)) <= TOL
+        assert rel_l2(got, oracle.reduce_binned(exact, wk.sensor, tab)) <= TOL
 
 
 def gpu_precision_host(ctx, samples, out_shape, pinned=True):
@@ -175,8 +167,8 @@ def test_precision_host_entry_matches_device_entry(oracle, n):
     # two device runs), which moves the ping by ~1e-6 relative at 5M samples.
     assert rel_l2(host, dev) <= 1e-5
     if n <= 1 << 21:
-        D, taps, c = wl.precision_tables(wk.sensor)
-        want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+        tab = tables(wk)
+        want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, tab)
         assert rel_l2(host, want) <= TOL
 
 
@@ -199,8 +191,8 @@ def test_precision_fp16_rowscale_matches_binned_fp64_oracle(oracle, maker):
     the BF16 split's."""
     from rtac_simulation_gb300 import _lib
     wk = maker()
-    D, taps, c = wl.precision_tables(wk.sensor)
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    tab = tables(wk)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     got16 = gpu_precision(precision_context(wk, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE), wk.samples, wk.out_shape)
     gotbf = gpu_precision(precision_context(wk), wk.samples, wk.out_shape)
     assert np.isfinite(got16).all()
@@ -219,8 +211,8 @@ def test_precision_fp16_rowscale_wide_dynamic_range(oracle):
     scale = np.exp2(40.0 * (t - t.min()) / (t.max() - t.min()) - 20.0).astype(np.float32)
     smp[:, 0] *= scale
     smp[:, 1] *= scale
-    D, taps, c = wl.precision_tables(wk.sensor)
-    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    tab = tables(wk)
+    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, tab)
     got = gpu_precision(precision_context(wk, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE), smp, wk.out_shape)
     assert np.isfinite(got).all()
     # per-row relative error, so that the small rows count as much as the large ones
@@ -233,9 +225,9 @@ def test_precision_fp16_rowscale_wide_dynamic_range(oracle):
 def test_precision_long_pulse_multi_chunk_filter(oracle, flags):
     """101 range taps: the range filter stages its taps in several chunks."""
     wk = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512, taps=101)
-    D, taps, c = wl.precision_tables(wk.sensor)
-    assert taps.size > 64
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    tab = tables(wk)
+    assert tab["range_taps"].size > 64
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     got = gpu_precision(precision_context(wk, flags=flags), wk.samples, wk.out_shape)
     assert rel_l2(got, want) <= TOL
 
@@ -298,7 +290,7 @@ def test_precision_zero_amplitude_samples_open_windows(oracle):
     give non-empty windows, bin 200 alone gives the empty view."""
     wk = _small_precision()
     ctx = precision_context(wk)
-    D, taps, c = wl.precision_tables(wk.sensor)
+    tab = tables(wk)
     smp = wk.samples[:64].copy()
     smp[:, 2] = _bin_travel(oracle, wk.sensor, 200)
     zero = smp[:8].copy()
@@ -307,47 +299,50 @@ def test_precision_zero_amplitude_samples_open_windows(oracle):
     zero[:, 2] = _bin_travel(oracle, wk.sensor, 201)
     both = np.concatenate([smp, zero])
     got = gpu_precision(ctx, both, wk.out_shape)
-    want = oracle.reduce_binned(oracle.apply_echo(both, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(oracle.apply_echo(both, wk.sensor, wk.echo), wk.sensor, tab)
     assert np.linalg.norm(want) > 0
     assert rel_l2(got, want) <= TOL
     assert np.all(gpu_precision(ctx, smp, wk.out_shape) == 0)
 
 
 def test_precision_degenerate_bearings_match_oracle(oracle):
-    """NaN, infinite and out-of-table bearings clamp to the edge cells in the
-    kernel exactly as in the oracle's binary search."""
+    """Out-of-grid bearings clamp to the grid's end bearings; NaN and
+    infinite bearings contribute nothing (their bins still count as
+    non-empty), in the kernel as in the oracle."""
     wk = _small_precision()
     ctx = precision_context(wk)
-    D, taps, c = wl.precision_tables(wk.sensor)
+    tab = tables(wk)
     smp = wk.samples.copy()
     bad = np.array([np.nan, np.inf, -np.inf, 3.0, -3.0, 1e30], np.float32)
     smp[:bad.size * 64, 3] = np.repeat(bad, 64)
     got = gpu_precision(ctx, smp, wk.out_shape)
-    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, tab)
     assert np.isfinite(got).all()
     assert rel_l2(got, want) <= TOL
 
 
-@pytest.mark.parametrize("gap", [None, 1e-6])
-def test_precision_bearing_lookup_exact_and_searched(oracle, gap):
-    """The bearing lookup grid is exact (one table lookup, no search) when no
-    grid cell holds two interior bearings, and falls back to a corrected
-    search otherwise: a table with two bearings 1e-6 rad apart takes the
-    search. Both match the oracle's binary search, including samples placed
-    exactly on table bearings and just below them."""
+@pytest.mark.parametrize("grid", [None, (768, -1.3, 1.25), (130, 0.0, 0.0)])
+def test_precision_grid_edges(oracle, grid):
+    """Samples exactly on grid bearings and one ulp below them, outside the
+    grid (clamped to its end bearings), on the default grid and on explicit
+    ones (a grid wider than the fan, a coarse one), against the oracle's
+    restatement of the same float arithmetic."""
     wk = wl.precision_2d(n_samples=1 << 14, n_bearings=128, n_ranges=512)
-    b = np.array(wk.sensor["bearings"], dtype=np.float32)
-    if gap is not None:
-        b[60] = np.float32(b[61] - np.float32(gap))
-        wk.sensor["bearings"] = b
+    kw = {} if grid is None else dict(grid_count=grid[0], grid_first=grid[1], grid_last=grid[2])
+    if grid is not None and grid[1] == grid[2]:
+        kw = dict(grid_count=grid[0])
+    tab = tables(wk, **kw)
+    g = wl.grid_points(tab["grid_first"], tab["grid_last"], tab["grid_count"])
     smp = wk.samples.copy()
-    on = b[np.arange(smp.shape[0] // 4) % b.size]
-    smp[:on.size, 3] = on                                          # exactly on a bearing
-    smp[on.size:2 * on.size, 3] = np.nextafter(on, np.float32(-np.inf))   # just below it
-    ctx = precision_context(wk)
-    D, taps, c = wl.precision_tables(wk.sensor)
+    on = g[np.arange(smp.shape[0] // 4) % g.size]
+    smp[:on.size, 3] = on
+    smp[on.size:2 * on.size, 3] = np.nextafter(on, np.float32(-np.inf))
+    smp[2 * on.size:2 * on.size + 64, 3] = np.float32(1.5)      # beyond the last grid bearing
+    ctx = make_context(wk)
+    ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    ctx.configure_precision(**tab)
     got = gpu_precision(ctx, smp, wk.out_shape)
-    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(oracle.apply_echo(smp, wk.sensor, wk.echo), wk.sensor, tab)
     assert np.isfinite(got).all()
     assert rel_l2(got, want) <= TOL
 
@@ -360,9 +355,9 @@ def test_precision_partial_stage_and_unaligned_records(oracle, n):
     16-byte aligned (accumulated by the general kernel) give the same ping."""
     wk = wl.precision_2d(n_samples=n, n_bearings=128, n_ranges=512)
     ctx = precision_context(wk)
-    D, taps, c = wl.precision_tables(wk.sensor)
+    tab = tables(wk)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     assert np.isfinite(got).all()
     assert rel_l2(got, want) <= TOL
     d = to_device(wk.samples, offset_floats=1)
@@ -381,8 +376,8 @@ def test_precision_consecutive_pings_start_from_a_zero_grid(oracle):
     wk_a = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512, seed=5)
     wk_b = wl.precision_2d(n_samples=1 << 14, n_bearings=128, n_ranges=512, seed=6)
     ctx = precision_context(wk_a)
-    D, taps, c = wl.precision_tables(wk_a.sensor)
-    want = {id(w): oracle.reduce_binned(oracle.apply_echo(w.samples, w.sensor, w.echo), w.sensor, D, taps, c)
+    tab = tables(wk_a)
+    want = {id(w): oracle.reduce_binned(oracle.apply_echo(w.samples, w.sensor, w.echo), w.sensor, tab)
             for w in (wk_a, wk_b)}
     side = torch.cuda.Stream()
     for w, stream in ((wk_a, None), (wk_b, None), (wk_a, side), (wk_b, side), (wk_a, None)):
@@ -411,36 +406,62 @@ def test_precision_complex_directivity(oracle, fp16, kind):
     imaginary rows) against the FP64 oracle of the binned model."""
     from rtac_simulation_gb300 import _lib
     wk = wl.precision_2d(n_samples=1 << 18, n_ranges=1024)
-    D, taps, c = wl.precision_tables(wk.sensor, **wk.precision)
+    tab = tables(wk)
     if kind == "random_phase":
-        D = _random_phase(D)
-    assert np.abs(D.imag).max() > 0.03
+        tab["directivity"] = _random_phase(tab["directivity"])
+    assert np.abs(tab["directivity"].imag).max() > 0.03
+    flags = _lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0
     ctx = make_context(wk)
     ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
-    ctx.configure_precision(D, taps, c, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
+    ctx.configure_precision(**tab, flags=flags)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     assert np.isfinite(got).all()
     err = rel_l2(got, want)
     assert err <= TOL, err
     # The real-directivity ping differs: the imaginary half is really used.
-    Dr = D.real.astype(np.complex64)
-    ctx.configure_precision(Dr, taps, c, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
+    ctx.configure_precision(**{**tab, "directivity": tab["directivity"].real.astype(np.complex64)}, flags=flags)
     assert rel_l2(gpu_precision(ctx, wk.samples, wk.out_shape), want) > 100 * TOL
 
 
 @pytest.mark.parametrize("fp16", [False, True])
 def test_precision_complex_directivity_full_size_band(oracle, fp16):
     """The headline ping (2^24 samples, 512 x 4096, steered complex
-    directivity) against the binned FP64 oracle on two bands of rows."""
+    directivity on a 2048-bearing grid) against the binned FP64 oracle on two
+    bands of rows."""
     from rtac_simulation_gb300 import _lib
     wk = wl.precision_2d()
-    D, taps, c = wl.precision_tables(wk.sensor, **wk.precision)
+    tab = tables(wk)
     ctx = make_context(wk)
     ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
-    ctx.configure_precision(D, taps, c, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
+    ctx.configure_precision(**tab, flags=_lib.RTACX_PRECISION_FP16_ROWSCALE if fp16 else 0)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
     smp = oracle.apply_echo(wk.samples, wk.sensor, wk.echo)
     for rows in ((0, 32), (2500, 2532)):
-        want = oracle.reduce_binned(smp, wk.sensor, D, taps, c, rows=rows)
+        want = oracle.reduce_binned(smp, wk.sensor, tab, rows=rows)
         assert rel_l2(got[rows[0]:rows[1]], want) <= TOL, rows
+
+
+def per_sample_ping(ctx_plain, wk, steer):
+    """The plain form's per-sample ping with the steering phase of the
+    precision workload's directivity (samples rotated by exp(i kappa sin
+    theta_s), the ping by exp(-i kappa sin theta_b))."""
+    got = gpu_reduce(ctx_plain, wl.steer_samples(wk.samples, steer), wk.out_shape)
+    return wl.steer_ping(got, wk.sensor["bearings"], steer)
+
+
+@pytest.mark.parametrize("n_ranges", [1024, 4096])
+def test_precision_model_close_to_per_sample_psf(n_ranges):
+    """The binned model against the reference's per-sample PSF (the plain
+    form, itself within 1e-5 of the FP64 oracle) on the same ping: the
+    range split is the per-sample interpolation, the bearing grid of four
+    cells per output bearing with the projected directivity leaves about
+    5e-3 relative L2 (bar: 1e-2)."""
+    wk = wl.precision_2d(n_samples=1 << 18, n_ranges=n_ranges)
+    prec = gpu_precision(precision_context(wk), wk.samples, wk.out_shape)
+    plain_ctx = make_context(wk)
+    plain_ctx.set_echo_model(wk.echo["carrier_hz"], wk.echo["flags"])
+    plain = per_sample_ping(plain_ctx, wk, wk.precision["steer"])
+    diff = rel_l2(prec, plain)
+    print(f"binned vs per-sample model ({n_ranges} ranges): rel-L2 {diff:.3e}")
+    assert diff <= 1e-2, diff

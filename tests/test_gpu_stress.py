@@ -71,8 +71,8 @@ def test_stress_reduced_precision_matches_oracle(oracle):
     wk = wl.stress_2d(n_samples=1 << 20, n_ranges=2048)
     ctx = precision_context(wk)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
-    D, taps, c = wl.precision_tables(wk.sensor)
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    tab = wl.precision_tables(wk.sensor, **wk.precision)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     assert rel_l2(got, want) <= 1e-4
 
 
@@ -88,8 +88,8 @@ def test_stress_reduced_precision_hot_range_matches_oracle(oracle, flags_name):
         flags |= _lib.RTACX_PRECISION_FP16_ROWSCALE
     wk = wl.stress_2d(n_samples=1 << 20, n_ranges=2048)
     ctx = precision_context(wk, flags=flags)
-    D, taps, c = wl.precision_tables(wk.sensor)
-    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, D, taps, c)
+    tab = wl.precision_tables(wk.sensor, **wk.precision)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     got = gpu_precision(ctx, wk.samples, wk.out_shape)
     assert rel_l2(got, want) <= 1e-4
     host = gpu_precision_host(ctx, wk.samples, wk.out_shape)
