@@ -71,6 +71,20 @@ typedef int rtacx_status;
  * (one texture fetch per sample and output cell). The batched and the
  * allocation-free entry points do not take it (RTACX_ERR_UNSUPPORTED). */
 #define RTACX_FLAG_TEXTURE_PSF 2u
+/* On a 1D sensor (rtacx_sensor_1d.flags) RTACX_FLAG_TEXTURE_PSF fetches the
+ * pulse as the reference's 1D kernel does (tex1D of a one-row float2 texture,
+ * linear filter, normalized coordinates; src/SensorInstance1D.cu:15-33,
+ * include/rtac_simulation/ReductionKernel.h:44-55). The reference sets
+ * neither filter nor address mode there, so both are rtac_base defaults that
+ * are not vendored: border addressing is taken, or clamp addressing with
+ * RTACX_FLAG_TEXTURE_CLAMP as well. Measured on the reference's own kernel:
+ * with border addressing the fetch blends the pulse row with the zero row
+ * beyond it and returns half the pulse; with clamp addressing it returns the
+ * pulse, extended by its edge taps outside the table. rtacx_reduce then
+ * reproduces the reference's 1D pings in either mode to float round-off.
+ * Without the flags the 1D pulse is the exact linear interpolation of the
+ * table, zero outside it (the evident intent). */
+#define RTACX_FLAG_TEXTURE_CLAMP 4u
 
 /* 1D echosounder (SensorInstance1D, include/rtac_simulation/SensorInstance1D.h). */
 typedef struct {

@@ -319,13 +319,20 @@ void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void*
         }
     }
     else if((mode == 2 || mode == 3) && S.dims == 1) {
-        // Texture-unit emulation (1D): the linear fetch of the pulse table
-        // with the texture unit's per-axis weight (texel_weight) at the
-        // kernel's coordinate fmaf(scale, delta, 0.5)
-        // (include/rtac_simulation/ReductionKernel.h:44-55), border (mode 2)
-        // or clamp (mode 3) addressing -- the reference's 1D texture takes
-        // rtac_base's defaults (src/SensorInstance1D.cu:15-25), which are not
-        // vendored; accumulation in double.
+        // Texture-unit emulation (1D): the reference's tex1D fetch of its
+        // one-row pulse texture (include/rtac_simulation/ReductionKernel.h:
+        // 44-55) at the kernel's coordinate fmaf(scale, delta, 0.5), linear
+        // filter, normalized coordinates, border (mode 2) or clamp (mode 3)
+        // addressing -- the reference's 1D texture takes rtac_base's
+        // defaults (src/SensorInstance1D.cu:15-25), which are not vendored.
+        // Measured on GB300 (the reference's own kernel, recorded in
+        // tests/golden/ref_pings_1d.npz): the fetch filters the missing
+        // second axis as a one-texel axis sampled at its texel edge, so the
+        // pulse row is blended half-and-half with the row beyond it. With
+        // clamp addressing that row is the pulse row again (a plain linear
+        // fetch); with border addressing it is zero and the value is halved.
+        // The bilinear corner weights follow texel_weight's rule with the
+        // second axis' weight b = 128; accumulation in double.
         std::complex<double>* o = static_cast<std::complex<double>*>(out_row);
         auto texel = [&](int j) -> std::complex<double> {
             if(mode == 3) j = std::min(std::max(j, 0), H - 1);
@@ -336,9 +343,16 @@ void reduce_row(const Sensor& S, const BinResult& B, uint32_t r, int mode, void*
         for(uint32_t k = 0; k < size; k++) {
             const SortedSample& s = B.sorted[off + k];
             const float uy = std::fmaf(S.pulse_scale, s.travel - R, 0.5f);
-            int c;
-            const int j = texel_weight(uy, H, c);
-            const std::complex<double> w = ((double)(256 - c) * texel(j) + (double)c * texel(j + 1)) / 256.0;
+            int a;
+            const int j = texel_weight(uy, H, a);
+            std::complex<double> w;
+            if(mode == 3) {
+                w = ((double)(256 - a) * texel(j) + (double)a * texel(j + 1)) / 256.0;
+            }
+            else {
+                const int b = 128, w11 = (a * b + 128) >> 8, w01 = b - w11;   // the pulse row's corners
+                w = ((double)w01 * texel(j) + (double)w11 * texel(j + 1)) / 256.0;
+            }
             acc += std::complex<double>(s.re, s.im) * w;
         }
         o[0] = acc;

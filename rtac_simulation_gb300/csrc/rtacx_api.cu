@@ -74,6 +74,43 @@ rtacx_status make_psf_texture(Context& c, const rtacx_sensor_2d* s)
     return RTACX_OK;
 }
 
+// The reference's 1D pulse texture (SensorInstance1D::generate_psf_data,
+// src/SensorInstance1D.cu:15-25): the waveform's taps as a one-row float2
+// texture with linear filtering and normalized coordinates; the address mode
+// is an rtac_base default (border, or clamp with RTACX_FLAG_TEXTURE_CLAMP).
+// KernelView1D scaling {scale, 0.5} (src/SensorInstance1D.cu:27-33).
+rtacx_status make_pulse_texture_1d(Context& c, const rtacx_sensor_1d* s, float scale)
+{
+    const cudaChannelFormatDesc ch = cudaCreateChannelDesc<float2>();
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] =
+        (s->flags & RTACX_FLAG_TEXTURE_CLAMP) ? cudaAddressModeClamp : cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    if(cudaMallocArray(&c.psf_array, &ch, s->pulse_len, 0) != cudaSuccess ||
+       cudaMemcpy2DToArray(c.psf_array, 0, 0, s->pulse, s->pulse_len * sizeof(float2), s->pulse_len * sizeof(float2),
+                           1, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        c.error = "cannot upload the pulse texture (texture width limit)";
+        return RTACX_ERR_CUDA;
+    }
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = c.psf_array;
+    if(cudaCreateTextureObject(&c.psf_tex, &rd, &td, nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        c.psf_tex = 0;
+        c.error = "cannot create the pulse texture";
+        return RTACX_ERR_CUDA;
+    }
+    c.tex_xscale = 0.0f;
+    c.tex_yscale = scale;
+    return RTACX_OK;
+}
+
 void free_config(Context& c)
 {
     free_precision(c);
@@ -243,6 +280,11 @@ rtacx_status rtacx_configure_1d(rtacx_ctx* ctx, const rtacx_sensor_1d* s)
     if(!s) { c.error = "null sensor"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(set_device(c) != RTACX_OK) return RTACX_ERR_CUDA;
     free_config(c);
+    if(s->flags & ~(RTACX_FLAG_1D_LITERAL_SCALING | RTACX_FLAG_TEXTURE_PSF | RTACX_FLAG_TEXTURE_CLAMP) ||
+       ((s->flags & RTACX_FLAG_TEXTURE_CLAMP) && !(s->flags & RTACX_FLAG_TEXTURE_PSF))) {
+        c.error = "unknown 1D sensor flags (RTACX_FLAG_TEXTURE_CLAMP needs RTACX_FLAG_TEXTURE_PSF)";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
     const bool literal = (s->flags & RTACX_FLAG_1D_LITERAL_SCALING) != 0;
     const float scale = host_pulse_scale(s->pulse_duration, s->sound_celerity, literal);
     Common cm{s->range_min, s->range_max, s->sound_celerity, s->pulse_duration, s->margin,
@@ -261,6 +303,14 @@ rtacx_status rtacx_configure_1d(rtacx_ctx* ctx, const rtacx_sensor_1d* s)
     std::vector<float> one(1, 0.0f);
     if(!upload(c, c.d_beam, one.data(), 1) || !upload(c, c.d_bearings, one.data(), 1) || !allocate_bins(c))
         return RTACX_ERR_OUT_OF_MEMORY;
+    if((s->flags & RTACX_FLAG_TEXTURE_PSF) && make_pulse_texture_1d(c, s, scale) != RTACX_OK) return RTACX_ERR_CUDA;
+    if(s->flags & RTACX_FLAG_TEXTURE_CLAMP) {
+        // Clamp addressing gives every sample of the window the pulse's edge
+        // taps, so each row reads its whole reference window, not only the
+        // bins that hold the pulse's support.
+        std::vector<int2> whole(c.nR, make_int2(0, (int)c.nR - 1));
+        if(!upload(c, c.d_support, whole.data(), whole.size())) return RTACX_ERR_OUT_OF_MEMORY;
+    }
     c.configured = true;
     return RTACX_OK;
 }

@@ -140,8 +140,8 @@ extern "C" rtacx_status rtacx_reduce_noalloc(int sample_kind, const void* sensor
     if(!(std::isfinite(rmin) && std::isfinite(rmax) && std::isfinite(margin))) return RTACX_ERR_INVALID_ARGUMENT;
     if(!(duration > 0.0f) || !(c > 0.0f) || !std::isfinite(duration * c)) return RTACX_ERR_INVALID_ARGUMENT;
     if(!finite_all(pulse, 2 * (size_t)H)) return RTACX_ERR_INVALID_ARGUMENT;
+    if(flags & (RTACX_FLAG_TEXTURE_PSF | RTACX_FLAG_TEXTURE_CLAMP)) return RTACX_ERR_UNSUPPORTED;
     if(two_d) {
-        if(flags & RTACX_FLAG_TEXTURE_PSF) return RTACX_ERR_UNSUPPORTED;
         if(!s2->beam || W == 0 || !s2->bearings || nB == 0) return RTACX_ERR_INVALID_ARGUMENT;
         if(!(s2->beam_span > 0.0f) || !std::isfinite(s2->beam_span)) return RTACX_ERR_INVALID_ARGUMENT;
         if(!finite_all(s2->beam, W) || !finite_all(s2->bearings, nB)) return RTACX_ERR_INVALID_ARGUMENT;

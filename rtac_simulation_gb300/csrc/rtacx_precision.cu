@@ -49,26 +49,45 @@ constexpr int kHotRows = 256, kHotReplicas = 8;
 constexpr int kAccLoads = 4;                     // independent record loads per thread in flight
 constexpr int kAccEchoModels = 6;                // echo models of the staged accumulation
 
-__device__ __forceinline__ void red_add_v4(float2* addr, float4 v)
+// L2 eviction priorities (createpolicy): the sample stream is read once
+// and marked evict-first, the grid's reductions evict-last, so that the
+// grid (68 MB on the 512 x 4096 ping) stays in L2 while 268 MB of samples
+// stream past it.
+__device__ __forceinline__ uint64_t policy_evict_first()
 {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w));
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
 }
 
-__device__ __forceinline__ void red_add_v2(float2* addr, float2 v)
+__device__ __forceinline__ uint64_t policy_evict_last()
 {
-    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(v.x), "f"(v.y));
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ void red_add_v4(float2* addr, float4 v, uint64_t pol)
+{
+    asm volatile("red.global.add.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;"
+                 ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol));
+}
+
+__device__ __forceinline__ void red_add_v2(float2* addr, float2 v, uint64_t pol)
+{
+    asm volatile("red.global.add.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(addr), "f"(v.x), "f"(v.y), "l"(pol));
 }
 
 // Adds a sample's share (1 - w) v to grid bearing q and w v to q + 1 of one
 // grid row. An even q starts a 16-byte pair: one vector reduction; an odd q
 // straddles two pairs: two 8-byte reductions. The grid is never read by the
 // kernels that reduce into it, so the reductions carry no memory clobber.
-__device__ __forceinline__ void deposit(float2* row, int q, float w, float2 v)
+__device__ __forceinline__ void deposit(float2* row, int q, float w, float2 v, uint64_t pol)
 {
     const float w0 = 1.0f - w;
     const float2 a = make_float2(w0 * v.x, w0 * v.y), b = make_float2(w * v.x, w * v.y);
-    if((q & 1) == 0) red_add_v4(row + q, make_float4(a.x, a.y, b.x, b.y));
-    else { red_add_v2(row + q, a); red_add_v2(row + q + 1, b); }
+    if((q & 1) == 0) red_add_v4(row + q, make_float4(a.x, a.y, b.x, b.y), pol);
+    else { red_add_v2(row + q, a, pol); red_add_v2(row + q + 1, b, pol); }
 }
 
 size_t accumulate_smem_bytes(uint32_t nR)
@@ -97,6 +116,7 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p, Gr
         return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * cells : G + (size_t)jg * cells;
     };
     const uint32_t words = (p.key.nR + 31) / 32;
+    const uint64_t keep = policy_evict_last();
     for(uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_bits[i] = 0u;
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -119,8 +139,8 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p, Gr
             if(!grid_coords(g, rec[u].z, rec[u].w, jg, alpha, q, w)) continue;
             const float2 v = apply_echo(p, make_float2(rec[u].x, rec[u].y), rec[u].z);
             const float a0 = 1.0f - alpha;
-            deposit(grid_row(jg), q, w, make_float2(a0 * v.x, a0 * v.y));
-            deposit(grid_row(jg + 1), q, w, make_float2(alpha * v.x, alpha * v.y));
+            deposit(grid_row(jg), q, w, make_float2(a0 * v.x, a0 * v.y), keep);
+            deposit(grid_row(jg + 1), q, w, make_float2(alpha * v.x, alpha * v.y), keep);
         }
     }
     __syncthreads();
@@ -167,6 +187,7 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
     const uint32_t words = (p.key.nR + 31) / 32;
     const uint64_t stages = (n + kStageRecs - 1) / kStageRecs;
     const uint32_t cells = g.cells;
+    const uint64_t stream_pol = policy_evict_first(), keep = policy_evict_last();
     auto issue = [&](uint64_t c, int slot) {
         if(c == drop_stage) return;      // failure-path test: this stage's copy never comes
         const uint64_t first = c * kStageRecs;
@@ -174,8 +195,10 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
         const uint32_t bytes = (uint32_t)(left < (uint64_t)kStageRecs ? left : (uint64_t)kStageRecs) * (uint32_t)sizeof(float4);
         const uint32_t bar = smem_u32(&s_full[slot]);
         mbar_expect_tx(bar, bytes);
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(s_ring + slot * kStageRecs)), "l"(samples + first), "r"(bytes), "r"(bar)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+                     " [%0], [%1], %2, [%3], %4;"
+                     ::"r"(smem_u32(s_ring + slot * kStageRecs)), "l"(samples + first), "r"(bytes), "r"(bar),
+                       "l"(stream_pol)
                      : "memory");
     };
     if(threadIdx.x == 0) {
@@ -230,8 +253,8 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
             if(key[u] != kOutOfRange) atomicOr(&s_bits[key[u] >> 5], 1u << (key[u] & 31));
             if(row[u] >= 0) {
                 float2* r0 = G + (size_t)row[u] * cells;
-                deposit(r0, cell[u], wgt[u], make_float2(add[u].x, add[u].y));
-                deposit(r0 + cells, cell[u], wgt[u], make_float2(add[u].z, add[u].w));
+                deposit(r0, cell[u], wgt[u], make_float2(add[u].x, add[u].y), keep);
+                deposit(r0 + cells, cell[u], wgt[u], make_float2(add[u].z, add[u].w), keep);
             }
         }
         if(aborted) break;
@@ -515,11 +538,13 @@ size_t filter_smem_bytes(uint32_t ntaps)
 // 1][b] (C row j holds grid row j: absolute range row j - tap_center - 1),
 // or 0 when row r's reference window is empty. One CTA per 64 rows x 64
 // bearings; per chunk of up to 64 taps the C rows it needs are staged in
-// shared memory once (column cc = 32 h + lane stored at (cc & 1) * 32 + cc /
-// 2, so that lane l reads columns 2l and 2l + 1 from two conflict-free
-// planes). Each warp filters 8 rows x 64 bearings with a sliding window of
-// eight staged rows per column in registers: one shared load per tap and
-// column.
+// shared memory once, row-major: every warp first loads all of its rows
+// (up to 16, two 256-byte row segments each) and only then stores them, so
+// the loads are in flight together. Lane l owns columns l and l + 32; each
+// warp filters 8 rows with a sliding window of eight staged rows per column
+// in registers (one shared load per tap and column).
+constexpr int kFiltRowsPerWarp = (kFiltRows + kFiltTapsMax - 1 + 7) / 8;
+
 __global__ void __launch_bounds__(kFiltThreads, 2)
 k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, const uint32_t* __restrict__ nonempty,
               int ov, const float2* __restrict__ taps, uint32_t ntaps, uint32_t nR, uint32_t nB,
@@ -542,14 +567,25 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, cons
         const int rows_s = kFiltRows + nt - 1;
         __syncthreads();
         if(tid < nt) sT[tid] = taps[tc + tid];
-        for(int rr = warp; rr < rows_s; rr += kFiltThreads / 32) {
+        float2 v[kFiltRowsPerWarp][2];
+#pragma unroll
+        for(int i = 0; i < kFiltRowsPerWarp; i++) {
+            const int rr = warp + 8 * i;
             const uint32_t j = (uint32_t)(r0 + tc + rr + 1);        // C row of staged row rr
-            const float2* row = C + (size_t)(j < c_rows ? j : 0) * ldc2;
+            const bool live = rr < rows_s && j < c_rows;
+            const float2* row = C + (size_t)(live ? j : 0) * ldc2;
 #pragma unroll
             for(int h = 0; h < 2; h++) {
                 const int k = k0 + 32 * h + lane;
-                const float2 c = (j < c_rows && k < (int)nB) ? row[k] : make_float2(0.f, 0.f);
-                sG[rr * kFiltCols + (lane & 1) * 32 + 16 * h + (lane >> 1)] = c;
+                v[i][h] = (live && k < (int)nB) ? __ldg(row + k) : make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for(int i = 0; i < kFiltRowsPerWarp; i++) {
+            const int rr = warp + 8 * i;
+            if(rr < rows_s) {
+                sG[rr * kFiltCols + lane] = v[i][0];
+                sG[rr * kFiltCols + 32 + lane] = v[i][1];
             }
         }
         __syncthreads();
@@ -590,19 +626,15 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, cons
             }
         }
     }
-    const int k = k0 + 2 * lane;
-    const bool pair = (nB & 1u) == 0u && k + 1 < (int)nB;
 #pragma unroll
     for(int q = 0; q < 8; q++) {
         const int r = r0 + warp * 8 + q;
-        if(r >= (int)nR || k >= (int)nB) continue;
+        if(r >= (int)nR) continue;
         const bool on = sW[warp * 8 + q] != 0;
-        const float2 v0 = on ? acc[q][0] : make_float2(0.f, 0.f), v1 = on ? acc[q][1] : make_float2(0.f, 0.f);
-        float2* o = out + (size_t)r * nB + k;
-        if(pair) *reinterpret_cast<float4*>(o) = make_float4(v0.x, v0.y, v1.x, v1.y);
-        else {
-            o[0] = v0;
-            if(k + 1 < (int)nB) o[1] = v1;
+#pragma unroll
+        for(int h = 0; h < 2; h++) {
+            const int k = k0 + 32 * h + lane;
+            if(k < (int)nB) out[(size_t)r * nB + k] = on ? acc[q][h] : make_float2(0.f, 0.f);
         }
     }
 }

@@ -335,6 +335,38 @@ k_gather_tex(const float4* __restrict__ sorted, const uint32_t* __restrict__ off
     if(lane == 0) out[cell] = acc;
 }
 
+// RTACX_FLAG_TEXTURE_PSF on a 1D sensor: one warp per output range r, the
+// lanes stride over row r's window and fetch the pulse as the reference's 1D
+// kernel does, tex1D at fmaf(scale, t_s - R_r, 0.5)
+// (src/SensorInstance1D.cu:52-55, include/rtac_simulation/ReductionKernel.h:
+// 44-55); value * pulse in complex float, a warp reduction writes the row.
+__global__ void __launch_bounds__(kThreads)
+k_gather_tex_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ off, const int2* __restrict__ win,
+                const float* __restrict__ ranges, cudaTextureObject_t pulse, float scale, uint32_t nR,
+                float2* __restrict__ out)
+{
+    const uint32_t r = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if(r >= nR) return;
+    const int2 w = win[r];
+    float2 acc = make_float2(0.f, 0.f);
+    if(w.x <= w.y) {
+        const float R = ranges[r];
+        const uint32_t p0 = off[w.x], p1 = off[w.y + 1];
+        for(uint32_t i = p0 + lane; i < p1; i += 32) {
+            const float4 s = sorted[i];
+            const float2 f = tex1D<float2>(pulse, fmaf(scale, s.z - R, 0.5f));
+            acc.x += s.x * f.x - s.y * f.y;
+            acc.y += s.x * f.y + s.y * f.x;
+        }
+    }
+    for(int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if(lane == 0) out[r] = acc;
+}
+
 // ---- split persistent gather of one 2D ping -------------------------------
 // k_tile_parts counts each output tile's sample stream (same definition as
 // gather_tile_2d) and splits it into parts of at most kPartSamples samples
@@ -560,6 +592,13 @@ size_t gather_smem_bytes(uint32_t range_tile, uint32_t bearing_tile, uint32_t H,
 rtacx_status run_reduce(Context& ctx, float* out_f, cudaStream_t stream)
 {
     float2* out = reinterpret_cast<float2*>(out_f);
+    if(ctx.dims == 1 && ctx.psf_tex) {
+        k_gather_tex_1d<<<(ctx.nR + kWarps - 1) / kWarps, kThreads, 0, stream>>>(
+            ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_ranges, ctx.psf_tex, ctx.tex_yscale, ctx.nR, out);
+        const cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess) { ctx.error = std::string("k_gather_tex_1d: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+        return RTACX_OK;
+    }
     if(ctx.dims == 1) {
         const size_t smem = (ctx.H + 2) * sizeof(float2);
         if(smem > 48 * 1024) raise_smem_limit((const void*)k_gather_1d, smem);

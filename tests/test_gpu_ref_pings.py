@@ -76,3 +76,33 @@ def test_full_size_ping_against_the_live_reference_kernel(tmp_path):
     assert rel_l2(tex, ref) <= 1e-6
     exact = gpu_reduce(make_context(wk), wk.samples, wk.out_shape)
     assert rel_l2(exact, ref) <= REF_PINGS_TOL_EXACT
+
+
+def test_plain_1d_against_reference_kernel_pings(oracle):
+    """The 1D form against pings of the reference's own 1D kernel
+    (tests/golden/ref_pings_1d.npz), with the evident-intent scaling 1 /
+    (duration c) and, under RTACX_FLAG_1D_LITERAL_SCALING, the literal
+    1.0f / duration * c:
+      * RTACX_FLAG_TEXTURE_PSF (border) and | RTACX_FLAG_TEXTURE_CLAMP fetch
+        the pulse as the reference does and reproduce its pings in either
+        address mode to float round-off;
+      * k_gather_1d (exact weights, zero outside the table) is twice the
+        border-mode ping up to the texture weights' quantization, and meets
+        the FP64 oracle at the plain form's 1e-5."""
+    from rtac_simulation_gb300 import _lib
+    from test_oracle_golden import REF_PINGS_TOL_EXACT_1D, ref_ping_cases_1d
+    from rtac_simulation_gb300 import workloads as wl
+    seen = 0
+    for name, smp, sensor, literal, address, ref in ref_ping_cases_1d():
+        wk = wl.Workload(name, 1, sensor, smp)
+        base = _lib.RTACX_FLAG_1D_LITERAL_SCALING if literal else 0
+        tex_flags = base | _lib.RTACX_FLAG_TEXTURE_PSF | (_lib.RTACX_FLAG_TEXTURE_CLAMP if address else 0)
+        tex = gpu_reduce(make_context(wk, flags=tex_flags), smp, wk.out_shape)
+        assert np.isfinite(tex).all(), name
+        assert rel_l2(tex, ref) <= 1e-6, (name, rel_l2(tex, ref))
+        if address == 0:
+            got = gpu_reduce(make_context(wk, flags=base), smp, wk.out_shape)
+            assert rel_l2(got, 2.0 * ref) <= REF_PINGS_TOL_EXACT_1D, (name, rel_l2(got, 2.0 * ref))
+            assert rel_l2(got, oracle.reduce(smp, sensor, literal_1d=literal)) <= 1e-5, name
+        seen += 1
+    assert seen == 8

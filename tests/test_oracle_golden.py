@@ -135,3 +135,57 @@ def test_oracle_exact_psf_against_reference_kernel(oracle):
         err = _rel(exact, ref)
         # Non-zero (the texture quantization is real) and within its envelope.
         assert 1e-5 < err <= REF_PINGS_TOL_EXACT, (name, err)
+
+
+def ref_ping_cases_1d():
+    """(name, samples, sensor, literal scaling, address mode, reference ping)
+    of tests/golden/ref_pings_1d.npz, rebuilt as the recording script built
+    them (tests/golden/make_ref_pings.py --1d)."""
+    import ast
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_ref_pings", GOLDEN / "make_ref_pings.py")
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    z = np.load(GOLDEN / "ref_pings_1d.npz")
+    out = []
+    for name in sorted({k.split("__")[0] for k in z.files}):
+        builder = str(z[f"{name}__builder"])
+        kwargs = dict(ast.literal_eval(str(z[f"{name}__kwargs"])))
+        literal = bool(z[f"{name}__literal"])
+        smp, sensor = mk.case_samples_1d(builder, kwargs, literal)
+        out.append((name, smp, sensor, literal, int(z[f"{name}__address"]),
+                    z[f"{name}__ping"].astype(np.complex128)))
+    return out
+
+
+def test_oracle_texture_mode_reproduces_reference_1d_kernel(oracle):
+    """The reference's own 1D kernel (do_sparse_convolve_1d_f, compiled from
+    src/SensorInstance1D.cu and run on a GB300) under both address modes its
+    unvendored texture defaults allow and both PSF scalings: the oracle's
+    texture emulation (mode 2 border, mode 3 clamp) reproduces every ping."""
+    cases = ref_ping_cases_1d()
+    assert len(cases) == 8
+    for name, smp, sensor, literal, address, ref in cases:
+        assert np.linalg.norm(ref) > 0, name
+        got = oracle.reduce(smp, sensor, mode=3 if address else 2, literal_1d=literal)
+        assert _rel(got, ref) <= REF_PINGS_TOL_TEXTURE, (name, _rel(got, ref))
+
+
+# The 1D envelope: the quantized texture weights move a 65-tap aliased tone
+# (echosounder_1d) by up to ~1e-2 relative L2.
+REF_PINGS_TOL_EXACT_1D = 1.5e-2
+
+
+def test_oracle_exact_1d_psf_against_reference_kernel(oracle):
+    """With border addressing the reference's 1D fetch returns half the
+    pulse (the one-row texture is blended with the zero row beyond it): twice
+    its ping is the exact-weight FP64 oracle up to the texture weights'
+    quantization. With clamp addressing the pulse is extended by its edge
+    taps, which the exact PSF (zero outside the table) does not do."""
+    for name, smp, sensor, literal, address, ref in ref_ping_cases_1d():
+        exact = oracle.reduce(smp, sensor, mode=0, literal_1d=literal)
+        if address == 0:
+            err = _rel(exact, 2.0 * ref)
+            assert err <= REF_PINGS_TOL_EXACT_1D, (name, err)
+        else:
+            assert _rel(exact, ref) > 1e-2, name
