@@ -51,8 +51,15 @@ DEFAULT_CONFIG = "precision_2d"
 #       python bench.py --steps 2 --warmup 3 --no-cpu-baseline [--no-next-rows]
 # on a GB300. Reported as `traffic` beside the live `achieved` numbers.
 NCU_TRAFFIC_BYTES = {
+    "k_prec_accumulate_staged": 335.812e6 + 4.319e6,
+    "k_gemm_tn": 129.070e6 + 4.018e6,
     "sort_bin": (268.531e6 + 3.186e6) + (274.855e6 + 223.261e6),   # k_count + k_scatter_staged
 }
+# The accumulation's bound is the L2's reduction throughput, not HBM: ncu on
+# the default workload (profiles/k_prec_accumulate_staged_precision_2d.md)
+# shows 3.06 L2 reduction sectors per sample and the L2 at 77 % of its peak
+# throughput while DRAM carries the algorithmic bytes once.
+NCU_ACCUMULATE_L2 = {"l2_throughput_pct": 77.0, "l2_atomic_input_pct": 48.7, "red_sectors_per_sample": 3.06}
 
 KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
 PRECISION_KERNELS_PER_PING = 5   # clear, staged accumulate, operand split, tensor-core GEMM, range filter
@@ -362,14 +369,18 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # Single stream: one ping after the other (the per-ping latency).
+    # Single stream, one ping after the other: the timed throughput (and the
+    # per-ping latency).
+    clocks.begin()
     ev0.record(stream)
     for _ in range(steps):
         call(d_in, n, out, stream=stream)
     ev1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     t_single = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
-    # Two pings in flight (precision forms): the timed throughput.
+    # Two pings in flight (precision forms), reported beside it: consecutive
+    # pings alternate between two contexts on two streams.
     dev_lanes = [(ctx, stream, out)]
     if alt and form != "plain":
         dev_lanes.append((alt[0], torch.cuda.Stream(), alt[2]))
@@ -383,7 +394,6 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clocks.begin()
     ev0.record(stream)
     for _, s, _ in dev_lanes[1:]:
         s.wait_event(ev0)
@@ -395,12 +405,12 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
         stream.wait_event(done)
     ev1.record(stream)
     torch.cuda.synchronize()
-    clocks.end()
     clk = clocks.stop()
     for c, s, _ in dev_lanes:
         c.stream_status(s)
     ctx.stream_status(stream)
-    t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
+    t_two = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
+    t_dev = t_single
 
     ctx.set_tracing(True)
     names = _lib.STAGES if form == "plain" else _lib.PRECISION_STAGES
@@ -466,8 +476,8 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     e2e_split = {"h2d_ms": evs[0].elapsed_time(evs[1]), "ping_ms": evs[1].elapsed_time(evs[2]),
                  "d2h_ms": evs[2].elapsed_time(evs[3]), "e2e_step_ms": 1e3 * t_e2e / steps}
-    return dict(t_dev=t_dev, t_single=t_single, stage=stage, t_e2e=t_e2e, clocks=clk, e2e_split=e2e_split,
-                lanes=len(dev_lanes))
+    return dict(t_dev=t_dev, t_single=t_single, t_two=t_two, stage=stage, t_e2e=t_e2e, clocks=clk,
+                e2e_split=e2e_split, lanes=len(dev_lanes))
 
 
 def time_next_rows(torch, local, peaks, reps=20, warmup=3):
@@ -661,7 +671,7 @@ def run_ours(args, world, rank, local):
     def form_line(f):
         r = res[f]
         return {"samples_per_s": world * n * r["steps"] / r["t_dev"], "ms_per_step": 1e3 * r["t_dev"] / r["steps"],
-                "pings_in_flight": r["lanes"], "latency_ms_single_stream": 1e3 * r["t_single"] / r["steps"],
+                "ms_per_step_two_in_flight": 1e3 * r["t_two"] / r["steps"] if r["lanes"] > 1 else None,
                 "e2e_samples_per_s": world * n * r["steps"] / r["t_e2e"], "steps": r["steps"],
                 "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()},
                 "e2e_step_ms": {k: round(v, 4) for k, v in r["e2e_split"].items()},
@@ -681,8 +691,9 @@ def run_ours(args, world, rank, local):
                             if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
                    "l2": ("inputs larger than L2 (%.0f MB of samples)" if n * rec_in > 129e6 else
                           "inputs smaller than L2 (%.0f MB of samples): timed warm, not flushed") % (n * rec_in / 1e6),
-                   "timing": ("two pings in flight (two contexts on two streams, consecutive pings alternate); "
-                              "latency_ms = one ping at a time on one stream" if head == "precision" else
+                   "timing": ("one ping at a time on one stream (two pings in flight on two streams measured "
+                              "beside it: forms.*.ms_per_step_two_in_flight; slower, the second ping's GEMM "
+                              "contends with the accumulation's L2 reductions)" if head == "precision" else
                               "one ping at a time on one stream"),
                    "e2e_path": ("rtacx_reduce_precision_host from pinned host memory, two pings in flight "
                                 "(two contexts, two streams)" if head == "precision" else
@@ -725,7 +736,11 @@ def run_ours(args, world, rank, local):
                     "frac": acc_gbs / peaks["hbm_gbs"], "traffic": ncu.get("k_prec_accumulate_staged"),
                     "kernel": "k_prec_accumulate_staged",
                     "peak_source": peaks["source"],
-                    "algorithmic": f"{rec_in} B per sample read + 8 B per grid cell ({rows_g} x {cells})"}
+                    "algorithmic": f"{rec_in} B per sample read + 8 B per grid cell ({rows_g} x {cells})",
+                    "l2_bound": dict(NCU_ACCUMULATE_L2, reductions_per_s=NCU_ACCUMULATE_L2["red_sectors_per_sample"]
+                                     * n / (ps["accumulate"] / 1e3),
+                                     note="bound by the L2's reduction rate (4 complex values per sample "
+                                          "reduced into a 68 MB L2-resident grid); HBM carries the samples once")}
         roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": gemm_tf / peaks["bf16_tflops"], "traffic": ncu.get("k_gemm_tn"), "kernel": "k_gemm_tn",
                      "peak_source": peaks["source"],
