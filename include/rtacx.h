@@ -333,14 +333,20 @@ rtacx_status rtacx_rasterize(rtacx_ctx* ctx, const rtacx_mesh* mesh, const rtacx
 
 /* Batched plain form: many pings from heterogeneous sensors (each bound to
  * its own configured 1D or 2D context, whose scratch it uses) in one CUDA
- * graph: one launch per binning stage covering every ping, then one
- * persistent gather kernel that takes output tiles of all pings from an
- * atomic work counter, heaviest first. The reference has no batching
- * (one SensorInstance::compute_output per ping, each kernel followed by a
- * device sync). rtacx_batch_plan binds the pings (samples, counts, outputs
- * are baked into the graph: re-plan when any of them changes) and, with
+ * graph holding ONE kernel: a cooperative persistent launch (every CTA
+ * resident) that zeroes, counts, scans, windows, scatters and gathers every
+ * ping, taking work from atomic queues (gather tiles heaviest first) and
+ * separating the phases with grid barriers whose waits are bounded (about
+ * 1 s): a CTA that gives up sets the batch status word and stops, and so
+ * does every other CTA at the next barrier (rtacx_batch_status reports it;
+ * the pings are then incomplete; the next run starts clean). With
+ * RTACX_BATCH_STAGED the graph holds one launch per binning stage and a
+ * persistent gather instead. The reference has no batching (one
+ * SensorInstance::compute_output per ping, each kernel followed by a device
+ * sync). rtacx_batch_plan binds the pings (samples, counts, outputs are baked
+ * into the graph: re-plan when any of them changes) and, with
  * RTACX_BATCH_AUTOTUNE, times every candidate gather tile shape x samples
- * per binning CTA on this batch and keeps the fastest. rtacx_batch_run
+ * per binning chunk on this batch and keeps the fastest. rtacx_batch_run
  * replays the graph on `stream`. Results equal rtacx_reduce's per ping. */
 typedef struct rtacx_batch rtacx_batch;
 typedef struct {
@@ -350,11 +356,25 @@ typedef struct {
     float* out;              /* device ping (complex64)                   */
 } rtacx_ping_desc;
 #define RTACX_BATCH_AUTOTUNE 1u
+#define RTACX_BATCH_STAGED   2u
 rtacx_status rtacx_batch_create(rtacx_batch** batch, int device);
 void rtacx_batch_destroy(rtacx_batch* batch);
 const char* rtacx_batch_last_error(const rtacx_batch* batch);
 rtacx_status rtacx_batch_plan(rtacx_batch* batch, const rtacx_ping_desc* pings, uint32_t count, uint32_t flags);
 rtacx_status rtacx_batch_run(rtacx_batch* batch, void* stream);
+/* Wait for `stream` and report the batch status word (RTACX_ERR_DEVICE if a
+ * grid-barrier wait of a run expired since the last check; clears it). The
+ * per-ping device error words stay on the pings' contexts
+ * (rtacx_stream_status). */
+rtacx_status rtacx_batch_status(rtacx_batch* batch, void* stream);
+/* Number of kernel nodes in the planned graph (1 for the fused form). */
+rtacx_status rtacx_batch_graph_kernels(const rtacx_batch* batch, uint32_t* kernels);
+/* Diagnostic for the failure path (no counterpart in the reference), taken
+ * into account by the next rtacx_batch_plan: the fused kernel's grid barriers
+ * wait for `extra_arrivals` (0 or 1) more CTAs than the launch has, so with 1
+ * the first barrier never completes and every CTA gives up after `wait_ms`
+ * (1..10000; default 1000) and returns. */
+rtacx_status rtacx_diag_batch_barrier(rtacx_batch* batch, uint32_t extra_arrivals, uint32_t wait_ms);
 /* The plan's choice: gather tile rows x bearings, samples per binning CTA,
  * and the autotuned batch time in ms (0 without autotuning). */
 rtacx_status rtacx_batch_tuning(const rtacx_batch* batch, uint32_t* tile_rows, uint32_t* tile_bearings,

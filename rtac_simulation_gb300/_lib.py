@@ -91,9 +91,13 @@ SIGNATURES = {
     "rtacx_batch_run": (_I, [_P, _P]),
     "rtacx_batch_tuning": (_I, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_U32), ctypes.POINTER(_U32),
                                 ctypes.POINTER(ctypes.c_float)]),
+    "rtacx_batch_status": (_I, [_P, _P]),
+    "rtacx_batch_graph_kernels": (_I, [_P, ctypes.POINTER(_U32)]),
+    "rtacx_diag_batch_barrier": (_I, [_P, _U32, _U32]),
 }
 
 RTACX_BATCH_AUTOTUNE = 1
+RTACX_BATCH_STAGED = 2
 RTACX_DIRECTIVITY_RECTANGLE = 1
 RTACX_DIRECTIVITY_DISK = 2
 
@@ -368,15 +372,32 @@ class Batch:
             msg = self._lib.rtacx_batch_last_error(self._h)
             raise RtacxError(st, msg.decode() if msg else "")
 
-    def plan(self, pings, autotune: bool = True) -> None:
-        """pings: sequence of (Context, samples tensor, n, out tensor)."""
+    def plan(self, pings, autotune: bool = True, staged: bool = False) -> None:
+        """pings: sequence of (Context, samples tensor, n, out tensor). staged:
+        one launch per binning stage instead of the fused single launch."""
         arr = (PingDesc * len(pings))()
         for i, (ctx, smp, n, out) in enumerate(pings):
             arr[i] = PingDesc(ctx.handle, _ptr(smp), n, _ptr(out))
-        self._check(self._lib.rtacx_batch_plan(self._h, arr, len(pings), RTACX_BATCH_AUTOTUNE if autotune else 0))
+        flags = (RTACX_BATCH_AUTOTUNE if autotune else 0) | (RTACX_BATCH_STAGED if staged else 0)
+        self._check(self._lib.rtacx_batch_plan(self._h, arr, len(pings), flags))
 
     def run(self, stream=None) -> None:
         self._check(self._lib.rtacx_batch_run(self._h, _stream(stream)))
+
+    def status(self, stream=None) -> None:
+        """Waits for the stream; raises RtacxError (RTACX_ERR_DEVICE) if a
+        grid-barrier wait of a run expired."""
+        self._check(self._lib.rtacx_batch_status(self._h, _stream(stream)))
+
+    def graph_kernels(self) -> int:
+        k = _U32()
+        self._check(self._lib.rtacx_batch_graph_kernels(self._h, ctypes.byref(k)))
+        return k.value
+
+    def diag_barrier(self, extra_arrivals: int, wait_ms: int = 1000) -> None:
+        """Diagnostic (next plan): barriers wait for extra_arrivals more CTAs
+        than the launch has; each wait gives up after wait_ms."""
+        self._check(self._lib.rtacx_diag_batch_barrier(self._h, extra_arrivals, wait_ms))
 
     def tuning(self) -> dict:
         r, b, p = _U32(), _U32(), _U32()

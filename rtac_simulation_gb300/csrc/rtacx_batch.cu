@@ -3,15 +3,20 @@
 // A batch holds up to thousands of pings, each bound to its own configured
 // context (1D or 2D). rtacx_batch_plan builds, once:
 //   * a device descriptor per ping (PingDev: its samples, scratch, tables);
-//   * (ping, index) maps that let one launch per binning stage cover every
-//     ping (reset of the totals, count, bin scan, scatter, windows);
+//   * (ping, index) maps of the binning work of every ping (totals to zero,
+//     count / scatter chunks, bin-scan blocks, window row groups);
 //   * the gather work list: 2D output tiles and 1D row groups of every ping,
-//     heaviest first, consumed by one persistent kernel through an atomic
-//     work counter;
-// then captures the whole sequence into a CUDA graph. rtacx_batch_run replays
-// it with one cudaGraphLaunch. With RTACX_BATCH_AUTOTUNE the plan times every
-// candidate (gather tile shape x samples per binning CTA) on the real batch
-// and keeps the fastest.
+//     heaviest first;
+// then captures the batch into a CUDA graph. By default the graph holds one
+// kernel: k_batch_fused, a cooperative persistent launch (one or two CTAs per
+// SM, all resident) that runs every phase of every ping, taking work from
+// atomic queues and separating the phases with bounded grid barriers (and a
+// 24-byte memset node that resets the barrier and the queues). With
+// RTACX_BATCH_STAGED the graph holds one launch per binning stage and a
+// persistent gather kernel instead. rtacx_batch_run replays the graph with one
+// cudaGraphLaunch. With RTACX_BATCH_AUTOTUNE the plan times every candidate
+// (gather tile shape x samples per binning chunk) on the real batch and keeps
+// the fastest.
 #include "rtacx_internal.cuh"
 
 #include <algorithm>
@@ -43,11 +48,21 @@ struct Batch {
     uint2* d_chunk_map = nullptr;
     uint2* d_col_map = nullptr;
     uint2* d_win_map = nullptr;
+    uint2* d_scan_map = nullptr;
     uint4* d_items = nullptr;
     uint32_t* d_counter = nullptr;
-    uint32_t n_chunks = 0, n_col = 0, n_win = 0, n_items = 0, max_bins = 0;
+    BatchSync* d_sync = nullptr;
+    uint32_t* d_status = nullptr;
+    uint32_t n_chunks = 0, n_col = 0, n_win = 0, n_scan = 0, n_items = 0, max_bins = 0;
     size_t gather_smem = 0;
     uint32_t gather_grid = 0;
+    bool staged = false;            // RTACX_BATCH_STAGED
+    FusedBatch fb{};
+    size_t fused_smem = 0;
+    uint32_t fused_grid = 0;
+    uint32_t graph_kernels = 0;     // kernel nodes of the captured graph
+    uint32_t diag_extra = 0;        // extra barrier arrivals (diagnostic)
+    uint32_t wait_ms = 1000;        // bound of one grid-barrier wait
     Candidate chosen{2, 4096};
     float tuned_ms = 0.0f;
     cudaGraphExec_t exec = nullptr;
@@ -59,7 +74,8 @@ struct Batch {
     {
         if(exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
-        drop(d_pings); drop(d_chunk_map); drop(d_col_map); drop(d_win_map); drop(d_items);
+        drop(d_pings); drop(d_chunk_map); drop(d_col_map); drop(d_win_map); drop(d_scan_map); drop(d_items);
+        graph_kernels = 0;
     }
 
     template <typename T>
@@ -82,7 +98,7 @@ struct Batch {
         free_plan();
         const int TR = gather_shape_rows(cand.shape), TB = gather_shape_bearings(cand.shape);
         std::vector<PingDev> descs;
-        std::vector<uint2> chunk_map, col_map, win_map;
+        std::vector<uint2> chunk_map, col_map, win_map, scan_map;
         struct Item { uint4 v; double cost; };
         std::vector<Item> items;
         max_bins = 1;
@@ -106,6 +122,7 @@ struct Batch {
             for(uint32_t k = 0; k < d.chunks; k++) chunk_map.push_back(make_uint2(i, k));
             for(uint32_t k = 0; k < ceil_div(c.bin.nBins, 256); k++) col_map.push_back(make_uint2(i, k));
             for(uint32_t k = 0; k < ceil_div(c.nR, 256); k++) win_map.push_back(make_uint2(i, k));
+            for(uint32_t k = 0; k < ceil_div(c.bin.nBins, kScanBlock); k++) scan_map.push_back(make_uint2(i, k));
             max_bins = std::max(max_bins, c.bin.nBins);
             const double density = (double)n / c.nR;     // samples per range bin
             if(c.dims == 2) {
@@ -123,19 +140,54 @@ struct Batch {
         std::vector<uint4> iv(items.size());
         for(size_t k = 0; k < items.size(); k++) iv[k] = items[k].v;
         n_chunks = (uint32_t)chunk_map.size(); n_col = (uint32_t)col_map.size();
-        n_win = (uint32_t)win_map.size(); n_items = (uint32_t)iv.size();
+        n_win = (uint32_t)win_map.size(); n_scan = (uint32_t)scan_map.size(); n_items = (uint32_t)iv.size();
         if(!put(d_pings, descs) || !put(d_chunk_map, chunk_map) || !put(d_col_map, col_map) ||
-           !put(d_win_map, win_map) || !put(d_items, iv))
+           !put(d_win_map, win_map) || !put(d_scan_map, scan_map) || !put(d_items, iv))
             return RTACX_ERR_OUT_OF_MEMORY;
         if(gather_smem > 227 * 1024) { error = "PSF tables too large for the batched gather"; return RTACX_ERR_UNSUPPORTED; }
-        if((size_t)max_bins * 4 > 227 * 1024) { error = "histograms too large for the batched binning"; return RTACX_ERR_UNSUPPORTED; }
-        gather_grid = (uint32_t)sm_count * (gather_smem <= 100 * 1024 ? 2u : 1u);
+        if(staged && (size_t)max_bins * 4 > 227 * 1024) { error = "histograms too large for the batched binning"; return RTACX_ERR_UNSUPPORTED; }
         chosen = cand;
+        return staged ? capture_staged(cand, (uint32_t)descs.size()) : capture_fused(cand);
+    }
+
+    // Graph of the fused form: reset of the barrier and queues, one
+    // cooperative launch.
+    rtacx_status capture_fused(const Candidate& cand)
+    {
+        fused_smem = gather_smem;
+        rtacx_status prep = prepare_fused_batch(error, cand.shape, fused_smem, sm_count, fused_grid);
+        if(prep != RTACX_OK) return prep;
+        fb = FusedBatch{};
+        fb.pings = d_pings;
+        fb.col_map = d_col_map; fb.n_col = n_col;
+        fb.chunk_map = d_chunk_map; fb.n_chunks = n_chunks;
+        fb.scan_map = d_scan_map; fb.n_scan = n_scan;
+        fb.win_map = d_win_map; fb.n_win = n_win;
+        fb.items = d_items; fb.n_items = n_items;
+        fb.sync = d_sync;
+        fb.status = d_status;
+        fb.arrivals = fused_grid + diag_extra;
+        fb.wait_ns = (unsigned long long)wait_ms * 1000000ull;
+        cudaGraph_t graph = nullptr;
+        if(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            error = "cudaStreamBeginCapture failed";
+            return RTACX_ERR_CUDA;
+        }
+        rtacx_status st = RTACX_OK;
+        if(cudaMemsetAsync(d_sync, 0, sizeof(BatchSync), stream) != cudaSuccess) st = RTACX_ERR_CUDA;
+        if(st == RTACX_OK) st = launch_fused_batch(error, cand.shape, fb, fused_smem, fused_grid, stream);
+        return finish_capture(st, graph);
+    }
+
+    // Graph of the staged form: reset of the work counter, five binning
+    // launches, one persistent gather.
+    rtacx_status capture_staged(const Candidate& cand, uint32_t n_pings)
+    {
+        gather_grid = (uint32_t)sm_count * (gather_smem <= 100 * 1024 ? 2u : 1u);
         rtacx_status prep = prepare_bin_batch(error, max_bins);
         if(prep == RTACX_OK) prep = prepare_gather_batch(error, cand.shape, gather_smem);
         if(prep != RTACX_OK) return prep;
-
-        // Capture: reset the work counter, five binning launches, one gather.
         cudaGraph_t graph = nullptr;
         if(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             cudaGetLastError();
@@ -145,21 +197,42 @@ struct Batch {
         rtacx_status st = RTACX_OK;
         if(cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), stream) != cudaSuccess) st = RTACX_ERR_CUDA;
         if(st == RTACX_OK)
-            st = launch_bin_batch(error, d_pings, (uint32_t)descs.size(), d_chunk_map, n_chunks, d_col_map, n_col,
+            st = launch_bin_batch(error, d_pings, n_pings, d_chunk_map, n_chunks, d_col_map, n_col,
                                   d_win_map, n_win, max_bins, stream);
         if(st == RTACX_OK)
             st = launch_gather_batch(error, cand.shape, d_pings, d_items, n_items, d_counter, gather_smem, gather_grid,
                                      stream);
+        return finish_capture(st, graph);
+    }
+
+    rtacx_status finish_capture(rtacx_status st, cudaGraph_t graph)
+    {
         const cudaError_t ec = cudaStreamEndCapture(stream, &graph);
         if(st != RTACX_OK || ec != cudaSuccess) {
             cudaGetLastError();
             if(graph) cudaGraphDestroy(graph);
-            if(st == RTACX_OK) { error = "stream capture failed"; st = RTACX_ERR_CUDA; }
+            if(st == RTACX_OK) { error = std::string("stream capture failed: ") + cudaGetErrorString(ec); st = RTACX_ERR_CUDA; }
             return st;
         }
+        size_t n_nodes = 0;
+        graph_kernels = 0;
+        if(cudaGraphGetNodes(graph, nullptr, &n_nodes) == cudaSuccess && n_nodes) {
+            std::vector<cudaGraphNode_t> nodes(n_nodes);
+            if(cudaGraphGetNodes(graph, nodes.data(), &n_nodes) == cudaSuccess)
+                for(size_t k = 0; k < n_nodes; k++) {
+                    cudaGraphNodeType t;
+                    if(cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) graph_kernels++;
+                }
+        }
+        cudaGetLastError();
         const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
-        if(ei != cudaSuccess) { cudaGetLastError(); exec = nullptr; error = "cudaGraphInstantiate failed"; return RTACX_ERR_CUDA; }
+        if(ei != cudaSuccess) {
+            cudaGetLastError();
+            exec = nullptr;
+            error = std::string("cudaGraphInstantiate failed: ") + cudaGetErrorString(ei);
+            return RTACX_ERR_CUDA;
+        }
         return RTACX_OK;
     }
 
@@ -205,7 +278,10 @@ rtacx_status rtacx_batch_create(rtacx_batch** out, int device)
     B.device = device;
     if(cudaDeviceGetAttribute(&B.sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
        cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking) != cudaSuccess ||
-       cudaMalloc(&B.d_counter, sizeof(uint32_t)) != cudaSuccess) {
+       cudaMalloc(&B.d_counter, sizeof(uint32_t)) != cudaSuccess ||
+       cudaMalloc(&B.d_sync, sizeof(BatchSync)) != cudaSuccess ||
+       cudaMalloc(&B.d_status, sizeof(uint32_t)) != cudaSuccess ||
+       cudaMemset(B.d_status, 0, sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
         rtacx_batch_destroy(b);
         return RTACX_ERR_CUDA;
@@ -221,6 +297,8 @@ void rtacx_batch_destroy(rtacx_batch* b)
     cudaSetDevice(B.device);
     B.free_plan();
     B.drop(B.d_counter);
+    B.drop(B.d_sync);
+    B.drop(B.d_status);
     if(B.stream) cudaStreamDestroy(B.stream);
     delete b;
 }
@@ -251,6 +329,7 @@ rtacx_status rtacx_batch_plan(rtacx_batch* b, const rtacx_ping_desc* pings, uint
         if(!ensure_capacity(c, p.n)) { B.error = c.error; return RTACX_ERR_OUT_OF_MEMORY; }
     }
     B.pings.assign(pings, pings + count);
+    B.staged = (flags & RTACX_BATCH_STAGED) != 0;
     if(!(flags & RTACX_BATCH_AUTOTUNE)) {
         const rtacx_status st = B.build(Candidate{2, 4096});
         B.tuned_ms = 0.0f;
@@ -283,6 +362,43 @@ rtacx_status rtacx_batch_run(rtacx_batch* b, void* stream)
         B.error = "cudaGraphLaunch failed";
         return RTACX_ERR_CUDA;
     }
+    return RTACX_OK;
+}
+
+rtacx_status rtacx_batch_status(rtacx_batch* b, void* stream)
+{
+    if(!b) return RTACX_ERR_INVALID_ARGUMENT;
+    Batch& B = b->impl;
+    if(cudaSetDevice(B.device) != cudaSuccess) { cudaGetLastError(); B.error = "cudaSetDevice failed"; return RTACX_ERR_CUDA; }
+    const cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if(e != cudaSuccess) { B.error = std::string("stream: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    uint32_t word = 0;
+    if(cudaMemcpy(&word, B.d_status, sizeof(word), cudaMemcpyDeviceToHost) != cudaSuccess ||
+       cudaMemset(B.d_status, 0, sizeof(word)) != cudaSuccess) {
+        cudaGetLastError();
+        B.error = "reading the batch status word failed";
+        return RTACX_ERR_CUDA;
+    }
+    if(word) {
+        B.error = "batch status word " + std::to_string(word) +
+                  ((word & kErrBatchWaitTimeout) ? " (a grid-barrier wait expired; the batch's pings are incomplete)" : "");
+        return RTACX_ERR_DEVICE;
+    }
+    return RTACX_OK;
+}
+
+rtacx_status rtacx_batch_graph_kernels(const rtacx_batch* b, uint32_t* kernels)
+{
+    if(!b || !kernels) return RTACX_ERR_INVALID_ARGUMENT;
+    *kernels = b->impl.exec ? b->impl.graph_kernels : 0u;
+    return RTACX_OK;
+}
+
+rtacx_status rtacx_diag_batch_barrier(rtacx_batch* b, uint32_t extra_arrivals, uint32_t wait_ms)
+{
+    if(!b || wait_ms == 0 || wait_ms > 10000 || extra_arrivals > 1) return RTACX_ERR_INVALID_ARGUMENT;
+    b->impl.diag_extra = extra_arrivals;
+    b->impl.wait_ms = wait_ms;
     return RTACX_OK;
 }
 

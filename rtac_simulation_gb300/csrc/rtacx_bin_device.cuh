@@ -13,8 +13,6 @@ namespace rtacx {
 
 namespace {
 
-constexpr uint32_t kScanBlock = 1024;   // bins per CTA of the parallel bin scan
-
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 constexpr int kTileLoads = 4;        // independent record loads per thread and tile
@@ -218,20 +216,31 @@ __device__ __forceinline__ void window_row(const uint32_t* __restrict__ off, uin
 }
 
 // Exclusive scan of bins [blk kScanBlock, (blk + 1) kScanBlock) of
-// totals[0, nBins), offset by the sum of the block sums before it
-// (totals[nBins + j], j < blk, accumulated by the count pass). Writes
-// offsets (and offsets[nBins] from the block holding the last bin) and the
-// scatter's per-bin cursors. Each thread scans kScanBlock / blockDim.x
-// consecutive bins; blockDim.x divides kScanBlock.
+// totals[0, nBins), offset by the count of every bin before the block: the
+// sum of the block sums before it (totals[nBins + j], j < blk, accumulated by
+// the count pass) when block_sums, else the sum of totals[0, blk kScanBlock)
+// taken by the whole CTA. Writes offsets (and offsets[nBins] from the block
+// holding the last bin) and the scatter's per-bin cursors. Each thread scans
+// kScanBlock / blockDim.x consecutive bins; blockDim.x divides kScanBlock.
 __device__ __forceinline__ void scan_bin_block(const uint32_t* __restrict__ totals, uint32_t nBins, uint32_t blk,
                                                uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursor,
-                                               uint32_t* s_warp, uint32_t* s_prefix)
+                                               uint32_t* s_warp, uint32_t* s_prefix, bool block_sums = true)
 {
-    if(threadIdx.x < 32) {
+    if(block_sums) {
+        if(threadIdx.x < 32) {
+            uint32_t s = 0;
+            for(uint32_t j = threadIdx.x; j < blk; j += 32) s += totals[nBins + j];
+            for(int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if(threadIdx.x == 0) *s_prefix = s;
+        }
+    }
+    else {
+        if(threadIdx.x == 0) *s_prefix = 0u;
+        __syncthreads();
         uint32_t s = 0;
-        for(uint32_t j = threadIdx.x; j < blk; j += 32) s += totals[nBins + j];
+        for(uint32_t i = threadIdx.x; i < blk * kScanBlock; i += blockDim.x) s += totals[i];
         for(int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if(threadIdx.x == 0) *s_prefix = s;
+        if(lane_id() == 0 && s) atomicAdd(s_prefix, s);
     }
     const uint32_t per = kScanBlock / blockDim.x;
     const uint32_t b0 = blk * kScanBlock + threadIdx.x * per;
@@ -249,6 +258,65 @@ __device__ __forceinline__ void scan_bin_block(const uint32_t* __restrict__ tota
         o += v;
         if(b == nBins - 1) offsets[nBins] = o;
     }
+}
+
+// Count pass of chunk c of nc straight into totals[0, nBins) with one global
+// atomic per sample (no shared histogram: the fused batched kernel keeps its
+// shared memory for the gather). Out-of-range counts as count_chunk.
+__device__ __forceinline__ void count_chunk_global(const float* __restrict__ samples, uint64_t n, const BinParams& p,
+                                                   uint32_t c, uint32_t nc, uint32_t* __restrict__ totals,
+                                                   unsigned long long* __restrict__ oor, unsigned long long* s_oor)
+{
+    if(threadIdx.x < 2) s_oor[threadIdx.x] = 0ull;
+    __syncthreads();
+    uint32_t low = 0, high = 0;
+    for_chunk(samples, n, p, c, nc, [&](const bool* valid, const float4*, const uint32_t* key, const int* side) {
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            if(valid[u] && key[u] != kOutOfRange) atomicAdd(&totals[key[u]], 1u);
+            else if(valid[u]) {
+                if(side[u] < 0) low++; else high++;
+            }
+        }
+    });
+    for(int o = 16; o > 0; o >>= 1) {
+        low += __shfl_down_sync(0xffffffffu, low, o);
+        high += __shfl_down_sync(0xffffffffu, high, o);
+    }
+    if(lane_id() == 0 && (low | high)) {
+        atomicAdd(&s_oor[0], (unsigned long long)low);
+        atomicAdd(&s_oor[1], (unsigned long long)high);
+    }
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        if(s_oor[0]) atomicAdd(&oor[0], s_oor[0]);
+        if(s_oor[1]) atomicAdd(&oor[1], s_oor[1]);
+    }
+}
+
+// Scatter pass of chunk c of nc with one global atomic per sample on its
+// bin's cursor (no shared histogram); positions past the counted total set
+// kErrScatterOverflow instead of being written.
+__device__ __forceinline__ void scatter_chunk_global(const float* __restrict__ samples, uint64_t n, const BinParams& p,
+                                                     uint32_t c, uint32_t nc, uint32_t* __restrict__ cursor,
+                                                     const uint32_t* __restrict__ offsets, float4* __restrict__ sorted,
+                                                     uint32_t* __restrict__ err)
+{
+    const uint32_t total = offsets[p.nBins];
+    for_chunk(samples, n, p, c, nc, [&](const bool* valid, const float4* rec, const uint32_t* key, const int*) {
+#pragma unroll
+        for(int u = 0; u < kTileLoads; u++) {
+            if(!valid[u] || key[u] == kOutOfRange) continue;
+            const uint32_t pos = atomicAdd(&cursor[(size_t)key[u] * kCursorStride], 1u);
+            float4 out = rec[u];
+            if(p.echo_flags) {
+                const float2 v = apply_echo(p, make_float2(out.x, out.y), out.z);
+                out.x = v.x; out.y = v.y;
+            }
+            if(pos < total) sorted[pos] = out;
+            else atomicOr(err, kErrScatterOverflow);
+        }
+    });
 }
 
 } // namespace

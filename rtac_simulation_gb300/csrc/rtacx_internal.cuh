@@ -15,6 +15,7 @@ namespace rtacx {
 // Words between two bins' write cursors: one 128-byte L2 line per bin, so the
 // scatter's run reservations spread over all L2 slices.
 constexpr uint32_t kCursorStride = 32;
+constexpr uint32_t kScanBlock = 1024;     // bins per block of the parallel bin scan
 constexpr uint32_t kOutOfRange = RTACX_KEY_OUT_OF_RANGE;
 
 // Device error word bits (OR-ed by kernels, read by rtacx_stream_status).
@@ -22,6 +23,7 @@ constexpr uint32_t kErrScatterOverflow = 1u << 0;  // sorted position beyond the
 constexpr uint32_t kErrBadWindow       = 1u << 1;  // window bounds outside the sorted array
 constexpr uint32_t kErrGemmTimeout     = 1u << 2;  // a bounded mbarrier wait of the tensor-core GEMM expired
 constexpr uint32_t kErrAccumulateTimeout = 1u << 3; // a bounded wait for a staged copy of samples expired
+constexpr uint32_t kErrBatchWaitTimeout  = 1u << 4; // a bounded grid-barrier wait of the fused batched kernel expired
 
 // Largest (range bin x bearing bin) histogram a CTA keeps in shared memory.
 constexpr uint32_t kMaxSmemBins = 49152;
@@ -302,6 +304,29 @@ struct PingDev {
     float2* out;
 };
 
+// Grid-barrier and work-queue state of the fused batched kernel (zeroed
+// before every launch): barrier arrivals and generation, then one work
+// counter per dynamically scheduled phase (count, scan, scatter, gather).
+struct BatchSync {
+    uint32_t arrived;
+    uint32_t generation;
+    uint32_t next[4];
+};
+
+// Parameters of the fused batched kernel. Maps are (ping, index) pairs.
+struct FusedBatch {
+    const PingDev* pings;
+    const uint2* col_map;   uint32_t n_col;      // 256-bin groups of the totals to zero
+    const uint2* chunk_map; uint32_t n_chunks;   // chunks of the count and scatter passes
+    const uint2* scan_map;  uint32_t n_scan;     // kScanBlock-bin blocks of the bin scan
+    const uint2* win_map;   uint32_t n_win;      // 256-row groups of the windows
+    const uint4* items;     uint32_t n_items;    // gather items (2D tiles, 1D row groups)
+    BatchSync* sync;
+    uint32_t* status;                            // batch error word
+    uint32_t arrivals;                           // CTAs each grid barrier waits for
+    unsigned long long wait_ns;                  // bound of one barrier wait
+};
+
 // Scratch and configuration owned by one context.
 struct Context {
     int device = 0;
@@ -449,6 +474,11 @@ size_t gather_batch_smem(int shape, uint32_t H, uint32_t W);
 rtacx_status launch_gather_batch(std::string& error, int shape, const PingDev* pings, const uint4* items,
                                  uint32_t n_items, uint32_t* counter, size_t smem, uint32_t grid,
                                  cudaStream_t stream);
+// Fused batched form: the whole batch (zeroing, count, scan, windows,
+// scatter, gather) in one cooperative persistent launch.
+rtacx_status prepare_fused_batch(std::string& error, int shape, size_t smem, int sm_count, uint32_t& grid);
+rtacx_status launch_fused_batch(std::string& error, int shape, const FusedBatch& fb, size_t smem, uint32_t grid,
+                                cudaStream_t stream);
 int gather_shape_rows(int shape);
 int gather_shape_bearings(int shape);
 

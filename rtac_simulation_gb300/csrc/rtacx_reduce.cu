@@ -19,6 +19,7 @@
 // once, then every thread accumulates its (rows x bearings) register block:
 // acc[r][b] += U[k][r] * B[k][b]. A warp skips a chunk whose range bins lie
 // outside its rows' windows.
+#include "rtacx_bin_device.cuh"
 #include "rtacx_internal.cuh"
 
 #include <algorithm>
@@ -534,7 +535,207 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
     return RTACX_OK;
 }
 
+// ---- fused batched form -----------------------------------------------------
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier of the cooperative launch (every CTA is resident). Thread 0
+// of each CTA publishes the CTA's writes (fence), arrives, and waits for the
+// generation to move; the last arrival resets the count and advances the
+// generation. The wait is bounded by fb.wait_ns of the global timer: a CTA
+// that gives up sets kErrBatchWaitTimeout in the batch status word and the
+// whole CTA returns false. A barrier passed by any CTA had every arrival, so
+// the data of the phase before it is complete; a CTA that gave up does no
+// further work, so no later barrier completes and every CTA stops at it.
+__device__ __forceinline__ bool grid_barrier(const FusedBatch& fb, int* s_ok)
+{
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        int ok = 1;
+        const uint32_t gen = ld_acquire_gpu(&fb.sync->generation);
+        __threadfence();
+        if(atomicAdd(&fb.sync->arrived, 1u) + 1u == fb.arrivals) {
+            atomicExch(&fb.sync->arrived, 0u);
+            __threadfence();
+            atomicAdd(&fb.sync->generation, 1u);
+        }
+        else {
+            const unsigned long long t0 = global_ns();
+            while(ld_acquire_gpu(&fb.sync->generation) == gen) {
+                if(global_ns() - t0 > fb.wait_ns) {
+                    atomicOr(fb.status, kErrBatchWaitTimeout);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(200);
+            }
+        }
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// Next item of a dynamically scheduled phase (one atomicAdd per item, no
+// waiting); the leading barrier frees the shared memory of the last item.
+__device__ __forceinline__ uint32_t claim(uint32_t* counter, uint32_t* s_item)
+{
+    __syncthreads();
+    if(threadIdx.x == 0) *s_item = atomicAdd(counter, 1u);
+    __syncthreads();
+    return *s_item;
+}
+
+// The whole batched plain form in one cooperative persistent launch:
+//   phase 0  zero every ping's bin totals and out-of-range counts
+//   phase 1  count chunks (a global atomic per sample)       dynamic queue
+//   phase 2  bin-scan blocks of kScanBlock bins              dynamic queue
+//   phase 3  reference windows (static), scatter chunks      dynamic queue
+//            (a global cursor atomic per sample)
+//   phase 4  gather items, heaviest first                    dynamic queue
+// separated by bounded grid barriers. The binning phases use no shared
+// histogram, so the dynamic shared memory is the gather's and as many CTAs
+// per SM stay resident as for a gather alone.
+template <int TR, int TB>
+__global__ void __launch_bounds__(kThreads) k_batch_fused(const FusedBatch fb)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ unsigned long long s_oor[2];
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_prefix, s_item;
+    __shared__ int s_ok;
+
+    for(uint32_t k = blockIdx.x; k < fb.n_col; k += gridDim.x) {
+        const uint2 m = fb.col_map[k];
+        const PingDev& P = fb.pings[m.x];
+        const uint32_t b = m.y * kThreads + threadIdx.x;
+        if(b < P.bin.nBins) P.totals[b] = 0u;
+        if(b < (P.bin.nBins + kScanBlock - 1) / kScanBlock) P.totals[P.bin.nBins + b] = 0u;
+        if(m.y == 0 && threadIdx.x < 2) P.oor[threadIdx.x] = 0ull;
+    }
+    if(!grid_barrier(fb, &s_ok)) return;
+
+    for(;;) {
+        const uint32_t k = claim(&fb.sync->next[0], &s_item);
+        if(k >= fb.n_chunks) break;
+        const uint2 m = fb.chunk_map[k];
+        const PingDev& P = fb.pings[m.x];
+        count_chunk_global(P.samples, P.n, P.bin, m.y, P.chunks, P.totals, P.oor, s_oor);
+    }
+    if(!grid_barrier(fb, &s_ok)) return;
+
+    for(;;) {
+        const uint32_t k = claim(&fb.sync->next[1], &s_item);
+        if(k >= fb.n_scan) break;
+        const uint2 m = fb.scan_map[k];
+        const PingDev& P = fb.pings[m.x];
+        scan_bin_block(P.totals, P.bin.nBins, m.y, P.offsets, P.hist, s_warp, &s_prefix, false);   // hist = cursors
+    }
+    if(!grid_barrier(fb, &s_ok)) return;
+
+    for(uint32_t k = blockIdx.x; k < fb.n_win; k += gridDim.x) {
+        const uint2 m = fb.win_map[k];
+        const PingDev& P = fb.pings[m.x];
+        window_row(P.offsets, P.bin.nBB, P.nR, P.overlap, P.support, P.win, (int)(m.y * kThreads + threadIdx.x));
+    }
+    for(;;) {
+        const uint32_t k = claim(&fb.sync->next[2], &s_item);
+        if(k >= fb.n_chunks) break;
+        const uint2 m = fb.chunk_map[k];
+        const PingDev& P = fb.pings[m.x];
+        scatter_chunk_global(P.samples, P.n, P.bin, m.y, P.chunks, P.hist, P.offsets, P.sorted, P.err);
+    }
+    if(!grid_barrier(fb, &s_ok)) return;
+
+    for(;;) {
+        const uint32_t it = claim(&fb.sync->next[3], &s_item);
+        if(it >= fb.n_items) break;
+        const uint4 item = fb.items[it];
+        const PingDev& P = fb.pings[item.x];
+        if(item.w == 0) {
+            gather_tile_2d<TR, TB>(P.sorted, P.offsets, P.win, P.bb_tiles, P.ranges, P.bearings, P.pulse, P.beam,
+                                   P.red, P.bin.nBB, P.out, (int)item.y, (int)item.z, smem_raw);
+        }
+        else {
+            float2* s_pulse = reinterpret_cast<float2*>(smem_raw);
+            for(int i = threadIdx.x; i < P.red.range_axis.n + 2; i += kThreads) s_pulse[i] = P.pulse[i];
+            __syncthreads();
+            gather_rows_1d(P.sorted, P.offsets, P.win, P.ranges, s_pulse, P.red, P.out, (int)item.y * kWarps);
+        }
+    }
+}
+
+template <int TR, int TB>
+rtacx_status prepare_fused_shape(std::string& error, size_t smem, int sm_count, uint32_t& grid)
+{
+    if(raise_smem_limit((const void*)k_batch_fused<TR, TB>, smem) != cudaSuccess) {
+        cudaGetLastError();
+        error = "shared memory of the fused batched kernel (" + std::to_string(smem) + " B) not available";
+        return RTACX_ERR_UNSUPPORTED;
+    }
+    int per_sm = 0;
+    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_fused<TR, TB>, kThreads, smem) != cudaSuccess ||
+       per_sm < 1) {
+        cudaGetLastError();
+        error = "the fused batched kernel does not fit on an SM";
+        return RTACX_ERR_UNSUPPORTED;
+    }
+    grid = (uint32_t)sm_count * (uint32_t)per_sm;
+    return RTACX_OK;
+}
+
+template <int TR, int TB>
+rtacx_status launch_fused_shape(std::string& error, const FusedBatch& fb, size_t smem, uint32_t grid,
+                                cudaStream_t stream)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_fused<TR, TB>, fb);
+    if(e != cudaSuccess) {
+        cudaGetLastError();
+        error = std::string("k_batch_fused: ") + cudaGetErrorString(e);
+        return RTACX_ERR_CUDA;
+    }
+    return RTACX_OK;
+}
+
 } // namespace
+
+rtacx_status prepare_fused_batch(std::string& error, int shape, size_t smem, int sm_count, uint32_t& grid)
+{
+    if(shape == 2) return prepare_fused_shape<32, 128>(error, smem, sm_count, grid);
+    if(shape == 1) return prepare_fused_shape<16, 128>(error, smem, sm_count, grid);
+    return prepare_fused_shape<16, 64>(error, smem, sm_count, grid);
+}
+
+rtacx_status launch_fused_batch(std::string& error, int shape, const FusedBatch& fb, size_t smem, uint32_t grid,
+                                cudaStream_t stream)
+{
+    if(shape == 2) return launch_fused_shape<32, 128>(error, fb, smem, grid, stream);
+    if(shape == 1) return launch_fused_shape<16, 128>(error, fb, smem, grid, stream);
+    return launch_fused_shape<16, 64>(error, fb, smem, grid, stream);
+}
 
 // Batched gather tile shapes: 0 = 16 x 64, 1 = 16 x 128, 2 = 32 x 128.
 int gather_shape_rows(int shape) { return shape == 2 ? 32 : 16; }

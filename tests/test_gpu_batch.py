@@ -1,5 +1,8 @@
 """Batched plain form (rtacx_batch_*): every ping of a heterogeneous batch
-equals the single-ping path, and the single-ping path equals the oracle."""
+equals the single-ping path, and the single-ping path equals the oracle; the
+fused form is one kernel in the graph, and its grid-barrier waits are
+bounded (a barrier that cannot complete sets the batch status word and the
+run stops without touching the pings)."""
 import numpy as np
 import pytest
 
@@ -31,16 +34,19 @@ def batch_setup():
     return pings, ctxs, devs, outs
 
 
+@pytest.mark.parametrize("staged", [False, True])
 @pytest.mark.parametrize("autotune", [False, True])
-def test_batch_equals_single_ping(batch_setup, autotune):
+def test_batch_equals_single_ping(batch_setup, autotune, staged):
     pings, ctxs, devs, outs = batch_setup
     batch = _lib.Batch(0)
-    batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)], autotune=autotune)
+    batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)], autotune=autotune,
+               staged=staged)
     stream = torch.cuda.current_stream()
     for _ in range(2):
         for o in outs:
             o.fill_(float("nan"))
         batch.run(stream)
+        batch.status(stream)
         torch.cuda.synchronize()
         for wk, o in zip(pings, outs):
             got = _complex(o)
@@ -52,6 +58,46 @@ def test_batch_equals_single_ping(batch_setup, autotune):
     assert t["tile_rows"] in (16, 32) and t["tile_bearings"] in (64, 128)
     if autotune:
         assert t["tuned_ms"] > 0
+
+
+def test_fused_batch_is_one_kernel(batch_setup):
+    pings, ctxs, devs, outs = batch_setup
+    batch = _lib.Batch(0)
+    args = [(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)]
+    batch.plan(args, autotune=False)
+    assert batch.graph_kernels() == 1
+    batch.plan(args, autotune=False, staged=True)
+    assert batch.graph_kernels() == 7      # reset, zero, count, scan, scatter, windows, gather
+    batch.close()
+
+
+def test_fused_batch_barrier_wait_is_bounded(batch_setup):
+    """The first grid barrier waits for one CTA more than the launch has:
+    every CTA gives up after 100 ms, the status word reports it, no ping is
+    written, and the next plan runs clean."""
+    pings, ctxs, devs, outs = batch_setup
+    batch = _lib.Batch(0)
+    args = [(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)]
+    stream = torch.cuda.current_stream()
+    batch.diag_barrier(1, 100)
+    batch.plan(args, autotune=False)
+    for o in outs:
+        o.fill_(float("nan"))
+    batch.run(stream)
+    with pytest.raises(_lib.RtacxError) as e:
+        batch.status(stream)
+    assert e.value.status == _lib.RTACX_ERR_DEVICE
+    for o in outs:
+        assert torch.isnan(o).all()
+    batch.status(stream)                   # the word was cleared
+    batch.diag_barrier(0, 1000)
+    batch.plan(args, autotune=False)
+    batch.run(stream)
+    batch.status(stream)
+    for wk, o in zip(pings, outs):
+        want = gpu_reduce(make_context(wk), wk.samples, wk.out_shape)
+        assert rel_l2(_complex(o), want) <= 1e-6, wk.name
+    batch.close()
 
 
 def test_batch_pings_match_oracle(batch_setup, oracle):
@@ -85,7 +131,9 @@ def test_batch_full_size_mix(oracle):
         outs.append(torch.full(wk.out_shape + (2,), float("nan"), device="cuda"))
     batch = _lib.Batch(0)
     batch.plan([(c, d, wk.n, o) for wk, c, d, o in zip(pings, ctxs, devs, outs)], autotune=False)
+    assert batch.graph_kernels() == 1
     batch.run(torch.cuda.current_stream())
+    batch.status(torch.cuda.current_stream())
     torch.cuda.synchronize()
     for wk, o, ctx in zip(pings, outs, ctxs):
         got = _complex(o)
