@@ -87,6 +87,24 @@ def build_demo(verbose: bool = False) -> Path:
     return DEMO_BIN
 
 
+BINDING_SRC = ROOT / "tests" / "cpp" / "binding" / "run_ping.cpp"
+BINDING_BIN = OBJ / "binding_run_ping"
+
+
+def build_binding(verbose: bool = False) -> Path:
+    """The reference-side binding statements (tests/cpp/binding) in a
+    stand-in of the reference's SensorInstance2D, linked to librtacx.so."""
+    cuda = Path(_nvcc()).resolve().parent.parent
+    OBJ.mkdir(exist_ok=True)
+    _run(["g++", "-std=c++17", "-O2", "-I", str(ROOT / "include"), "-I", str(cuda / "include"), str(BINDING_SRC),
+          "-L", str(PKG), "-lrtacx", f"-Wl,-rpath,{PKG}", "-L", str(cuda / "lib64"), "-lcudart",
+          f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(BINDING_BIN)])
+    if verbose:
+        print(f"built {BINDING_BIN}")
+    return BINDING_BIN
+
+
 if __name__ == "__main__":
     build_library(verbose=True, ptxas_info="--ptxas" in sys.argv)
     build_demo(verbose=True)
+    build_binding(verbose=True)
