@@ -51,15 +51,16 @@ DEFAULT_CONFIG = "precision_2d"
 #       python bench.py --steps 2 --warmup 3 --no-cpu-baseline [--no-next-rows]
 # on a GB300. Reported as `traffic` beside the live `achieved` numbers.
 NCU_TRAFFIC_BYTES = {
-    "k_prec_accumulate_staged": 335.812e6 + 4.319e6,
-    "k_gemm_tn": 129.070e6 + 4.018e6,
+    "k_prec_accumulate_staged": 335.831e6 + 4.377e6,
+    "k_gemm_tn": 78.715e6 + 4.004e6,
     "sort_bin": (268.531e6 + 3.186e6) + (274.855e6 + 223.261e6),   # k_count + k_scatter_staged
 }
 # The accumulation's bound is the L2's reduction throughput, not HBM: ncu on
 # the default workload (profiles/k_prec_accumulate_staged_precision_2d.md)
-# shows 3.06 L2 reduction sectors per sample and the L2 at 77 % of its peak
-# throughput while DRAM carries the algorithmic bytes once.
-NCU_ACCUMULATE_L2 = {"l2_throughput_pct": 77.0, "l2_atomic_input_pct": 48.7, "red_sectors_per_sample": 3.06}
+# shows 2.00 L2 reduction requests (2.07 sectors) per sample and the L2 at
+# 72 % of its peak throughput while DRAM carries the algorithmic bytes once.
+NCU_ACCUMULATE_L2 = {"l2_throughput_pct": 71.6, "l2_red_sectors_pct": 45.6, "red_sectors_per_sample": 2.07,
+                     "red_requests_per_sample": 2.0}
 
 KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
 PRECISION_KERNELS_PER_PING = 5   # clear, staged accumulate, operand split, tensor-core GEMM, range filter
@@ -350,9 +351,12 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     "precision_compensated" is the precision form with the carrier phase
     reduced in compensated float arithmetic instead of FP64. With `alt` (a
     second context, its host and device ping buffers) the precision forms are
-    timed with two pings in flight: consecutive pings alternate between the
-    two contexts on two streams, as a streaming caller double-buffers; the
-    single-stream time of the same pings is reported beside it."""
+    also timed with two pings in flight: consecutive pings alternate between
+    the two contexts on two streams, as a streaming caller double-buffers;
+    the timed throughput is the single-stream one (one ping at a time, which
+    is also the latency), the two-in-flight time is reported beside it (it
+    swings between 0.28 and 0.32 ms per ping from box to box, around the
+    single-stream 0.29-0.30 ms, as the two pings' grids share the L2)."""
     from rtac_simulation_gb300 import _lib
     if echo:
         extra = _lib.RTACX_ECHO_PHASE_COMPENSATED if form == "precision_compensated" else 0
@@ -369,8 +373,11 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     torch.cuda.synchronize()
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # Single stream, one ping after the other: the timed throughput (and the
-    # per-ping latency).
+    dev_lanes = [(ctx, stream, out)]
+    if alt and form != "plain":
+        dev_lanes.append((alt[0], torch.cuda.Stream(), alt[2]))
+    # Single stream, one ping after the other: the timed throughput and the
+    # per-ping latency.
     clocks.begin()
     ev0.record(stream)
     for _ in range(steps):
@@ -381,9 +388,6 @@ def time_form(ctx, form, d_in, n, out, host_in, host_out, steps, warmup, dist, l
     t_single = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3)
     # Two pings in flight (precision forms), reported beside it: consecutive
     # pings alternate between two contexts on two streams.
-    dev_lanes = [(ctx, stream, out)]
-    if alt and form != "plain":
-        dev_lanes.append((alt[0], torch.cuda.Stream(), alt[2]))
 
     def dev_step(i):
         c, s, o = dev_lanes[i % len(dev_lanes)]
@@ -686,15 +690,15 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": wk_desc(wk),
-                   "form": ("precision: bin onto a 4x bearing grid, BF16x3 tcgen05 complex contraction, FP32 range "
-                            "filter, FP64 carrier phase"
+                   "form": ("precision: bin onto range nodes two bins apart x a 4x bearing grid, BF16x3 tcgen05 "
+                            "complex contraction (K split in two), FP32 polyphase range filter, FP64 carrier phase"
                             if head == "precision" else "plain (FP32 SIMT sparse PSF gather)"),
                    "l2": ("inputs larger than L2 (%.0f MB of samples)" if n * rec_in > 129e6 else
                           "inputs smaller than L2 (%.0f MB of samples): timed warm, not flushed") % (n * rec_in / 1e6),
-                   "timing": ("one ping at a time on one stream (two pings in flight on two streams measured "
-                              "beside it: forms.*.ms_per_step_two_in_flight; slower, the second ping's GEMM "
-                              "contends with the accumulation's L2 reductions)" if head == "precision" else
-                              "one ping at a time on one stream"),
+                   "timing": ("one ping at a time on one stream (two pings in flight on two contexts and "
+                              "two streams measured beside it: forms.*.ms_per_step_two_in_flight, within "
+                              "+/-10 % of it from box to box as the two pings' grids share the L2)"
+                              if head == "precision" else "one ping at a time on one stream"),
                    "e2e_path": ("rtacx_reduce_precision_host from pinned host memory, two pings in flight "
                                 "(two contexts, two streams)" if head == "precision" else
                                 "pinned H2D copy + rtacx_reduce + D2H copy"),
@@ -726,9 +730,11 @@ def run_ours(args, world, rank, local):
     if "precision" in forms:
         ps = res["precision"]["stage"]
         nR, nB = wk.sensor["range_count"], len(wk.sensor["bearings"])
-        cells, rows_g = tab["grid_count"], nR + len(tab["range_taps"]) + 1
-        # Accumulate: one read of every sample (16 B) + the binned grid written once (8 B / cell).
-        acc_bytes = n * rec_in + rows_g * cells * 8
+        cells = tab["grid_count"]
+        rows_g = (nR - 1) // 2 + 1 + np.asarray(tab["range_taps"]).reshape(2, -1).shape[1] + 1
+        # Accumulate: one read of every sample (16 B) + the binned grid (one
+        # 16-byte {left, right} pair per node and bearing interval) written once.
+        acc_bytes = n * rec_in + rows_g * cells * 16
         acc_gbs = acc_bytes / (ps["accumulate"] / 1e3) / 1e9
         Mp, Np, Kp = -(-rows_g // 128) * 128, -(-2 * nB // 256) * 256, -(-6 * cells // 64) * 64
         gemm_tf = 2.0 * Mp * Np * Kp / (ps["gemm"] / 1e3) / 1e12
@@ -736,11 +742,11 @@ def run_ours(args, world, rank, local):
                     "frac": acc_gbs / peaks["hbm_gbs"], "traffic": ncu.get("k_prec_accumulate_staged"),
                     "kernel": "k_prec_accumulate_staged",
                     "peak_source": peaks["source"],
-                    "algorithmic": f"{rec_in} B per sample read + 8 B per grid cell ({rows_g} x {cells})",
+                    "algorithmic": f"{rec_in} B per sample read + 16 B per grid interval ({rows_g} x {cells})",
                     "l2_bound": dict(NCU_ACCUMULATE_L2, reductions_per_s=NCU_ACCUMULATE_L2["red_sectors_per_sample"]
                                      * n / (ps["accumulate"] / 1e3),
-                                     note="bound by the L2's reduction rate (4 complex values per sample "
-                                          "reduced into a 68 MB L2-resident grid); HBM carries the samples once")}
+                                     note="bound by the L2's reduction rate (two 16-byte vector reductions "
+                                          "per sample into a 68 MB L2-resident grid); HBM carries the samples once")}
         roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": gemm_tf / peaks["bf16_tflops"], "traffic": ncu.get("k_gemm_tn"), "kernel": "k_gemm_tn",
                      "peak_source": peaks["source"],

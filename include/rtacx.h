@@ -187,14 +187,15 @@ typedef struct {
 } rtacx_echo_model;
 rtacx_status rtacx_set_echo_model(rtacx_ctx* ctx, const rtacx_echo_model* model);
 
-/* Precision (tensor-core) form of a configured 2D sensor. Bins onto a fine
- * grid first, then contracts over bearings on the tensor cores, then filters
- * in range. Per sample s (reference range key in range, finite travel t and
+/* Precision (tensor-core) form of a configured 2D sensor. Bins onto a grid
+ * first, then contracts over bearings on the tensor cores, then filters in
+ * range. Per sample s (reference range key in range, finite travel t and
  * bearing theta; float arithmetic, every operation rounded on its own):
  *   range    res = (range_max - range_min) / (range_count - 1) (the output
- *            ranges' Linspace resolution), j = floor((t - range_min) / res),
- *            alpha = (t - (range_min + j res)) / res: the value goes to grid
- *            rows j and j + 1 with weights 1 - alpha and alpha;
+ *            ranges' Linspace resolution), h = 2 res (one range node every
+ *            two output bins), j = floor((t - range_min) / h), alpha = (t -
+ *            (range_min + j h)) / h: the value goes to nodes j and j + 1
+ *            with weights 1 - alpha and alpha;
  *   bearing  a uniform grid of grid_count bearings from grid_first to
  *            grid_last, step = (grid_last - grid_first) / (grid_count - 1),
  *            q = clamp(floor((theta - grid_first) / step), 0, grid_count - 2),
@@ -202,30 +203,33 @@ rtacx_status rtacx_set_echo_model(rtacx_ctx* ctx, const rtacx_echo_model* model)
  *            bearings q and q + 1 with weights 1 - w and w
  *            (divisions as products with the float reciprocals);
  *   G[j][q] += v_s times the product of the two weights (four cells);
- *   out(r, b) = sum_t taps[t] sum_q G[r + t - tap_center][q] D[q][b],
- *            D the dense complex [grid_count][bearing_count] directivity
- *            (D[q][b]: response of beam b to grid bearing q); a row whose
- *            reference window (do_make_bins rule, src/Binner.cu:90-102, on
- *            the keyed non-empty range bins) is empty is zero.
- * For a pulse sampled at bin spacing the range part is the per-sample PSF's
- * own interpolation (the taps at whole-bin offsets, linearly interpolated),
- * so the model differs from rtacx_reduce only by the bearing grid. The
+ *   out(r, b) = sum_t taps[r % 2][t] sum_q G[r / 2 + t - tap_center][q]
+ *            D[q][b], D the dense complex [grid_count][bearing_count]
+ *            directivity (D[q][b]: response of beam b to grid bearing q); a
+ *            row whose reference window (do_make_bins rule,
+ *            src/Binner.cu:90-102, on the keyed non-empty range bins) is
+ *            empty is zero.
+ * Each sample costs two 16-byte vector reductions: the grid is stored by
+ * bearing interval (the shares of its two bearings side by side). The
  * contraction runs in BF16 with three split products (hi*hi + hi*lo +
  * lo*hi) and FP32 accumulation on tcgen05 tensor cores; the rest is FP32.
- * NULL tables are derived from the 2D sensor: taps[t] = pulse((t -
- * tap_center) * resolution) (texture-equivalent lerp, |t - tap_center| <=
- * the reference's bin overlap, trimmed to the non-zero span), and D[.][b] the
- * least-squares projection of beam(theta - theta_b) onto the grid's hat
- * functions (the coefficients whose linear interpolation between grid
- * bearings is closest in mean square to the per-sample response). grid_count
- * 0 selects four grid bearings per output bearing (rounded up to a multiple
- * of 32); grid_first == grid_last selects the first and last table bearings.
- * Samples outside the grid's bearings take its end bearing. */
+ * NULL tables are derived from the 2D sensor: taps[p][t] the least-squares
+ * (L2) projection of the pulse response pulse(x - p res) (texture-equivalent
+ * lerp, seen from a node) onto the hat functions of the nodes (the weight of
+ * node offset t - tap_center), and D[.][b] the least-squares projection of
+ * beam(theta - theta_b) onto the bearing grid's hat functions (the
+ * coefficients whose linear interpolation between grid bearings is closest
+ * in mean square to the per-sample response). On the 512-bearing
+ * 2^24-sample benchmark ping the derived model is within 6e-3 to 7e-3
+ * relative L2 of the per-sample PSF. grid_count 0 selects four grid bearings
+ * per output bearing (rounded up to a multiple of 32); grid_first ==
+ * grid_last selects the first and last table bearings. Samples outside the
+ * grid's bearings take its end bearing. */
 typedef struct {
     const float* directivity;   /* host complex [grid_count][bearing_count] or NULL */
-    const float* range_taps;    /* host complex [tap_count] or NULL                 */
-    uint32_t tap_count;
-    uint32_t tap_center;
+    const float* range_taps;    /* host complex [2][tap_count] (even, odd rows) or NULL */
+    uint32_t tap_count;         /* taps per output-row parity (<= 1024)            */
+    uint32_t tap_center;        /* index of node offset 0                          */
     uint32_t flags;             /* 0 or RTACX_PRECISION_* below                     */
     uint32_t grid_count;        /* bearing grid size (even, <= 16384), 0: default   */
     float grid_first;           /* first and last grid bearing (rad)                */
@@ -240,7 +244,7 @@ typedef struct {
 /* Contention relief for clustered scenes (a strong target concentrating many
  * samples in few range bins): a strided subsample of each ping (1/128 of the
  * samples, or of the first 2^21-record chunk of rtacx_reduce_precision_host)
- * finds the densest 256-row interval of grid rows; if it holds at least a
+ * finds the densest interval of 128 range nodes (256 output bins); if it holds at least a
  * tenth of the samples and four times its uniform share, those rows are
  * accumulated into eight replicas (chosen by CTA and warp), added back into
  * the grid before the contraction, so vector reductions to the same cells no

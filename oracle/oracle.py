@@ -181,22 +181,22 @@ def apply_echo(samples: np.ndarray, sensor: dict, echo: dict | None, mode: int =
 def reduce_binned(samples: np.ndarray, sensor: dict, tables: dict, rows=None, threads: int = 0) -> np.ndarray:
     """FP64 oracle of the binned precision model (complex128 [rows][nB]).
     `tables` holds the precision configuration (workloads.precision_tables):
-    directivity [grid_count][nB], range_taps, tap_center, grid_count,
-    grid_first, grid_last."""
+    directivity [grid_count][nB], range_taps [2][L] (one tap set per output
+    row parity), tap_center, grid_count, grid_first, grid_last."""
     lib = load()
     s = np.ascontiguousarray(samples, dtype=np.float32)
     n = s.shape[0]
     nR = sensor["range_count"]
     nB = len(sensor["bearings"])
     D = np.ascontiguousarray(tables["directivity"], dtype=np.complex64)
-    t = np.ascontiguousarray(tables["range_taps"], dtype=np.complex64)
+    t = np.ascontiguousarray(tables["range_taps"], dtype=np.complex64).reshape(2, -1)   # [phase][tap]
     cells = int(tables["grid_count"])
     assert D.shape == (cells, nB)
     r0, r1 = rows if rows is not None else (0, nR)
     out = np.zeros((r1 - r0, nB), dtype=np.complex128)
     lib.rtacx_oracle_reduce_binned(s.ctypes.data, n, sensor["range_min"], sensor["range_max"], nR,
                                    sensor["margin"], nB, tables["grid_first"], tables["grid_last"], cells,
-                                   D.ctypes.data, t.ctypes.data, t.size, int(tables["tap_center"]), r0, r1,
+                                   D.ctypes.data, t.ctypes.data, t.shape[1], int(tables["tap_center"]), r0, r1,
                                    threads or (os.cpu_count() or 1), out.ctypes.data)
     return out
 

@@ -421,19 +421,25 @@ struct GridAxes {
     int row_lo, row_hi;        // accepted absolute rows j: [row_lo, row_hi]
 };
 
+// Range grid of the binned model: one node every two output bins (node m at
+// rmin + m * hr, hr = 2 res), rows for the nodes of output rows 0 .. nR - 1
+// (m = r / 2) widened by the taps.
+uint32_t range_nodes(uint32_t nR) { return ((nR - 1u) >> 1) + 1u; }
+
 GridAxes make_grid_axes(float rmin, float rmax, uint32_t nR, float first, float last, uint32_t cells,
                         uint32_t ntaps, uint32_t center)
 {
     GridAxes g;
     g.rmin = rmin;
-    g.res = (rmax - rmin) / (float)(nR - 1u);
+    const float res = (rmax - rmin) / (float)(nR - 1u);
+    g.res = 2.0f * res;
     g.inv_res = 1.0f / g.res;
     g.first = first;
     g.step = (last - first) / (float)(cells - 1u);
     g.inv_step = 1.0f / g.step;
     g.cells = cells;
     g.row_lo = -(int)center - 1;
-    g.row_hi = (int)nR + (int)ntaps - (int)center - 2;
+    g.row_hi = (int)range_nodes(nR) + (int)ntaps - (int)center - 2;
     return g;
 }
 
@@ -603,22 +609,20 @@ void rtacx_oracle_apply_echo(float* samples, uint64_t n, uint32_t stride, double
 // in include/rtacx.h. Per sample (in-range reference key, finite travel and
 // bearing), with the float arithmetic of the device spelled out so that the
 // grid coordinates agree bit for bit:
-//   range    res = (rmax - rmin) / (nR - 1), inv_res = 1 / res (the Linspace
-//            resolution of the output ranges); j = floor((t - rmin) * inv_res),
-//            alpha = (t - (rmin + j * res)) * inv_res: weight 1 - alpha on
-//            grid row j, alpha on row j + 1. The per-sample PSF evaluates a
-//            pulse sampled at bin spacing at t - R_r, which is exactly this
-//            linear split followed by the taps at whole-bin offsets.
+//   range    res = (rmax - rmin) / (nR - 1) (the Linspace resolution of the
+//            output ranges), hr = 2 res, inv_hr = 1 / hr;
+//            j = floor((t - rmin) * inv_hr), alpha = (t - (rmin + j * hr)) *
+//            inv_hr: weight 1 - alpha on range node j, alpha on node j + 1;
 //   bearing  step = (last - first) / (cells - 1), inv_step = 1 / step;
 //            q = clamp(floor((theta - first) * inv_step), 0, cells - 2),
 //            w = clamp((theta - (first + q * step)) * inv_step, 0, 1): weight
 //            1 - w on grid bearing q, w on q + 1.
-// Grid row j is stored at jg = j + center + 1 of nR + ntaps + 1 rows; samples
-// whose rows fall outside reach no output row and are dropped. Output row r
-// is zero when its reference window (do_make_bins rule on the keyed
-// non-empty bins) is empty, else out(r, b) = sum_t taps[t] sum_q
-// G[r + t + 1][q] D[q][b]. Rows [row_begin, row_end) into out (complex
-// double).
+// Node j is stored at row jg = j + center + 1 of (nR - 1) / 2 + 1 + ntaps + 1
+// rows; samples whose rows fall outside reach no output row and are dropped.
+// Output row r is zero when its reference window (do_make_bins rule on the
+// keyed non-empty bins) is empty, else out(r, b) = sum_t taps[r % 2][t]
+// sum_q G[r / 2 + t + 1][q] D[q][b] (taps: two phases of ntaps complex
+// values). Rows [row_begin, row_end) into out (complex double).
 void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, float rmax, uint32_t nR,
                                 float margin, uint32_t nB, float grid_first, float grid_last, uint32_t cells,
                                 const float* D, const float* taps, uint32_t ntaps, uint32_t center,
@@ -628,7 +632,7 @@ void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, fl
     if(nR < 2 || cells < 2 || ntaps == 0) return;
     KeyParams key = make_key(nR, rmin, rmax, margin);
     const GridAxes ax = make_grid_axes(rmin, rmax, nR, grid_first, grid_last, cells, ntaps, center);
-    const size_t rows = (size_t)nR + ntaps + 1;
+    const size_t rows = (size_t)range_nodes(nR) + ntaps + 1;
     std::vector<cd> G(rows * cells, cd(0.0, 0.0));
     std::vector<uint8_t> nonempty(nR, 0);
     for(uint64_t i = 0; i < n; i++) {
@@ -649,8 +653,8 @@ void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, fl
         r1[1] += a * b * v;
     }
     const int ov = bin_overlap(rmin, rmax, nR, margin);
-    std::vector<cd> tv(ntaps);
-    for(uint32_t t = 0; t < ntaps; t++) tv[t] = cd(taps[2 * t], taps[2 * t + 1]);
+    std::vector<cd> tv(2 * (size_t)ntaps);
+    for(uint32_t t = 0; t < 2 * ntaps; t++) tv[t] = cd(taps[2 * t], taps[2 * t + 1]);
     std::vector<cd> Dd((size_t)cells * nB);
     for(size_t e = 0; e < Dd.size(); e++) Dd[e] = cd(D[2 * e], D[2 * e + 1]);
     row_end = std::min(row_end, nR);
@@ -663,9 +667,10 @@ void rtacx_oracle_reduce_binned(const float* samples, uint64_t n, float rmin, fl
         for(long long jj = lo; jj <= hi && nonempty_bins < 2; jj++) nonempty_bins += nonempty[jj];
         if(nonempty_bins < 2) return;          // the reference's empty view (src/Binner.cu:90-102)
         std::vector<cd> g(cells, cd(0.0, 0.0));
+        const cd* tp = tv.data() + (size_t)(r & 1u) * ntaps;
         for(uint32_t t = 0; t < ntaps; t++) {
-            const cd* row = G.data() + ((size_t)r + t + 1) * cells;
-            for(uint32_t q = 0; q < cells; q++) g[q] += tv[t] * row[q];
+            const cd* row = G.data() + ((size_t)(r >> 1) + t + 1) * cells;
+            for(uint32_t q = 0; q < cells; q++) g[q] += tp[t] * row[q];
         }
         for(uint32_t q = 0; q < cells; q++) {
             if(g[q] == cd(0.0, 0.0)) continue;

@@ -289,9 +289,9 @@ class Context:
         """rtacx_configure_precision; the keyword arguments are those of
         workloads.precision_tables (directivity [grid_count][nB] complex)."""
         d = None if directivity is None else np.ascontiguousarray(np.asarray(directivity, dtype=np.complex64))
-        t = None if range_taps is None else np.ascontiguousarray(np.asarray(range_taps, dtype=np.complex64))
+        t = None if range_taps is None else np.ascontiguousarray(np.asarray(range_taps, dtype=np.complex64).reshape(2, -1))
         desc = PrecisionDesc(None if d is None else d.ctypes.data, None if t is None else t.ctypes.data,
-                             0 if t is None else t.size, tap_center, flags, grid_count, grid_first, grid_last)
+                             0 if t is None else t.shape[1], tap_center, flags, grid_count, grid_first, grid_last)
         self._check(self._lib.rtacx_configure_precision(self._h, ctypes.byref(desc)))
 
     def reduce_precision(self, samples, n: int, out, stream=None) -> None:

@@ -247,6 +247,7 @@ struct GridParams {
     float rmin, res, inv_res;
     float first, step, inv_step;
     uint32_t cells;
+    uint32_t pitch;                  // entries per stored grid row (cells + padding)
     int row_lo, row_hi, row_shift;
 };
 
@@ -403,19 +404,20 @@ struct Context {
 
     // Precision form (rtacx_configure_precision).
     bool prec_configured = false;
-    uint32_t taps = 0, tap_center = 0;
+    uint32_t taps = 0, tap_center = 0;   // taps per output-row parity, index of node offset 0
     uint32_t Mpad = 0, Npad = 0, Kp = 0;
-    GridParams grid{};                  // range rows and uniform bearing grid of the binned model
-    uint32_t grid_rows = 0;             // nR + taps + 1 rows of the binned grid
-    float2* d_G = nullptr;              // [grid_rows][grid.cells] binned grid (complex)
+    uint32_t ksplit = 1;                // K parts of the contraction (partial products summed by the filter)
+    GridParams grid{};                  // range nodes (two output bins apart) and uniform bearing grid
+    uint32_t grid_rows = 0;             // (nR - 1) / 2 + 1 + taps + 1 node rows of the binned grid
+    float4* d_G = nullptr;              // [grid_rows][grid.cells] bearing intervals: {left, right} shares (complex)
     uint32_t* d_flags = nullptr;        // [(nR + 31) / 32] bitmap of non-empty range bins (reference keys)
     uint32_t acc_staged_blocks[6] = {}; // resident CTAs per SM of each staged accumulation (0: not used)
     size_t acc_staged_smem = 0;
     uint32_t diag_drop_stage = 0xFFFFFFFFu; // failure-path test: stage whose copy the staged accumulation skips
     uint16_t* d_A = nullptr;            // [Mpad][Kp] bf16 [hi | hi | lo] split of the binned grid
     uint16_t* d_B = nullptr;            // [Npad][Kp] bf16 [hi | lo | hi] split of the directivity
-    float* d_C = nullptr;               // [Mpad][Npad] GEMM output: the grid contracted over bearings
-    float2* d_taps = nullptr;           // [taps] range taps at bin offsets t - tap_center
+    float* d_C = nullptr;               // [ksplit][Mpad][Npad] GEMM partial outputs: the grid contracted over bearings
+    float2* d_taps = nullptr;           // [2][taps] range taps per output-row parity at node offsets t - tap_center
     // FP16 per-row-scaled contraction (RTACX_PRECISION_FP16_ROWSCALE): A and B
     // hold fp16 splits instead of bf16 ones.
     bool prec_f16 = false;
@@ -425,7 +427,7 @@ struct Context {
     bool prec_hot = false;
     int2* d_hot = nullptr;              // {first grid row, length} of the hot interval (length 0: none)
     uint32_t* d_hotcnt = nullptr;       // [grid_rows] subsample counts (zero between pings)
-    float2* d_rep = nullptr;            // [hot rows][replicas][grid.cells] grid replicas
+    float4* d_rep = nullptr;            // [hot rows][replicas][grid.cells] grid replicas
 
     // Host-buffer streaming (rtacx_reduce_precision_host): two device staging
     // buffers of RTACX_STREAM_CHUNK records, a copy stream fork-joined to the
@@ -492,9 +494,11 @@ void free_streaming(Context& ctx);
 void free_precision(Context& ctx);
 
 // Tensor-core GEMM (rtacx_umma.cu): C = row_scale * col_scale * (A * B^T),
-// K-major operands, both bf16 or both fp16 (f16); scales optional.
+// K-major operands, both bf16 or both fp16 (f16); scales optional; ksplit
+// partial products at C + z M ldc.
 rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K, int ldc,
-                     cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale);
+                     cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale,
+                     int ksplit);
 size_t gemm_smem_bytes();
 
 } // namespace rtacx

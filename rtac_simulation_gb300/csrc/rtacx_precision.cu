@@ -1,4 +1,4 @@
-// Precision (tensor-core) form: bin onto a fine grid first, contract over
+// Precision (tensor-core) form: bin onto a grid first, contract over
 // bearings on the tensor cores, then filter in range.
 //
 //   k_prec_clear       zeroes the binned grid and the non-empty bitmap.
@@ -6,21 +6,26 @@
 //   (_staged)          reference range key (Binner::Key, bit-exact) into the
 //                      non-empty bitmap, optional FP64 echo pre-step, then a
 //                      bilinear split onto the grid: linear in range between
-//                      the two output-range rows around the travel, linear in
-//                      bearing between the two grid bearings around the
-//                      sample bearing; four complex reductions (two 16-byte
-//                      vector reductions when the bearing cell is even). No
+//                      the two range nodes around the travel (one node every
+//                      two output bins), linear in bearing between the two
+//                      grid bearings around the sample bearing. The grid is
+//                      stored by bearing interval: entry (node, q) holds the
+//                      interval's shares of grid bearings q and q + 1, so each
+//                      sample is exactly two 16-byte vector reductions. No
 //                      sort.
-//   k_prec_split       the grid as the bf16 A operand [hi | hi | lo] of the
-//                      three-term split product (k_prec_split_f16: fp16 with
-//                      a power-of-two scale per row).
+//   k_prec_split       grid bearing q of a node = left share of interval q +
+//                      right share of interval q - 1, as the bf16 A operand
+//                      [hi | hi | lo] of the three-term split product
+//                      (k_prec_split_f16: fp16 with a power-of-two scale per
+//                      row).
 //   gemm_tn            C = A x B^T on tcgen05 (rtacx_umma.cu), B the
 //                      [hi | lo | hi] split of the complex directivity laid
 //                      out so that column 2b of C is the real and 2b + 1 the
 //                      imaginary part of the grid contracted onto bearing b.
-//   k_prec_filter      the range taps over C's rows, rows whose reference
-//                      window (src/Binner.cu:90-102) is empty set to zero:
-//                      the complex64 ping.
+//   k_prec_filter      the range taps of each output-row parity over C's
+//                      node rows, rows whose reference window
+//                      (src/Binner.cu:90-102) is empty set to zero: the
+//                      complex64 ping.
 // The range filter runs after the contraction (the two commute): it then
 // works on bearing_count columns instead of the grid's.
 #include "rtacx_internal.cuh"
@@ -45,9 +50,13 @@ constexpr int kAccThreads = 256;
 // rows replicated kHotReplicas times; samples in them reduce into the replica
 // of their CTA and warp, and k_hot_fold adds the replicas back into the grid
 // before the contraction.
-constexpr int kHotRows = 256, kHotReplicas = 8;
+constexpr int kHotRows = 128, kHotReplicas = 8;
 constexpr int kAccLoads = 4;                     // independent record loads per thread in flight
 constexpr int kAccEchoModels = 6;                // echo models of the staged accumulation
+// Grid rows are stored cells + kRowPad entries apart (128 bytes of padding,
+// so that the row pitch is not a power of two): 4 % faster accumulation on
+// the clustered 2^27-sample stress ping, no change on the uniform one.
+constexpr uint32_t kRowPad = 8;
 
 // L2 eviction priorities (createpolicy): the sample stream is read once
 // and marked evict-first, the grid's reductions evict-last, so that the
@@ -67,27 +76,20 @@ __device__ __forceinline__ uint64_t policy_evict_last()
     return p;
 }
 
-__device__ __forceinline__ void red_add_v4(float2* addr, float4 v, uint64_t pol)
+__device__ __forceinline__ void red_add_v4(float4* addr, float4 v, uint64_t pol)
 {
     asm volatile("red.global.add.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;"
                  ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol));
 }
 
-__device__ __forceinline__ void red_add_v2(float2* addr, float2 v, uint64_t pol)
-{
-    asm volatile("red.global.add.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(addr), "f"(v.x), "f"(v.y), "l"(pol));
-}
-
-// Adds a sample's share (1 - w) v to grid bearing q and w v to q + 1 of one
-// grid row. An even q starts a 16-byte pair: one vector reduction; an odd q
-// straddles two pairs: two 8-byte reductions. The grid is never read by the
-// kernels that reduce into it, so the reductions carry no memory clobber.
-__device__ __forceinline__ void deposit(float2* row, int q, float w, float2 v, uint64_t pol)
+// Adds a sample's share v of one range node to bearing interval q of the
+// node's grid row: (1 - w) v to the interval's left bearing, w v to its
+// right bearing, in one 16-byte vector reduction. The grid is never read by
+// the kernels that reduce into it, so the reductions carry no memory clobber.
+__device__ __forceinline__ void deposit(float4* row, int q, float w, float2 v, uint64_t pol)
 {
     const float w0 = 1.0f - w;
-    const float2 a = make_float2(w0 * v.x, w0 * v.y), b = make_float2(w * v.x, w * v.y);
-    if((q & 1) == 0) red_add_v4(row + q, make_float4(a.x, a.y, b.x, b.y), pol);
-    else { red_add_v2(row + q, a, pol); red_add_v2(row + q + 1, b, pol); }
+    red_add_v4(row + q, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y), pol);
 }
 
 size_t accumulate_smem_bytes(uint32_t nR)
@@ -101,19 +103,19 @@ size_t accumulate_smem_bytes(uint32_t nR)
 // OR-ed into the global one once per CTA.
 __global__ void __launch_bounds__(kAccThreads)
 k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p, GridParams g,
-                  float2* __restrict__ G, uint32_t* __restrict__ nonempty, const int2* __restrict__ hot,
-                  float2* __restrict__ rep)
+                  float4* __restrict__ G, uint32_t* __restrict__ nonempty, const int2* __restrict__ hot,
+                  float4* __restrict__ rep)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_raw);
     int hot_lo = 0, hot_len = 0;
     if(hot) { const int2 h = *hot; hot_lo = h.x; hot_len = h.y; }
     const uint32_t rsel = (blockIdx.x + (threadIdx.x >> 5)) & (kHotReplicas - 1);   // by CTA and warp
-    const uint32_t cells = g.cells;
+    const uint32_t pitch = g.pitch;
     // Grid row jg: the grid's, or this warp's replica of a hot row.
-    auto grid_row = [&](int jg) -> float2* {
+    auto grid_row = [&](int jg) -> float4* {
         const uint32_t hj = (uint32_t)(jg - hot_lo);
-        return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * cells : G + (size_t)jg * cells;
+        return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * pitch : G + (size_t)jg * pitch;
     };
     const uint32_t words = (p.key.nR + 31) / 32;
     const uint64_t keep = policy_evict_last();
@@ -176,7 +178,7 @@ size_t staged_smem_bytes(uint32_t nR)
 template <uint32_t kEcho>
 __global__ void __launch_bounds__(kStagedThreads)
 k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinParams p, GridParams g,
-                         float2* __restrict__ G, uint32_t* __restrict__ nonempty, uint32_t* __restrict__ err,
+                         float4* __restrict__ G, uint32_t* __restrict__ nonempty, uint32_t* __restrict__ err,
                          uint32_t drop_stage)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -186,7 +188,7 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
     uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_ring + kStages * kStageRecs);
     const uint32_t words = (p.key.nR + 31) / 32;
     const uint64_t stages = (n + kStageRecs - 1) / kStageRecs;
-    const uint32_t cells = g.cells;
+    const uint32_t pitch = g.pitch;
     const uint64_t stream_pol = policy_evict_first(), keep = policy_evict_last();
     auto issue = [&](uint64_t c, int slot) {
         if(c == drop_stage) return;      // failure-path test: this stage's copy never comes
@@ -252,9 +254,9 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
         for(int u = 0; u < kStagedPerThread; u++) {
             if(key[u] != kOutOfRange) atomicOr(&s_bits[key[u] >> 5], 1u << (key[u] & 31));
             if(row[u] >= 0) {
-                float2* r0 = G + (size_t)row[u] * cells;
+                float4* r0 = G + (size_t)row[u] * pitch;
                 deposit(r0, cell[u], wgt[u], make_float2(add[u].x, add[u].y), keep);
-                deposit(r0 + cells, cell[u], wgt[u], make_float2(add[u].z, add[u].w), keep);
+                deposit(r0 + pitch, cell[u], wgt[u], make_float2(add[u].z, add[u].w), keep);
             }
         }
         if(aborted) break;
@@ -397,30 +399,30 @@ __global__ void __launch_bounds__(kHotPickThreads) k_hot_pick(uint32_t* __restri
 }
 
 // Adds the replicas of the hot rows into the grid once every sample is in
-// (nothing when the interval is empty).
-__global__ void k_hot_fold(const int2* __restrict__ hot, uint32_t cells, const float2* __restrict__ rep,
-                           float2* __restrict__ G)
+// (nothing when the interval is empty). Rows of `pitch` entries.
+__global__ void k_hot_fold(const int2* __restrict__ hot, uint32_t pitch, const float4* __restrict__ rep,
+                           float4* __restrict__ G)
 {
     const int2 h = *hot;
-    const uint64_t total = (uint64_t)h.y * cells;
+    const uint64_t total = (uint64_t)h.y * pitch;
     for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t row = i / cells, k = i % cells;
-        const float2* rb = rep + row * kHotReplicas * cells + k;
-        float2 acc = G[((uint64_t)h.x + row) * cells + k];
+        const uint64_t row = i / pitch, k = i % pitch;
+        const float4* rb = rep + row * kHotReplicas * pitch + k;
+        float4 acc = G[((uint64_t)h.x + row) * pitch + k];
         for(int r = 0; r < kHotReplicas; r++) {
-            const float2 e = rb[(uint64_t)r * cells];
-            acc.x += e.x; acc.y += e.y;
+            const float4 e = rb[(uint64_t)r * pitch];
+            acc.x += e.x; acc.y += e.y; acc.z += e.z; acc.w += e.w;
         }
-        G[((uint64_t)h.x + row) * cells + k] = acc;
+        G[((uint64_t)h.x + row) * pitch + k] = acc;
     }
 }
 
 // Zeroes the replicas of the hot rows (nothing when the interval is empty).
-__global__ void k_hot_zero(const int2* __restrict__ hot, uint32_t cells, float2* __restrict__ rep)
+__global__ void k_hot_zero(const int2* __restrict__ hot, uint32_t pitch, float4* __restrict__ rep)
 {
-    const uint64_t total = (uint64_t)hot->y * kHotReplicas * cells;
+    const uint64_t total = (uint64_t)hot->y * kHotReplicas * pitch;
     for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
-        rep[i] = make_float2(0.f, 0.f);
+        rep[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __device__ __forceinline__ bool bit_set(const uint32_t* bits, long long j)
@@ -452,18 +454,29 @@ __device__ __forceinline__ uint16_t bf16_bits(float x)
 
 __device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
 
-// The A operand of the three-term split product: grid row r (cells complex
+// Grid bearing q of a node row: the left share of bearing interval q plus
+// the right share of interval q - 1 (interval cells - 1 is never written).
+__device__ __forceinline__ float2 node_value(const float4* __restrict__ row, uint32_t q)
+{
+    const float4 a = row[q];
+    if(q == 0) return make_float2(a.x, a.y);
+    const float4 b = row[q - 1];
+    return make_float2(a.x + b.z, a.y + b.w);
+}
+
+// The A operand of the three-term split product: node row r (cells complex
 // values) becomes A row r = [hi(Re) | hi(Im) | hi(Re) | hi(Im) | lo(Re) |
 // lo(Im)], each block `cells` wide, lo = bf16(x - hi). One thread per pair of
-// grid bearings: one 16-byte load, six 4-byte stores.
-__global__ void k_prec_split(const float4* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t Kp,
+// grid bearings: three 16-byte loads, six 4-byte stores.
+__global__ void k_prec_split(const float4* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t pitch, uint32_t Kp,
                              uint16_t* __restrict__ A)
 {
     const uint32_t r = blockIdx.y;
     const uint32_t k2 = blockIdx.x * blockDim.x + threadIdx.x;
     if(r >= rows || 2 * k2 >= cells) return;
-    const float4 v = G[((size_t)r * cells >> 1) + k2];
-    const float x[4] = {v.x, v.y, v.z, v.w};        // re0, im0, re1, im1
+    const float4* grow = G + (size_t)r * pitch;
+    const float2 n0 = node_value(grow, 2 * k2), n1 = node_value(grow, 2 * k2 + 1);
+    const float x[4] = {n0.x, n0.y, n1.x, n1.y};     // re0, im0, re1, im1
     uint16_t h[4], l[4];
 #pragma unroll
     for(int i = 0; i < 4; i++) { h[i] = bf16_bits(x[i]); l[i] = bf16_bits(x[i] - bf16_value(h[i])); }
@@ -494,16 +507,16 @@ __device__ __forceinline__ int scale_exponent(uint32_t maxbits)
 constexpr int kSplitF16Threads = 256;
 
 __global__ void __launch_bounds__(kSplitF16Threads)
-k_prec_split_f16(const float2* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t Kp, uint16_t* __restrict__ A,
-                 float* __restrict__ row_scale)
+k_prec_split_f16(const float4* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t pitch, uint32_t Kp,
+                 uint16_t* __restrict__ A, float* __restrict__ row_scale)
 {
     __shared__ float s_max[kSplitF16Threads / 32];
     const uint32_t r = blockIdx.x;
     if(r >= rows) return;
-    const float2* grow = G + (size_t)r * cells;
+    const float4* grow = G + (size_t)r * pitch;
     float m = 0.0f;
     for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
-        const float2 v = grow[k];
+        const float2 v = node_value(grow, k);
         m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
     }
     for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -516,7 +529,7 @@ k_prec_split_f16(const float2* __restrict__ G, uint32_t rows, uint32_t cells, ui
     if(threadIdx.x == 0) row_scale[r] = __uint_as_float((uint32_t)(127 - se) << 23);
     uint16_t* row = A + (size_t)r * Kp;
     for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
-        const float2 v = grow[k];
+        const float2 v = node_value(grow, k);
         const float xr = v.x * s, xi = v.y * s;
         const __half hr = __float2half_rn(xr), hi = __float2half_rn(xi);
         const __half lr = __float2half_rn(xr - __half2float(hr)), li = __float2half_rn(xi - __half2float(hi));
@@ -534,21 +547,23 @@ size_t filter_smem_bytes(uint32_t ntaps)
     return (kFiltRows + nt - 1) * kFiltCols * sizeof(float2) + kFiltTapsMax * sizeof(float2) + kFiltRows * sizeof(int);
 }
 
-// Range filter on the contracted grid: out(r, b) = sum_t taps[t] C[r + t +
-// 1][b] (C row j holds grid row j: absolute range row j - tap_center - 1),
-// or 0 when row r's reference window is empty. One CTA per 64 rows x 64
-// bearings; per chunk of up to 64 taps the C rows it needs are staged in
-// shared memory once, row-major: every warp first loads all of its rows
-// (up to 16, two 256-byte row segments each) and only then stores them, so
-// the loads are in flight together. Lane l owns columns l and l + 32; each
-// warp filters 8 rows with a sliding window of eight staged rows per column
-// in registers (one shared load per tap and column).
+// Range filter on the contracted grid: out(r, b) = sum_t taps[r % 2][t]
+// C[r / 2 + t + 1][b] (C row j holds range node j - tap_center - 1), or 0
+// when row r's reference window is empty. One CTA per 64 node rows x 64
+// bearings x one output-row parity (blockIdx.z): output rows 2 m + parity.
+// Per chunk of up to 64 taps the C rows it needs are staged in shared memory
+// once, row-major: every warp first loads all of its rows (up to 16, two
+// 256-byte row segments each) and only then stores them, so the loads are in
+// flight together. Lane l owns columns l and l + 32; each warp filters 8 node
+// rows with a sliding window of eight staged rows per column in registers
+// (one shared load per tap and column).
 constexpr int kFiltRowsPerWarp = (kFiltRows + kFiltTapsMax - 1 + 7) / 8;
 
+template <int kParts>
 __global__ void __launch_bounds__(kFiltThreads, 2)
-k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, const uint32_t* __restrict__ nonempty,
-              int ov, const float2* __restrict__ taps, uint32_t ntaps, uint32_t nR, uint32_t nB,
-              float2* __restrict__ out)
+k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size_t part2,
+              const uint32_t* __restrict__ nonempty, int ov, const float2* __restrict__ taps, uint32_t ntaps,
+              uint32_t nR, uint32_t nB, float2* __restrict__ out)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int ntc = min((int)max(ntaps, 1u), kFiltTapsMax);
@@ -556,8 +571,12 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, cons
     float2* sT = sG + (size_t)(kFiltRows + ntc - 1) * kFiltCols;       // [kFiltTapsMax]
     int* sW = reinterpret_cast<int*>(sT + kFiltTapsMax);                // [kFiltRows]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols;
-    if(tid < kFiltRows) sW[tid] = (r0 + tid < (int)nR) ? (row_has_window(nonempty, nR, ov, r0 + tid) ? 1 : 0) : 0;
+    const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols, par = blockIdx.z;
+    taps += (size_t)par * ntaps;
+    if(tid < kFiltRows) {
+        const int r = 2 * (r0 + tid) + par;
+        sW[tid] = r < (int)nR ? (row_has_window(nonempty, nR, ov, r) ? 1 : 0) : 0;
+    }
     float2 acc[8][2];
 #pragma unroll
     for(int q = 0; q < 8; q++) { acc[q][0] = make_float2(0.f, 0.f); acc[q][1] = make_float2(0.f, 0.f); }
@@ -577,7 +596,15 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, cons
 #pragma unroll
             for(int h = 0; h < 2; h++) {
                 const int k = k0 + 32 * h + lane;
-                v[i][h] = (live && k < (int)nB) ? __ldg(row + k) : make_float2(0.f, 0.f);
+                float2 x = make_float2(0.f, 0.f);
+                if(live && k < (int)nB) {
+                    float2 y[kParts];
+#pragma unroll
+                    for(int z = 0; z < kParts; z++) y[z] = __ldg(row + (size_t)z * part2 + k);
+#pragma unroll
+                    for(int z = 0; z < kParts; z++) { x.x += y[z].x; x.y += y[z].y; }
+                }
+                v[i][h] = x;
             }
         }
 #pragma unroll
@@ -628,7 +655,7 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, cons
     }
 #pragma unroll
     for(int q = 0; q < 8; q++) {
-        const int r = r0 + warp * 8 + q;
+        const int r = 2 * (r0 + warp * 8 + q) + par;
         if(r >= (int)nR) continue;
         const bool on = sW[warp * 8 + q] != 0;
 #pragma unroll
@@ -760,6 +787,88 @@ void project_directivity(const std::vector<float>& g, const std::vector<float>& 
     }
 }
 
+// Range nodes of the binned model's output rows: one node every two output
+// bins (node m at range_min + m * 2 * resolution; output row r uses node
+// r / 2 and the taps of its parity r % 2).
+uint32_t range_nodes(uint32_t nR) { return ((nR - 1u) >> 1) + 1u; }
+
+// Derived range taps: for output row r = 2 m + p the pulse response
+// P(x - R_r), seen from node m, is P(x - p res); its least-squares (L2)
+// projection onto the hat functions of the nodes (spacing h = 2 res) gives
+// taps[p][t], the weight of node m + t - center. P is the texture-equivalent
+// lerp of the pulse table (border addressing; coordinate y ky + cy). Each
+// right-hand side integrates hat x P over the two halves of the hat, split
+// at the pulse table's knots, with the three-point Gauss-Legendre rule
+// (exact for these linear x linear pieces); the Gram system of the uniform
+// hats (h / 6, 2 h / 3, h / 6) is solved (Thomas) on the nodes the pulse
+// reaches widened by kTapPad + kSolvePad on each side, and the nodes widened
+// by kTapPad are kept. Output: taps complex [2][L] as float pairs.
+constexpr int kTapPad = 6, kSolvePad = 10;
+
+void project_range_taps(const std::vector<float>& pulse, uint32_t H, float res_f, float pscale,
+                        std::vector<float>& taps, uint32_t& center)
+{
+    const double res = res_f, hr = (double)(2.0f * res_f);
+    const double ky = (double)pscale * H, cy = 0.5 * H - 0.5;
+    const double y_lo = (-1.0 - cy) / ky, y_hi = (H - cy) / ky;
+    const int dmin = (int)std::floor(y_lo / hr) - 1;
+    const int dmax = (int)std::ceil((y_hi + res) / hr) + 1;
+    const int s0 = dmin - kTapPad - kSolvePad, s1 = dmax + kTapPad + kSolvePad;
+    const int ns = s1 - s0 + 1, L = dmax - dmin + 1 + 2 * kTapPad;
+    const double gx[3] = {-std::sqrt(0.6), 0.0, std::sqrt(0.6)}, gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+    taps.assign((size_t)4 * L, 0.0f);
+    std::vector<double> fr(ns), fi(ns), cp(ns), dr(ns), di(ns), xr(ns), xi(ns);
+    for(int p = 0; p < 2; p++) {
+        const double off = p * res;
+        for(int i = 0; i < ns; i++) {
+            const int dd = s0 + i;
+            double sr = 0.0, si = 0.0;
+            for(int half_i = 0; half_i < 2; half_i++) {
+                const double a = (dd - 1 + half_i) * hr, b = (dd + half_i) * hr;
+                std::vector<double> pts{a};
+                const long long k_lo = (long long)std::ceil((a - off) * ky + cy), k_hi = (long long)std::floor((b - off) * ky + cy);
+                for(long long k = k_lo; k <= k_hi; k++) {
+                    const double x = off + ((double)k - cy) / ky;
+                    if(x >= a && x <= b) pts.push_back(x);
+                }
+                pts.push_back(b);
+                std::sort(pts.begin(), pts.end());
+                for(size_t e = 0; e + 1 < pts.size(); e++) {
+                    const double half = 0.5 * (pts[e + 1] - pts[e]), mid = 0.5 * (pts[e + 1] + pts[e]);
+                    if(!(half > 0.0)) continue;
+                    for(int g = 0; g < 3; g++) {
+                        const double x = mid + half * gx[g];
+                        const double xt = (x - off) * ky + cy;
+                        const double lam = half_i == 0 ? (x - a) / hr : (b - x) / hr;
+                        const double wq = gw[g] * half * lam;
+                        sr += wq * host_lerp(pulse.data(), (int)H, 2, 0, xt);
+                        si += wq * host_lerp(pulse.data(), (int)H, 2, 1, xt);
+                    }
+                }
+            }
+            fr[i] = sr; fi[i] = si;
+        }
+        // Thomas algorithm: sub = sup = h / 6, diag = 2 h / 3 on every row.
+        const double sub = hr / 6.0, diag = 2.0 * hr / 3.0;
+        for(int i = 0; i < ns; i++) {
+            const double den = diag - (i > 0 ? sub * cp[i - 1] : 0.0);
+            cp[i] = sub / den;
+            dr[i] = (fr[i] - (i > 0 ? sub * dr[i - 1] : 0.0)) / den;
+            di[i] = (fi[i] - (i > 0 ? sub * di[i - 1] : 0.0)) / den;
+        }
+        for(int i = ns; i-- > 0;) {
+            xr[i] = dr[i] - (i + 1 < ns ? cp[i] * xr[i + 1] : 0.0);
+            xi[i] = di[i] - (i + 1 < ns ? cp[i] * xi[i + 1] : 0.0);
+        }
+        for(int t = 0; t < L; t++) {
+            const int i = (dmin - kTapPad + t) - s0;
+            taps[((size_t)p * L + t) * 2] = (float)xr[i];
+            taps[((size_t)p * L + t) * 2 + 1] = (float)xi[i];
+        }
+    }
+    center = (uint32_t)(kTapPad - dmin);
+}
+
 #define RTACX_CUDA(call)                                                         \
     do {                                                                         \
         cudaError_t e_ = (call);                                                 \
@@ -822,51 +931,41 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     if(!(step > 0.0f) || !std::isfinite(1.0f / step)) { ctx.error = "degenerate bearing grid"; return RTACX_ERR_INVALID_ARGUMENT; }
     free_precision(ctx);
 
-    // Range taps, given or derived from the pulse table at bin offsets.
+    // Range taps (two phases: even and odd output rows), given or projected
+    // from the pulse table.
     std::vector<float> taps;
     uint32_t center;
     if(d->range_taps) {
         if(d->tap_count == 0 || d->tap_center >= d->tap_count) { ctx.error = "bad tap_count / tap_center"; return RTACX_ERR_INVALID_ARGUMENT; }
-        taps.assign(d->range_taps, d->range_taps + 2 * (size_t)d->tap_count);
+        if(d->tap_count > 1024) { ctx.error = "tap_count above 1024"; return RTACX_ERR_UNSUPPORTED; }
+        taps.assign(d->range_taps, d->range_taps + 4 * (size_t)d->tap_count);
         center = d->tap_center;
     }
     else {
-        const int ov = std::max(0, ctx.overlap);
-        const double res = (double)((ctx.rmax - ctx.rmin) / (float)(nR - 1u));
-        const float pscale = host_pulse_scale(ctx.duration, ctx.c, false);
-        const double ky = (double)pscale * ctx.H, cy = 0.5 * ctx.H - 0.5;
-        int lo_t = ov + 1, hi_t = -ov - 1;
-        std::vector<float> full((size_t)(2 * ov + 1) * 2);
-        for(int t = -ov; t <= ov; t++) {
-            const double x = t * res * ky + cy;
-            const float re = (float)host_lerp(ctx.pulse.data(), (int)ctx.H, 2, 0, x);
-            const float im = (float)host_lerp(ctx.pulse.data(), (int)ctx.H, 2, 1, x);
-            full[(size_t)(t + ov) * 2] = re; full[(size_t)(t + ov) * 2 + 1] = im;
-            if(re != 0.0f || im != 0.0f) { lo_t = std::min(lo_t, t); hi_t = std::max(hi_t, t); }
-        }
-        if(lo_t > hi_t) { lo_t = 0; hi_t = 0; }
-        taps.assign(full.begin() + (size_t)(lo_t + ov) * 2, full.begin() + (size_t)(hi_t + ov + 1) * 2);
-        center = (uint32_t)(-lo_t);
+        project_range_taps(ctx.pulse, ctx.H, (ctx.rmax - ctx.rmin) / (float)(nR - 1u),
+                           host_pulse_scale(ctx.duration, ctx.c, false), taps, center);
     }
     for(float v : taps) if(!std::isfinite(v)) { ctx.error = "non-finite range taps"; return RTACX_ERR_INVALID_ARGUMENT; }
-    const uint32_t ntaps = (uint32_t)(taps.size() / 2);
+    const uint32_t ntaps = (uint32_t)(taps.size() / 4);
     ctx.taps = ntaps;
     ctx.tap_center = center;
 
     // Grid parameters (the oracle computes the same floats).
     GridParams& g = ctx.grid;
+    const uint32_t nodes = range_nodes(nR);
     g.rmin = ctx.rmin;
-    g.res = (ctx.rmax - ctx.rmin) / (float)(nR - 1u);
+    g.res = 2.0f * ((ctx.rmax - ctx.rmin) / (float)(nR - 1u));
     g.inv_res = 1.0f / g.res;
     g.first = first;
     g.step = step;
     g.inv_step = 1.0f / step;
     g.cells = cells;
+    g.pitch = cells + kRowPad;
     g.row_lo = -(int)center - 1;
-    g.row_hi = (int)nR + (int)ntaps - (int)center - 2;
+    g.row_hi = (int)nodes + (int)ntaps - (int)center - 2;
     g.row_shift = (int)center + 1;
     if(!(g.res > 0.0f) || !std::isfinite(g.inv_res)) { ctx.error = "degenerate range axis"; return RTACX_ERR_INVALID_ARGUMENT; }
-    ctx.grid_rows = nR + ntaps + 1;
+    ctx.grid_rows = nodes + ntaps + 1;
 
     // Directivity D[q][b] (complex), given or projected from the beam table.
     std::vector<float> D((size_t)cells * nB * 2, 0.0f);
@@ -903,7 +1002,8 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         cudaGetLastError();
         ctx.acc_staged_blocks[m] = (uint32_t)std::max(bs, 0);
     }
-    if(raise_smem_limit((const void*)k_prec_filter, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
+    if(raise_smem_limit((const void*)k_prec_filter<1>, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess ||
+       raise_smem_limit((const void*)k_prec_filter<2>, filter_smem_bytes(kFiltTapsMax)) != cudaSuccess) {
         ctx.error = "cannot reserve shared memory for the range filter";
         return RTACX_ERR_CUDA;
     }
@@ -913,6 +1013,11 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
     ctx.Mpad = (ctx.grid_rows + 127) / 128 * 128;
     ctx.Npad = (2 * nB + 255) / 256 * 256;
     ctx.Kp = (6 * cells + 63) / 64 * 64;
+    // Split K in two when the 128 x 256 output tiles cover at most half of
+    // the SMs (the node grid of a 4096-range ping: 68 tiles on 152 SMs): twice
+    // the CTAs, each over half of K; the range filter adds the two partials.
+    ctx.ksplit = ((uint64_t)(ctx.Npad / 256) * (ctx.Mpad / 128) * 2 <= (uint64_t)ctx.sm_count &&
+                  (ctx.Kp / 64) % 2 == 0) ? 2u : 1u;
 
     // B operand: row n = 2b (real) / 2b + 1 (imag); K blocks [hi | lo | hi]
     // of [real part of G | imaginary part of G]. FP16 form: each row n is
@@ -956,14 +1061,14 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         if(cudaMalloc(&p, bytes) != cudaSuccess) { cudaGetLastError(); p = nullptr; return false; }
         return true;
     };
-    const size_t grid_bytes = (size_t)ctx.grid_rows * cells * sizeof(float2);
+    const size_t grid_bytes = (size_t)ctx.grid_rows * g.pitch * sizeof(float4);
     if(!alloc(ctx.d_G, grid_bytes) || !alloc(ctx.d_flags, (size_t)(nR + 31) / 32 * 4) ||
        !alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) || !alloc(ctx.d_B, B.size() * 2) ||
-       !alloc(ctx.d_taps, taps.size() * sizeof(float)) || !alloc(ctx.d_C, (size_t)ctx.Mpad * ctx.Npad * sizeof(float)) ||
+       !alloc(ctx.d_taps, taps.size() * sizeof(float)) || !alloc(ctx.d_C, (size_t)ctx.ksplit * ctx.Mpad * ctx.Npad * sizeof(float)) ||
        (f16 && (!alloc(ctx.d_row_scale, (size_t)ctx.Mpad * sizeof(float)) ||
                 !alloc(ctx.d_col_scale, (size_t)ctx.Npad * sizeof(float)))) ||
        (hot && (!alloc(ctx.d_hot, sizeof(int2)) || !alloc(ctx.d_hotcnt, (size_t)ctx.grid_rows * 4) ||
-                !alloc(ctx.d_rep, (size_t)kHotRows * kHotReplicas * cells * sizeof(float2))))) {
+                !alloc(ctx.d_rep, (size_t)kHotRows * kHotReplicas * g.pitch * sizeof(float4))))) {
         free_precision(ctx);
         ctx.error = "out of device memory for the precision form";
         return RTACX_ERR_OUT_OF_MEMORY;
@@ -996,9 +1101,9 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
 // Zeroes the grid and the non-empty bitmap of a new ping.
 rtacx_status precision_begin(Context& ctx, cudaStream_t stream)
 {
-    const uint64_t quads = (uint64_t)ctx.grid_rows * ctx.grid.cells / 2;
+    const uint64_t quads = (uint64_t)ctx.grid_rows * ctx.grid.pitch;
     const uint32_t blocks = (uint32_t)std::min<uint64_t>((quads + 255) / 256, (uint64_t)ctx.sm_count * 32);
-    k_prec_clear<<<blocks, 256, 0, stream>>>(reinterpret_cast<float4*>(ctx.d_G), quads, ctx.d_flags, (ctx.nR + 31) / 32);
+    k_prec_clear<<<blocks, 256, 0, stream>>>(ctx.d_G, quads, ctx.d_flags, (ctx.nR + 31) / 32);
     RTACX_CUDA(cudaGetLastError());
     return RTACX_OK;
 }
@@ -1045,7 +1150,7 @@ rtacx_status precision_hot_scan(Context& ctx, const void* samples, uint64_t n, c
     k_hot_pick<<<1, kHotPickThreads, (ctx.grid_rows + 1) * sizeof(uint32_t), stream>>>(ctx.d_hotcnt, ctx.grid_rows,
                                                                                         ctx.d_hot);
     RTACX_CUDA(cudaGetLastError());
-    k_hot_zero<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, ctx.grid.cells, ctx.d_rep);
+    k_hot_zero<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, ctx.grid.pitch, ctx.d_rep);
     RTACX_CUDA(cudaGetLastError());
     return RTACX_OK;
 }
@@ -1070,32 +1175,32 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
 {
     const uint32_t nR = ctx.nR, nB = ctx.nB, cells = ctx.grid.cells;
     if(ctx.prec_hot) {
-        k_hot_fold<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, cells, ctx.d_rep, ctx.d_G);
+        k_hot_fold<<<ctx.sm_count * 4, 256, 0, stream>>>(ctx.d_hot, ctx.grid.pitch, ctx.d_rep, ctx.d_G);
         RTACX_CUDA(cudaGetLastError());
     }
     ctx.mark(1, false, stream);
     if(!ctx.prec_f16) {
         const dim3 sgrid((cells / 2 + 255) / 256, ctx.grid_rows);
-        k_prec_split<<<sgrid, 256, 0, stream>>>(reinterpret_cast<const float4*>(ctx.d_G), ctx.grid_rows, cells, ctx.Kp,
-                                                ctx.d_A);
+        k_prec_split<<<sgrid, 256, 0, stream>>>(ctx.d_G, ctx.grid_rows, cells, ctx.grid.pitch, ctx.Kp, ctx.d_A);
     }
     else {
-        k_prec_split_f16<<<ctx.grid_rows, kSplitF16Threads, 0, stream>>>(ctx.d_G, ctx.grid_rows, cells, ctx.Kp, ctx.d_A,
-                                                                         ctx.d_row_scale);
+        k_prec_split_f16<<<ctx.grid_rows, kSplitF16Threads, 0, stream>>>(ctx.d_G, ctx.grid_rows, cells, ctx.grid.pitch,
+                                                                         ctx.Kp, ctx.d_A, ctx.d_row_scale);
     }
     RTACX_CUDA(cudaGetLastError());
     ctx.mark(1, true, stream);
     ctx.mark(3, false, stream);
     rtacx_status st = gemm_tn(ctx.error, ctx.d_A, ctx.d_B, ctx.d_C, (int)ctx.Mpad, (int)ctx.Npad, (int)ctx.Kp,
                               (int)ctx.Npad, stream, ctx.d_err, ctx.prec_f16, ctx.prec_f16 ? ctx.d_row_scale : nullptr,
-                              ctx.prec_f16 ? ctx.d_col_scale : nullptr);
+                              ctx.prec_f16 ? ctx.d_col_scale : nullptr, (int)ctx.ksplit);
     if(st != RTACX_OK) return st;
     ctx.mark(3, true, stream);
     ctx.mark(2, false, stream);
-    const dim3 fgrid((nB + kFiltCols - 1) / kFiltCols, (nR + kFiltRows - 1) / kFiltRows);
-    k_prec_filter<<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
-        reinterpret_cast<const float2*>(ctx.d_C), ctx.Npad / 2, ctx.grid_rows, ctx.d_flags, ctx.overlap, ctx.d_taps,
-        ctx.taps, nR, nB, reinterpret_cast<float2*>(out));
+    const dim3 fgrid((nB + kFiltCols - 1) / kFiltCols, (range_nodes(nR) + kFiltRows - 1) / kFiltRows, 2);
+    auto filter = ctx.ksplit == 2 ? k_prec_filter<2> : k_prec_filter<1>;
+    filter<<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
+        reinterpret_cast<const float2*>(ctx.d_C), ctx.Npad / 2, ctx.grid_rows, (size_t)ctx.Mpad * ctx.Npad / 2,
+        ctx.d_flags, ctx.overlap, ctx.d_taps, ctx.taps, nR, nB, reinterpret_cast<float2*>(out));
     RTACX_CUDA(cudaGetLastError());
     ctx.mark(2, true, stream);
     return RTACX_OK;

@@ -134,7 +134,10 @@ k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
-    const int nkb = K / BK;
+    // Split K: CTA z multiplies K blocks [z nkb, (z + 1) nkb) into its own
+    // partial product C + z M ldc (the caller sums the partials).
+    const int nkb = K / BK / (int)gridDim.z, kb0 = (int)blockIdx.z * nkb;
+    C += (size_t)blockIdx.z * (size_t)M * ldc;
     auto full_bar = [&](int s) { return smem_u32(bars + s); };
     auto empty_bar = [&](int s) { return smem_u32(bars + STAGES + s); };
     const uint32_t accum_bar = smem_u32(bars + 2 * STAGES);
@@ -165,8 +168,8 @@ k_gemm_tn(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
             if(kb >= STAGES && !mbar_wait(empty_bar(s), ((kb / STAGES) - 1) & 1, abort_flag)) break;
             unsigned char* a = base + s * STAGE_BYTES;
             mbar_expect_tx(full_bar(s), STAGE_BYTES);
-            tma_load_2d(smem_u32(a), &tmA, kb * BK, m0, full_bar(s));
-            tma_load_2d(smem_u32(a + A_BYTES), &tmB, kb * BK, n0, full_bar(s));
+            tma_load_2d(smem_u32(a), &tmA, (kb0 + kb) * BK, m0, full_bar(s));
+            tma_load_2d(smem_u32(a + A_BYTES), &tmB, (kb0 + kb) * BK, n0, full_bar(s));
         }
     }
     else if(warp == 1 && lane == 0) {
@@ -271,19 +274,36 @@ size_t gemm_smem_bytes() { return std::max(TileWide::SMEM_BYTES, TileNarrow::SME
 // C = row_scale * col_scale * (A * B^T); A [M][K], B [N][K] both bf16 or
 // both fp16 (16-byte aligned, row stride K), C [M][ldc] fp32, scales
 // optional (row_scale [M], col_scale [N], 16-byte aligned). Shapes must be
-// multiples of the tile (128, 256, 64).
+// multiples of the tile (128, 128, 64). ksplit > 1 splits K into that many
+// parts with partial products at C + z M ldc, z = 0 .. ksplit - 1, for the
+// caller to sum.
 rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C, int M, int N, int K, int ldc,
-                     cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale)
+                     cudaStream_t stream, uint32_t* err, bool f16, const float* row_scale, const float* col_scale,
+                     int ksplit)
 {
     if(M <= 0 || N <= 0 || K <= 0 || M % BM || N % 128 || K % BK || ldc < N || ldc % 4) {
         error = "gemm shape must be multiples of 128 x 128 x 64";
         return RTACX_ERR_INVALID_ARGUMENT;
     }
-    // 128 x 256 tiles whenever N allows them; 128 x 128 tiles (two CTAs per
-    // SM) for N a multiple of 128 only. Measured on the 4096 x 1024 x 3072
-    // contraction: 27 us wide, 30 us narrow (the narrow grid re-reads A twice
-    // as often through L2).
-    const bool wide = N % 256 == 0;
+    if(ksplit < 1 || ksplit > 8 || (K / BK) % ksplit) {
+        error = "gemm K split must divide the K blocks (1 to 8 parts)";
+        return RTACX_ERR_INVALID_ARGUMENT;
+    }
+    // 128 x 256 tiles when N allows them and they cover more than half of
+    // the SMs; 128 x 128 tiles (two CTAs per SM) otherwise. Measured on the
+    // 4096 x 1024 x 3072 contraction (128 wide tiles): 27 us wide, 30 us
+    // narrow (the narrow grid re-reads A twice as often through L2); with
+    // half the SMs or fewer, wide tiles leave the tensor cores of the rest
+    // idle for the whole launch.
+    int dev_sms = 0;
+    {
+        int d0 = 0;
+        if(cudaGetDevice(&d0) != cudaSuccess || cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, d0) != cudaSuccess) {
+            cudaGetLastError();
+            dev_sms = 0;
+        }
+    }
+    const bool wide = N % 256 == 0 && 2ll * (N / 256) * (M / BM) * ksplit > (long long)dev_sms;
     const int bn = wide ? TileWide::BN : TileNarrow::BN;
     if((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) % 16 || reinterpret_cast<uintptr_t>(C) % 16 ||
        reinterpret_cast<uintptr_t>(col_scale) % 16) {
@@ -318,7 +338,7 @@ rtacx_status gemm_tn(std::string& error, const void* A, const void* B, float* C,
         }
         attr_done.fetch_or(1ull << dev);
     }
-    dim3 grid(N / bn, M / BM);
+    dim3 grid(N / bn, M / BM, ksplit);
     if(wide) {
         if(f16) k_gemm_tn<true, TileWide><<<grid, kThreads, TileWide::SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
         else k_gemm_tn<false, TileWide><<<grid, kThreads, TileWide::SMEM_BYTES, stream>>>(ma, mb, C, M, N, K, ldc, row_scale, col_scale, err);
@@ -349,7 +369,7 @@ extern "C" rtacx_status rtacx_gemm_bf16_tn(const void* A, const void* B, float* 
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if(cudaMemsetAsync(err, 0, sizeof(uint32_t), s) != cudaSuccess) { cudaGetLastError(); return RTACX_ERR_CUDA; }
-    rtacx_status st = rtacx::gemm_tn(error, A, B, C, M, N, K, N, s, err, false, nullptr, nullptr);
+    rtacx_status st = rtacx::gemm_tn(error, A, B, C, M, N, K, N, s, err, false, nullptr, nullptr, 1);
     if(st != RTACX_OK) return st;
     uint32_t word = 0;
     if(cudaStreamSynchronize(s) != cudaSuccess ||

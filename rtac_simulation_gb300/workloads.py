@@ -458,11 +458,12 @@ def precision_tables(sensor: dict, steer: float = 0.0, grid_count: int = 0, grid
     a uniform grid of `grid_count` bearings (default 4 x bearing_count) from
     the first to the last table bearing, the directivity projected onto it
     (project_directivity; with steer = kappa != 0 it carries the phase of a
-    phase reference off the origin and is complex), and the range taps
-    taps[t] = pulse((t - center) * resolution) for |t - center| <= overlap,
-    trimmed to the non-zero span. Returns the keyword arguments of
+    phase reference off the origin and is complex), and the range taps of
+    the range nodes two output bins apart, one set per output-row parity
+    (range_taps). Returns the keyword arguments of
     Context.configure_precision: directivity (complex64 [grid_count][nB]),
-    range_taps, tap_center, grid_count, grid_first, grid_last."""
+    range_taps (complex64 [2][L]), tap_center, grid_count, grid_first,
+    grid_last."""
     bear = np.asarray(sensor["bearings"], np.float32)
     nB = bear.size
     cells = int(grid_count) or 4 * nB
@@ -475,24 +476,65 @@ def precision_tables(sensor: dict, steer: float = 0.0, grid_count: int = 0, grid
                 grid_first=first, grid_last=last)
 
 
+RANGE_STEP = 2      # output range bins per node of the precision form's range grid
+TAP_PAD = 6         # taps kept beyond the nodes the pulse reaches
+SOLVE_PAD = 10      # further nodes of the truncated Gram system
+
+
 def range_taps(sensor: dict):
-    """Range taps of the binned model: the pulse at whole-bin offsets t *
-    resolution, |t| <= overlap, trimmed to the non-zero span. Returns
-    (taps complex64, index of the zero offset)."""
+    """Range taps of the binned model, whose range grid has one node every
+    RANGE_STEP = 2 output bins (node m at range_min + m * 2 * resolution).
+    For output row r = 2 m + p the pulse response P(x - R_r), seen from node
+    m, is P(x - p * resolution); its least-squares (L2) projection onto the
+    hat functions of the nodes gives taps[p][t], the weight of node
+    m + t - center. P is the texture-equivalent lerp of the pulse table
+    (border addressing). The right-hand sides integrate hat x P over each
+    half of every hat, split at the pulse table's knots, with the three-point
+    Gauss-Legendre rule (exact: linear x linear); the Gram system of the
+    uniform hats (spacing h: h / 6, 2 h / 3, h / 6) is solved on the nodes
+    the pulse reaches widened by TAP_PAD + SOLVE_PAD on each side, and the
+    taps of the nodes widened by TAP_PAD are kept. Returns (taps complex64
+    [2][L], index of node offset 0)."""
     nR = sensor["range_count"]
-    res = float(linspace_resolution(sensor["range_min"], sensor["range_max"], nR)) if nR > 1 else 0.0
-    mres = np.float32(np.float32(sensor["range_max"]) - np.float32(sensor["range_min"]))
-    margin = np.float32(sensor["margin"])
-    ov = int(np.float32(margin / np.float32(mres / np.float32(nR - 1)))) if nR > 1 else 0
-    ov = max(ov, 0)
+    res = float(linspace_resolution(sensor["range_min"], sensor["range_max"], nR))
+    hr = float(F32(RANGE_STEP) * F32(res))
     pulse = np.asarray(sensor["pulse"], np.complex64).astype(np.complex128)
     H = pulse.size
     pscale = float(np.float32(1.0) / np.float32(np.float32(sensor["pulse_duration"]) * np.float32(sensor["sound_celerity"])))
-    t = np.arange(-ov, ov + 1)
-    x = t * res * (pscale * H) + 0.5 * H - 0.5
-    full = (_lerp(pulse.real, x) + 1j * _lerp(pulse.imag, x)).astype(np.complex64)
-    nz = np.nonzero(full)[0]
-    if nz.size == 0:
-        return np.zeros(1, np.complex64), 0
-    first, last = nz[0], nz[-1]
-    return full[first:last + 1], int(ov - first)
+    ky, cy = pscale * H, 0.5 * H - 0.5
+    y_lo, y_hi = (-1.0 - cy) / ky, (H - cy) / ky            # P is zero outside (y_lo, y_hi)
+    dmin = int(math.floor(y_lo / hr)) - 1
+    dmax = int(math.ceil((y_hi + (RANGE_STEP - 1) * res) / hr)) + 1
+    s0, s1 = dmin - TAP_PAD - SOLVE_PAD, dmax + TAP_PAD + SOLVE_PAD
+    d = np.arange(s0, s1 + 1)
+    taps = []
+    for p in range(RANGE_STEP):
+        off = p * res
+        f = np.zeros(d.size, np.complex128)
+        for i, dd in enumerate(d):
+            for a, b, up in (((dd - 1) * hr, dd * hr, True), (dd * hr, (dd + 1) * hr, False)):
+                # knots of P(x - off) inside (a, b)
+                k_lo = math.ceil((a - off) * ky + cy)
+                k_hi = math.floor((b - off) * ky + cy)
+                pts = [a] + [off + (k - cy) / ky for k in range(k_lo, k_hi + 1)] + [b]
+                pts = sorted(x for x in pts if a <= x <= b)
+                for lo, hi in zip(pts[:-1], pts[1:]):
+                    half = 0.5 * (hi - lo)
+                    if not half > 0:
+                        continue
+                    mid = 0.5 * (hi + lo)
+                    for node, weight in _GL3:
+                        x = mid + half * node
+                        xt = np.array([(x - off) * ky + cy])
+                        pv = (_lerp(pulse.real, xt) + 1j * _lerp(pulse.imag, xt))[0]
+                        lam = (x - a) / hr if up else (b - x) / hr
+                        f[i] += weight * half * lam * pv
+        from scipy.linalg import solve_banded
+        ab = np.zeros((3, d.size))
+        ab[0, 1:] = hr / 6.0
+        ab[1, :] = 2.0 * hr / 3.0
+        ab[2, :-1] = hr / 6.0
+        t = solve_banded((1, 1), ab, f)
+        keep = (d >= dmin - TAP_PAD) & (d <= dmax + TAP_PAD)
+        taps.append(t[keep])
+    return np.array(taps, np.complex64), int(TAP_PAD - dmin)

@@ -226,7 +226,7 @@ def test_precision_long_pulse_multi_chunk_filter(oracle, flags):
     """101 range taps: the range filter stages its taps in several chunks."""
     wk = wl.precision_2d(n_samples=1 << 15, n_bearings=128, n_ranges=512, taps=101)
     tab = tables(wk)
-    assert tab["range_taps"].size > 64
+    assert tab["range_taps"].shape[1] > 64            # taps per output-row parity
     want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
     got = gpu_precision(precision_context(wk, flags=flags), wk.samples, wk.out_shape)
     assert rel_l2(got, want) <= TOL
@@ -453,10 +453,10 @@ def per_sample_ping(ctx_plain, wk, steer):
 @pytest.mark.parametrize("n_ranges", [1024, 4096])
 def test_precision_model_close_to_per_sample_psf(n_ranges):
     """The binned model against the reference's per-sample PSF (the plain
-    form, itself within 1e-5 of the FP64 oracle) on the same ping: the
-    range split is the per-sample interpolation, the bearing grid of four
-    cells per output bearing with the projected directivity leaves about
-    5e-3 relative L2 (bar: 1e-2)."""
+    form, itself within 1e-5 of the FP64 oracle) on the same ping: range
+    nodes two bins apart with the projected taps and the bearing grid of
+    four cells per output bearing with the projected directivity leave about
+    6e-3 to 7e-3 relative L2 (bar: 1e-2)."""
     wk = wl.precision_2d(n_samples=1 << 18, n_ranges=n_ranges)
     prec = gpu_precision(precision_context(wk), wk.samples, wk.out_shape)
     plain_ctx = make_context(wk)

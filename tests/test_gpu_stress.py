@@ -78,9 +78,10 @@ def test_stress_reduced_precision_matches_oracle(oracle):
 
 @pytest.mark.parametrize("flags_name", ["RTACX_PRECISION_HOT_RANGE", "RTACX_PRECISION_HOT_RANGE|FP16"])
 def test_stress_reduced_precision_hot_range_matches_oracle(oracle, flags_name):
-    """Clustered ping with the hot-range replicas (the densest 256 range rows
-    accumulate into 8 replicas the filter sums): same oracle bar, through the
-    device and the host-buffer entry points."""
+    """Clustered ping with the hot-range replicas (the densest 128 range
+    nodes, 256 output bins, accumulate into 8 replicas added back before the
+    contraction): same oracle bar, through the device and the host-buffer
+    entry points."""
     from rtac_simulation_gb300 import _lib
     from test_gpu_precision import gpu_precision_host
     flags = _lib.RTACX_PRECISION_HOT_RANGE
