@@ -714,10 +714,12 @@ def run_ours(args, world, rank, local):
     gather_s = st["reduce"] / 1e3
     fp32_peak = 152 * 128 * 2 * peaks["sm_max_mhz"] * 1e6 / 1e12
     gather_tf = 8.0 * pairs / gather_s / 1e12 if gather_s > 0 else 0.0
-    roof_plain = {"bound": "fp32", "achieved": gather_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+    roof_plain = {"bound": "fp32" if wk.dims == 1 else "issue (operand construction of the tensor-core gather)",
+                  "achieved": gather_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                   "frac": gather_tf / fp32_peak, "traffic": None,
-                  "kernel": "k_gather_split" if wk.dims == 2 else "k_gather_1d",
-                  "peak_source": "nominal FP32 SIMT (152 SMs x 128 FMA x max clock); no measured FP32 peak",
+                  "kernel": "k_gather_tc (TF32 x3 tcgen05)" if wk.dims == 2 else "k_gather_1d",
+                  "peak_source": "nominal FP32 SIMT (152 SMs x 128 FMA x max clock), the FP32-equivalent "
+                                 "denominator of the useful work; no measured FP32 peak",
                   "algorithmic": "8 flop per useful (sample, output cell) pair, %.3e pairs" % pairs}
     bin_bytes = n * (rec_in + 16)
     bin_s = (st["count"] + st["reset"] + st["binscan"] + st["scatter"] + st["windows"]) / 1e3

@@ -85,6 +85,13 @@ typedef int rtacx_status;
  * Without the flags the 1D pulse is the exact linear interpolation of the
  * table, zero outside it (the evident intent). */
 #define RTACX_FLAG_TEXTURE_CLAMP 4u
+/* rtacx_sensor_2d.flags: gather with the FP32 CUDA-core kernel instead of the
+ * tensor-core one. By default a 2D ping's gather (output tiles of 64 ranges x
+ * 128 bearings) forms its sample-by-PSF outer products on the tcgen05 tensor
+ * cores from TF32 operands split in hi + lo parts (three products, FP32
+ * accumulation: the same accuracy as the FP32 path, the float additions in
+ * another order). */
+#define RTACX_FLAG_SIMT_GATHER 8u
 
 /* 1D echosounder (SensorInstance1D, include/rtac_simulation/SensorInstance1D.h). */
 typedef struct {
@@ -351,7 +358,9 @@ rtacx_status rtacx_rasterize(rtacx_ctx* ctx, const rtacx_mesh* mesh, const rtacx
  * into the graph: re-plan when any of them changes) and, with
  * RTACX_BATCH_AUTOTUNE, times every candidate gather tile shape x samples
  * per binning chunk on this batch and keeps the fastest. rtacx_batch_run
- * replays the graph on `stream`. Results equal rtacx_reduce's per ping. */
+ * replays the graph on `stream`. Results equal rtacx_reduce's per ping with
+ * RTACX_FLAG_SIMT_GATHER (the batch gathers on the CUDA cores), and the
+ * default tensor-core gather's to float round-off. */
 typedef struct rtacx_batch rtacx_batch;
 typedef struct {
     rtacx_ctx* ctx;          /* configured context, one per ping          */

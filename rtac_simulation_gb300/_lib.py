@@ -27,6 +27,7 @@ RTACX_SAMPLE_2D = 2
 RTACX_FLAG_1D_LITERAL_SCALING = 1
 RTACX_FLAG_TEXTURE_PSF = 2
 RTACX_FLAG_TEXTURE_CLAMP = 4
+RTACX_FLAG_SIMT_GATHER = 8
 
 _STATUS_NAMES = {
     RTACX_OK: "RTACX_OK",

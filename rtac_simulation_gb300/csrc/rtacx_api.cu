@@ -325,7 +325,7 @@ rtacx_status rtacx_configure_2d(rtacx_ctx* ctx, const rtacx_sensor_2d* s)
     if(!s->beam || s->beam_len == 0) { c.error = "beam table is empty"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(!s->bearings || s->bearing_count == 0) { c.error = "bearing table is empty"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(!(s->beam_span > 0.0f) || !std::isfinite(s->beam_span)) { c.error = "beam_span must be positive"; return RTACX_ERR_INVALID_ARGUMENT; }
-    if(s->flags & ~RTACX_FLAG_TEXTURE_PSF) { c.error = "unknown 2D sensor flags"; return RTACX_ERR_INVALID_ARGUMENT; }
+    if(s->flags & ~(RTACX_FLAG_TEXTURE_PSF | RTACX_FLAG_SIMT_GATHER)) { c.error = "unknown 2D sensor flags"; return RTACX_ERR_INVALID_ARGUMENT; }
     if(!all_finite(s->beam, s->beam_len) || !all_finite(s->bearings, s->bearing_count)) {
         c.error = "beam or bearing table holds non-finite values";
         return RTACX_ERR_INVALID_ARGUMENT;

@@ -24,6 +24,7 @@ constexpr uint32_t kErrBadWindow       = 1u << 1;  // window bounds outside the 
 constexpr uint32_t kErrGemmTimeout     = 1u << 2;  // a bounded mbarrier wait of the tensor-core GEMM expired
 constexpr uint32_t kErrAccumulateTimeout = 1u << 3; // a bounded wait for a staged copy of samples expired
 constexpr uint32_t kErrBatchWaitTimeout  = 1u << 4; // a bounded grid-barrier wait of the fused batched kernel expired
+constexpr uint32_t kErrGatherTimeout     = 1u << 5; // a bounded mbarrier wait of the tensor-core gather expired
 
 // Largest (range bin x bearing bin) histogram a CTA keeps in shared memory.
 constexpr uint32_t kMaxSmemBins = 49152;

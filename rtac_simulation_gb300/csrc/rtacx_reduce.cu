@@ -21,6 +21,7 @@
 // outside its rows' windows.
 #include "rtacx_bin_device.cuh"
 #include "rtacx_internal.cuh"
+#include "rtacx_tcgen05.cuh"
 
 #include <algorithm>
 
@@ -457,6 +458,364 @@ k_gather_split(const float4* __restrict__ sorted, const uint32_t* __restrict__ o
     }
 }
 
+// ---- tensor-core gather of one 2D ping (tcgen05, TF32 x3) -----------------
+// The gather of a tile is a sum of outer products: for every sample k of the
+// tile's stream, out(r, b) += U[k][r] B[k][b] with U[k][r] = v_k pulse(t_k -
+// R_r) (complex, zero outside row r's window) and B[k][b] = beam(theta_k -
+// theta_b) (real). k_gather_tc evaluates U and B for chunks of 32 samples
+// into shared memory and lets the tensor cores form the products: D (128 x
+// 128 fp32 in TMEM, rows 0..63 the real and 64..127 the imaginary parts of
+// 64 output ranges, columns 128 output bearings) += A B^T with A = [Re U; Im
+// U], both operands K-major in the 128-byte swizzle layout. FP32 accuracy
+// from TF32 operands: each operand is split into tf32 hi + lo (21 significant
+// bits together) and three MMAs form hi*hi + hi*lo + lo*hi, products exact
+// in the FP32 accumulator. Per chunk the 256 threads write the operands of
+// one of two stages while the MMAs of the other run; one thread issues the
+// MMAs and commits them to the stage's mbarrier. The persistent CTA takes
+// (tile, part) items like k_gather_split and adds each finished tile into
+// the zeroed ping with vector reductions.
+constexpr int kTcRows = 64, kTcBearings = 128, kTcChunk = 32;
+constexpr int kTcThreads = 512, kTcWarps = kTcThreads / 32;
+constexpr uint32_t kTcOpBytes = 128u * 128u;                 // 128 rows x 32 tf32
+constexpr uint32_t kTcStageBytes = 4u * kTcOpBytes;          // A hi, A lo, B hi, B lo
+constexpr uint32_t kTcTmemCols = 128;
+constexpr int kTcPitch = 129;                                // epilogue rows (floats), bank-conflict free
+constexpr long long kTcWaitCycles = 2000000000ll;            // about one second
+// The tensor cores' FP32 accumulation over a whole tile stream (up to 12
+// MMAs per chunk, hundreds of chunks) drifts to ~1e-5 relative; every
+// kTcFlush chunks the accumulator is added into FP32 registers (round to
+// nearest) and restarted, which keeps the tensor-core chains short.
+constexpr uint32_t kTcFlush = 8;
+// tcgen05.mma.kind::tf32 instruction descriptor: D f32 (bits 4-5 = 1), A and
+// B tf32 (format 2 at bits 7-9 and 10-12), both K-major, N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdescTf32 = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+struct TcSmem {
+    float4 smp[kTcChunk];
+    int bin[kTcChunk];
+    uint32_t seg_start[kTcThreads];
+    uint32_t seg_pre[kTcThreads + 1];
+    float R[kTcRows];
+    float theta[kTcBearings];
+    int elo[kTcRows], ehi[kTcRows];
+    uint32_t warp_sums[kTcWarps];
+    int jmin, jmax;
+    uint32_t item;
+    unsigned long long count;
+    unsigned long long bar[2];
+    uint32_t tmem;
+    int abort;
+};
+
+__device__ __forceinline__ uint32_t tf32_bits(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+// x as tf32 hi + lo: hi = tf32(x), lo = tf32(x - hi).
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo)
+{
+    hi = tf32_bits(x);
+    lo = tf32_bits(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdescTf32), "r"(accumulate)
+                 : "memory");
+}
+
+size_t gather_tc_smem_bytes(uint32_t H, uint32_t W)
+{
+    return 1024 + 2 * (size_t)kTcStageBytes + (H + 2) * sizeof(float2) + (W + 2) * sizeof(float);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_gather_tc(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
+            const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
+            const float* __restrict__ ranges, const float* __restrict__ bearings,
+            const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
+            ReduceParams rp, uint32_t nBB, float2* __restrict__ out,
+            const uint4* __restrict__ items, const uint32_t* __restrict__ n_items_ptr,
+            uint32_t* __restrict__ counter, uint32_t* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ TcSmem S;
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* stages = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    float2* s_pulse = reinterpret_cast<float2*>(stages + 2 * kTcStageBytes);
+    float* s_beam = reinterpret_cast<float*>(s_pulse + (rp.range_axis.n + 2));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nR = (int)rp.nR, nB = (int)rp.nB;
+    const uint32_t n_items = *n_items_ptr;
+
+    for(int i = tid; i < rp.range_axis.n + 2; i += kTcThreads) s_pulse[i] = pulse_pad[i];
+    for(int i = tid; i < rp.beam_axis.n + 2; i += kTcThreads) s_beam[i] = beam_pad[i];
+    if(tid == 0) {
+        mbar_init(smem_u32(&S.bar[0]), 1);
+        mbar_init(smem_u32(&S.bar[1]), 1);
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if(warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem;
+    uint32_t gchunk = 0;          // chunks committed by this CTA (stage = gchunk & 1)
+    // This thread's share of the accumulator: TMEM lane quad * 32 + lane,
+    // columns 32 cg .. 32 cg + 31.
+    const int quad = warp & 3, cg = warp >> 2;
+    float acc[32];
+    // Waits for the last committed chunk, then adds the TMEM accumulator into
+    // acc (the next MMA starts a new chain). False if the wait expired.
+    auto flush = [&]() -> bool {
+        if(tid == 0 &&
+           !mbar_wait_bounded(smem_u32(&S.bar[(gchunk - 1) & 1u]), ((gchunk - 1) >> 1) & 1u, &S.abort, kTcWaitCycles))
+            atomicOr(err, kErrGatherTimeout);
+        __syncthreads();
+        if(S.abort) return false;
+        tc_fence_after();
+        {
+            uint32_t v[32];
+            tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(cg * 32), v);
+#pragma unroll
+            for(int q = 0; q < 32; q++) acc[q] += __uint_as_float(v[q]);
+        }
+        tc_fence_before();
+        __syncthreads();
+        return true;
+    };
+
+    for(;;) {
+        if(tid == 0) S.item = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t it = S.item;
+        if(it >= n_items || S.abort) break;
+        const uint4 item = items[it];
+        const int r0 = (int)item.y * kTcRows, b0 = (int)item.x * kTcBearings;
+        if(tid == 0) { S.jmin = INT_MAX; S.jmax = INT_MIN; }
+        __syncthreads();
+        if(tid < kTcRows) {
+            const int r = r0 + tid;
+            int2 w = make_int2(1, 0);
+            float R = 0.0f;
+            if(r < nR) { w = win[r]; R = ranges[r]; }
+            S.elo[tid] = w.x; S.ehi[tid] = w.y; S.R[tid] = R;
+            if(w.x <= w.y) { atomicMin(&S.jmin, w.x); atomicMax(&S.jmax, w.y); }
+        }
+        if(tid < kTcBearings) S.theta[tid] = b0 + tid < nB ? bearings[b0 + tid] : 0.0f;
+        __syncthreads();
+        const int jmin = S.jmin, jmax = S.jmax;
+        const int2 kb = bb_tiles[item.x];
+        // This part's share [g_begin, g_end) of the tile's sample stream.
+        uint32_t g_begin = 0, g_end = 0xFFFFFFFFu;
+        if(item.w > 1) {
+            if(tid == 0) {
+                unsigned long long count = 0;
+                for(int j = jmin; j <= jmax; j++)
+                    count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
+                S.count = count;
+            }
+            __syncthreads();
+            g_begin = (uint32_t)(S.count * item.z / item.w);
+            g_end = (uint32_t)(S.count * (item.z + 1) / item.w);
+        }
+        uint32_t nchunk = 0, chain = 0, base = 0;
+        bool stop = false;
+#pragma unroll
+        for(int q = 0; q < 32; q++) acc[q] = 0.0f;
+        for(int jg = jmin; jg <= jmax && base < g_end && !stop; jg += kTcThreads) {
+            const int j = jg + tid;
+            uint32_t start = 0, len = 0;
+            if(j <= jmax) {
+                start = off[(size_t)j * nBB + kb.x];
+                len = off[(size_t)j * nBB + kb.y + 1] - start;
+            }
+            uint32_t x = len;
+            for(int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if(lane >= o) x += y;
+            }
+            if(lane == 31) S.warp_sums[warp] = x;
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+            for(int w = 0; w < kTcWarps; w++) {
+                const uint32_t v = S.warp_sums[w];
+                if(w < warp) before += v;
+                total += v;
+            }
+            S.seg_start[tid] = start;
+            S.seg_pre[tid] = before + x - len;
+            if(tid == 0) S.seg_pre[kTcThreads] = total;
+            __syncthreads();
+            const uint32_t lo = g_begin > base ? min(g_begin - base, total) : 0u;
+            const uint32_t hi = (g_end - base < total) ? g_end - base : total;
+            base += total;
+            // Stream position g of this group -> (sample, bin), for the 32
+            // loader threads.
+            auto fetch = [&](uint32_t c0, float4& smp, int& bin) {
+                const uint32_t g = c0 + (uint32_t)tid;
+                if(g < hi) {
+                    int a = 0, z = kTcThreads - 1;        // largest t with seg_pre[t] <= g
+                    while(a < z) {
+                        const int mid = (a + z + 1) >> 1;
+                        if(S.seg_pre[mid] <= g) a = mid; else z = mid - 1;
+                    }
+                    smp = sorted[S.seg_start[a] + (g - S.seg_pre[a])];
+                    bin = jg + a;
+                }
+                else {
+                    smp = make_float4(0.f, 0.f, 0.f, 0.f);
+                    bin = INT_MIN;
+                }
+            };
+            float4 nsmp = make_float4(0.f, 0.f, 0.f, 0.f);
+            int nbin = INT_MIN;
+            if(tid < kTcChunk && lo < hi) fetch(lo, nsmp, nbin);
+            for(uint32_t c0 = lo; c0 < hi; c0 += kTcChunk) {
+                const int valid = (int)min((uint32_t)kTcChunk, hi - c0);
+                const uint32_t st = gchunk & 1u;
+                if(tid < kTcChunk) { S.smp[tid] = nsmp; S.bin[tid] = nbin; }
+                // Stage st was last read by the MMAs of chunk gchunk - 2.
+                if(tid == 0 && gchunk >= 2 &&
+                   !mbar_wait_bounded(smem_u32(&S.bar[st]), ((gchunk >> 1) - 1) & 1u, &S.abort, kTcWaitCycles))
+                    atomicOr(err, kErrGatherTimeout);
+                __syncthreads();
+                if(S.abort) { stop = true; break; }
+                if(tid < kTcChunk && c0 + kTcChunk < hi) fetch(c0 + kTcChunk, nsmp, nbin);   // next chunk in flight
+                unsigned char* sa = stages + st * kTcStageBytes;
+                // A: warp w computes rows 4w .. 4w + 3 for sample k = lane.
+                {
+                    const int k = lane;
+                    const float4 sm = S.smp[k];
+                    const int bin = S.bin[k];
+#pragma unroll
+                    for(int q = 0; q < 4; q++) {
+                        const int rr = warp * 4 + q;
+                        float2 u = make_float2(0.f, 0.f);
+                        if(bin >= S.elo[rr] && bin <= S.ehi[rr]) {
+                            const float2 w = lerp_cplx(s_pulse, rp.range_axis, sm.z - S.R[rr]);
+                            u = cmul(make_float2(sm.x, sm.y), w);
+                        }
+                        uint32_t h, l;
+                        tf32_split(u.x, h, l);
+                        *reinterpret_cast<uint32_t*>(sa + sw128_offset_b32(rr, k)) = h;
+                        *reinterpret_cast<uint32_t*>(sa + kTcOpBytes + sw128_offset_b32(rr, k)) = l;
+                        tf32_split(u.y, h, l);
+                        *reinterpret_cast<uint32_t*>(sa + sw128_offset_b32(kTcRows + rr, k)) = h;
+                        *reinterpret_cast<uint32_t*>(sa + kTcOpBytes + sw128_offset_b32(kTcRows + rr, k)) = l;
+                    }
+                    // B: warp w computes bearings 8w .. 8w + 7 for sample k = lane.
+                    const bool live = k < valid;
+#pragma unroll
+                    for(int q = 0; q < 8; q++) {
+                        const int n = warp * 8 + q;
+                        float v = 0.0f;
+                        if(live && b0 + n < nB) v = lerp_real(s_beam, rp.beam_axis, sm.w - S.theta[n]);
+                        uint32_t h, l;
+                        tf32_split(v, h, l);
+                        *reinterpret_cast<uint32_t*>(sa + 2 * kTcOpBytes + sw128_offset_b32(n, k)) = h;
+                        *reinterpret_cast<uint32_t*>(sa + 3 * kTcOpBytes + sw128_offset_b32(n, k)) = l;
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncthreads();
+                if(tid == 0) {
+                    tc_fence_after();
+                    const uint32_t a = smem_u32(sa);
+                    const uint64_t ahi = smem_desc(a), alo = smem_desc(a + kTcOpBytes);
+                    const uint64_t bhi = smem_desc(a + 2 * kTcOpBytes), blo = smem_desc(a + 3 * kTcOpBytes);
+#pragma unroll
+                    for(int kk = 0; kk < kTcChunk / 8; kk++) {      // 32 bytes of K per MMA: +2 in descriptor units
+                        umma_tf32(tmem, ahi + 2 * kk, bhi + 2 * kk, (chain > 0 || kk > 0) ? 1u : 0u);
+                        umma_tf32(tmem, ahi + 2 * kk, blo + 2 * kk, 1u);
+                        umma_tf32(tmem, alo + 2 * kk, bhi + 2 * kk, 1u);
+                    }
+                    umma_commit(smem_u32(&S.bar[st]));
+                }
+                nchunk++;
+                gchunk++;
+                if(++chain == kTcFlush) {
+                    if(!flush()) { stop = true; break; }
+                    chain = 0;
+                }
+            }
+        }
+        if(stop) break;
+        if(nchunk == 0) continue;
+        if(chain > 0 && !flush()) break;
+        chain = 0;
+        // Epilogue: registers -> shared (rows of kTcPitch floats) -> the ping.
+        float* dsm = reinterpret_cast<float*>(stages);
+        {
+            const int m = quad * 32 + lane;
+#pragma unroll
+            for(int q = 0; q < 32; q++) dsm[m * kTcPitch + cg * 32 + q] = acc[q];
+        }
+        __syncthreads();
+        for(int e = tid; e < kTcRows * kTcBearings; e += kTcThreads) {
+            const int rr = e / kTcBearings, n = e % kTcBearings;
+            const int r = r0 + rr, b = b0 + n;
+            if(r < nR && b < nB)
+                red_add_v2(out + (size_t)r * nB + b, make_float2(dsm[rr * kTcPitch + n], dsm[(kTcRows + rr) * kTcPitch + n]));
+        }
+        __syncthreads();
+    }
+    // Let issued MMAs finish (bounded) before the TMEM is released.
+    if(tid == 0 && gchunk > 0 && S.abort) {
+        volatile int keep_waiting = 0;
+        mbar_wait_bounded(smem_u32(&S.bar[(gchunk - 1) & 1u]), ((gchunk - 1) >> 1) & 1u, &keep_waiting, kTcWaitCycles);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if(warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+    }
+}
+
+rtacx_status launch_2d_tc(Context& ctx, float2* out, cudaStream_t stream)
+{
+    const size_t smem = gather_tc_smem_bytes(ctx.H, ctx.W);
+    if(raise_smem_limit((const void*)k_gather_tc, smem) != cudaSuccess) {
+        cudaGetLastError();
+        ctx.error = "PSF tables too large for the tensor-core gather";
+        return RTACX_ERR_UNSUPPORTED;
+    }
+    const uint32_t tiles_b = (ctx.nB + kTcBearings - 1) / kTcBearings;
+    const uint32_t tiles = tiles_b * ((ctx.nR + kTcRows - 1) / kTcRows);
+    k_tile_parts<kTcRows><<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles128, ctx.nR,
+                                                                   ctx.bin.nBB, tiles_b, tiles, ctx.d_tile_parts);
+    scan_u32(ctx.d_tile_parts, tiles, ctx.d_tile_first, stream);   // d_tile_first[tiles] = item count
+    k_tile_items<<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_tile_parts, ctx.d_tile_first, tiles_b, tiles,
+                                                          ctx.d_items);
+    cudaError_t me = cudaMemsetAsync(ctx.d_item_counter, 0, sizeof(uint32_t), stream);
+    if(me == cudaSuccess) me = cudaMemsetAsync(out, 0, (size_t)ctx.nR * ctx.nB * sizeof(float2), stream);
+    if(me != cudaSuccess) {
+        cudaGetLastError();
+        ctx.error = std::string("clearing the tensor-core gather's ping: ") + cudaGetErrorString(me);
+        return RTACX_ERR_CUDA;
+    }
+    k_gather_tc<<<ctx.sm_count, kTcThreads, smem, stream>>>(
+        ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles128, ctx.d_ranges, ctx.d_bearings, ctx.d_pulse,
+        ctx.d_beam, ctx.red, ctx.bin.nBB, out, ctx.d_items, ctx.d_tile_first + tiles, ctx.d_item_counter, ctx.d_err);
+    const cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) { ctx.error = std::string("k_gather_tc: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
+    return RTACX_OK;
+}
+
 // Persistent batched gather: each CTA takes work items from a global counter
 // (one atomicAdd per item, no waiting) until the list is exhausted. Items are
 // 2D tiles {ping, tile_b, tile_r, 0} or 1D row groups {ping, group, 0, 1}.
@@ -818,6 +1177,7 @@ rtacx_status run_reduce(Context& ctx, float* out_f, cudaStream_t stream)
         if(e != cudaSuccess) { ctx.error = std::string("k_gather_tex: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
         return RTACX_OK;
     }
+    if(!(ctx.flags & RTACX_FLAG_SIMT_GATHER) && ctx.d_tile_parts) return launch_2d_tc(ctx, out, stream);
     if(ctx.range_tile == 32) return launch_2d<32, 128>(ctx, out, stream);
     if(ctx.bearing_tile == 128) return launch_2d<16, 128>(ctx, out, stream);
     return launch_2d<16, 64>(ctx, out, stream);

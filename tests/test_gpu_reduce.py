@@ -35,6 +35,30 @@ def test_reduce_matches_fp64_oracle(oracle, maker):
     assert err <= TOL, err
 
 
+@pytest.mark.parametrize("maker", [
+    lambda: wl.oculus_reference_2d(),
+    lambda: wl.oculus_2d(n_samples=1 << 18),
+    lambda: wl.oculus_2d(n_samples=1 << 14, n_bearings=100, n_ranges=300),
+    lambda: wl.precision_2d(n_samples=1 << 16, n_ranges=1024),
+    lambda: wl.stress_2d(n_samples=1 << 18, n_ranges=2048),
+])
+def test_tensor_core_gather_matches_simt_gather(oracle, maker):
+    """The default 2D gather forms the sample x PSF outer products on the
+    tensor cores (TF32 hi / lo operands, three products, FP32 accumulation);
+    RTACX_FLAG_SIMT_GATHER selects the FP32 CUDA-core gather. Both meet the
+    FP64 oracle's bar, and they agree to float round-off (their sums run in
+    different orders)."""
+    from rtac_simulation_gb300 import _lib
+    wk = maker()
+    tc = gpu_reduce(make_context(wk), wk.samples, wk.out_shape)
+    simt = gpu_reduce(make_context(wk, flags=_lib.RTACX_FLAG_SIMT_GATHER), wk.samples, wk.out_shape)
+    want = oracle.reduce(wk.samples, wk.sensor)
+    assert np.isfinite(tc).all()
+    assert rel_l2(tc, want) <= TOL, rel_l2(tc, want)
+    assert rel_l2(simt, want) <= TOL
+    assert rel_l2(tc, simt) <= 5e-6, rel_l2(tc, simt)
+
+
 def test_reduce_1d_literal_scaling(oracle):
     wk = wl.ea400_reference_1d()
     ctx = make_context(wk, flags=1)
