@@ -1,7 +1,9 @@
 """Contention stress ping (half of the samples in ~1% of the range bins):
-bit-exact bin counts, segments and windows at the full 2^27-sample size, and
-both forms against their FP64 oracles on a reduced copy with the same
-structure (the hot tiles are split across CTAs by the persistent gather)."""
+bit-exact bin counts, segments and windows at the full 2^27-sample size, the
+precision form against the FP64 oracle of its binned model on every row of
+the full ping, and both forms against their FP64 oracles on a reduced copy
+with the same structure (the hot tiles are split across CTAs by the
+persistent gather)."""
 import numpy as np
 import pytest
 
@@ -56,6 +58,22 @@ def test_stress_full_size_binning_bit_exact(oracle):
     # The cluster really is hot: half of the samples in about 1% of the bins.
     top = np.sort(counts)[::-1][: s["range_count"] // 100].sum()
     assert top > 0.45 * wk.n
+
+
+@pytest.mark.parametrize("hot", [False, True])
+def test_stress_full_size_precision_every_row(oracle, hot):
+    """2^27 samples, 1024 x 8192, the 271 MB grid larger than the L2, with
+    and without the hot-range replicas: every row against the binned FP64
+    oracle."""
+    from rtac_simulation_gb300 import _lib
+    wk = wl.stress_2d()
+    ctx = precision_context(wk, flags=_lib.RTACX_PRECISION_HOT_RANGE if hot else 0)
+    got = gpu_precision(ctx, wk.samples, wk.out_shape)
+    ctx.close()
+    tab = wl.precision_tables(wk.sensor, **wk.precision)
+    want = oracle.reduce_binned(oracle.apply_echo(wk.samples, wk.sensor, wk.echo), wk.sensor, tab)
+    assert np.isfinite(got).all()
+    assert rel_l2(got, want) <= 1e-4
 
 
 def test_stress_reduced_plain_matches_oracle(oracle):
