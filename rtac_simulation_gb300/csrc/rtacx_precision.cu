@@ -539,28 +539,32 @@ k_prec_split_f16(const float4* __restrict__ G, uint32_t rows, uint32_t cells, ui
     }
 }
 
-constexpr int kFiltRows = 64, kFiltCols = 64, kFiltTapsMax = 64, kFiltThreads = 256;
+constexpr int kFiltRows = 64, kFiltCols = 64, kFiltTapsMax = 64, kFiltThreads = 512;
 
 size_t filter_smem_bytes(uint32_t ntaps)
 {
     const size_t nt = std::min<uint32_t>(std::max<uint32_t>(ntaps, 1u), (uint32_t)kFiltTapsMax);
-    return (kFiltRows + nt - 1) * kFiltCols * sizeof(float2) + kFiltTapsMax * sizeof(float2) + kFiltRows * sizeof(int);
+    return (kFiltRows + nt - 1) * kFiltCols * sizeof(float2) + 2 * kFiltTapsMax * sizeof(float2) +
+           2 * kFiltRows * sizeof(int);
 }
 
 // Range filter on the contracted grid: out(r, b) = sum_t taps[r % 2][t]
 // C[r / 2 + t + 1][b] (C row j holds range node j - tap_center - 1), or 0
 // when row r's reference window is empty. One CTA per 64 node rows x 64
-// bearings x one output-row parity (blockIdx.z): output rows 2 m + parity.
-// Per chunk of up to 64 taps the C rows it needs are staged in shared memory
-// once, row-major: every warp first loads all of its rows (up to 16, two
-// 256-byte row segments each) and only then stores them, so the loads are in
-// flight together. Lane l owns columns l and l + 32; each warp filters 8 node
-// rows with a sliding window of eight staged rows per column in registers
-// (one shared load per tap and column).
-constexpr int kFiltRowsPerWarp = (kFiltRows + kFiltTapsMax - 1 + 7) / 8;
+// bearings, both output-row parities (warps 0-7 the even rows 2 m, warps
+// 8-15 the odd rows 2 m + 1, from the same staged node rows). Per chunk of
+// up to 64 taps the C rows it needs are staged in shared memory once,
+// row-major: every warp first loads all of its rows (up to 8, two 256-byte
+// row segments each, the GEMM's K partials added) and only then stores
+// them, so the loads are in flight together. Lane l owns columns l and
+// l + 32; each warp filters 8 node rows of its parity with a sliding window
+// of eight staged rows per column in registers (one shared load per tap and
+// column).
+constexpr int kFiltWarps = kFiltThreads / 32;
+constexpr int kFiltRowsPerWarp = (kFiltRows + kFiltTapsMax - 1 + kFiltWarps - 1) / kFiltWarps;
 
 template <int kParts>
-__global__ void __launch_bounds__(kFiltThreads, 2)
+__global__ void __launch_bounds__(kFiltThreads, 1)
 k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size_t part2,
               const uint32_t* __restrict__ nonempty, int ov, const float2* __restrict__ taps, uint32_t ntaps,
               uint32_t nR, uint32_t nB, float2* __restrict__ out)
@@ -568,13 +572,14 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int ntc = min((int)max(ntaps, 1u), kFiltTapsMax);
     float2* sG = reinterpret_cast<float2*>(s_raw);                    // [kFiltRows + ntc - 1][kFiltCols]
-    float2* sT = sG + (size_t)(kFiltRows + ntc - 1) * kFiltCols;       // [kFiltTapsMax]
-    int* sW = reinterpret_cast<int*>(sT + kFiltTapsMax);                // [kFiltRows]
+    float2* sT = sG + (size_t)(kFiltRows + ntc - 1) * kFiltCols;       // [2][kFiltTapsMax]
+    int* sW = reinterpret_cast<int*>(sT + 2 * kFiltTapsMax);            // [2][kFiltRows]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols, par = blockIdx.z;
-    taps += (size_t)par * ntaps;
-    if(tid < kFiltRows) {
-        const int r = 2 * (r0 + tid) + par;
+    const int par = warp >> 3, wl = warp & 7;                           // parity, warp within it
+    const int r0 = blockIdx.y * kFiltRows, k0 = blockIdx.x * kFiltCols;
+    if(tid < 2 * kFiltRows) {
+        const int p = tid / kFiltRows, m = tid % kFiltRows;
+        const int r = 2 * (r0 + m) + p;
         sW[tid] = r < (int)nR ? (row_has_window(nonempty, nR, ov, r) ? 1 : 0) : 0;
     }
     float2 acc[8][2];
@@ -585,11 +590,11 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size
         const int nt = min(ntc, (int)ntaps - tc);
         const int rows_s = kFiltRows + nt - 1;
         __syncthreads();
-        if(tid < nt) sT[tid] = taps[tc + tid];
+        if(tid < 2 * nt) sT[(tid / nt) * kFiltTapsMax + tid % nt] = taps[(size_t)(tid / nt) * ntaps + tc + tid % nt];
         float2 v[kFiltRowsPerWarp][2];
 #pragma unroll
         for(int i = 0; i < kFiltRowsPerWarp; i++) {
-            const int rr = warp + 8 * i;
+            const int rr = warp + kFiltWarps * i;
             const uint32_t j = (uint32_t)(r0 + tc + rr + 1);        // C row of staged row rr
             const bool live = rr < rows_s && j < c_rows;
             const float2* row = C + (size_t)(live ? j : 0) * ldc2;
@@ -609,16 +614,17 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size
         }
 #pragma unroll
         for(int i = 0; i < kFiltRowsPerWarp; i++) {
-            const int rr = warp + 8 * i;
+            const int rr = warp + kFiltWarps * i;
             if(rr < rows_s) {
                 sG[rr * kFiltCols + lane] = v[i][0];
                 sG[rr * kFiltCols + 32 + lane] = v[i][1];
             }
         }
         __syncthreads();
+        const float2* tp = sT + par * kFiltTapsMax;
 #pragma unroll
         for(int h = 0; h < 2; h++) {
-            const float2* col = sG + h * 32 + lane + warp * 8 * kFiltCols;
+            const float2* col = sG + h * 32 + lane + wl * 8 * kFiltCols;
             float2 g[8];
 #pragma unroll
             for(int i = 0; i < 7; i++) g[i] = col[i * kFiltCols];
@@ -631,7 +637,7 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size
 #pragma unroll
                 for(int i = 0; i < 8; i++) {
                     g[(i + 7) & 7] = col[(tt + i + 7) * kFiltCols];
-                    const float2 c = sT[tt + i];
+                    const float2 c = tp[tt + i];
 #pragma unroll
                     for(int q = 0; q < 8; q++) {
                         const float2 gq = g[(q + i) & 7];
@@ -642,7 +648,7 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size
             }
             for(; tt < nt; tt++) {
                 g[7] = col[(tt + 7) * kFiltCols];
-                const float2 c = sT[tt];
+                const float2 c = tp[tt];
 #pragma unroll
                 for(int q = 0; q < 8; q++) {
                     acc[q][h].x = fmaf(c.x, g[q].x, fmaf(-c.y, g[q].y, acc[q][h].x));
@@ -655,9 +661,9 @@ k_prec_filter(const float2* __restrict__ C, uint32_t ldc2, uint32_t c_rows, size
     }
 #pragma unroll
     for(int q = 0; q < 8; q++) {
-        const int r = 2 * (r0 + warp * 8 + q) + par;
+        const int r = 2 * (r0 + wl * 8 + q) + par;
         if(r >= (int)nR) continue;
-        const bool on = sW[warp * 8 + q] != 0;
+        const bool on = sW[par * kFiltRows + wl * 8 + q] != 0;
 #pragma unroll
         for(int h = 0; h < 2; h++) {
             const int k = k0 + 32 * h + lane;
@@ -1196,7 +1202,7 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
     if(st != RTACX_OK) return st;
     ctx.mark(3, true, stream);
     ctx.mark(2, false, stream);
-    const dim3 fgrid((nB + kFiltCols - 1) / kFiltCols, (range_nodes(nR) + kFiltRows - 1) / kFiltRows, 2);
+    const dim3 fgrid((nB + kFiltCols - 1) / kFiltCols, (range_nodes(nR) + kFiltRows - 1) / kFiltRows);
     auto filter = ctx.ksplit == 2 ? k_prec_filter<2> : k_prec_filter<1>;
     filter<<<fgrid, kFiltThreads, filter_smem_bytes(ctx.taps), stream>>>(
         reinterpret_cast<const float2*>(ctx.d_C), ctx.Npad / 2, ctx.grid_rows, (size_t)ctx.Mpad * ctx.Npad / 2,
