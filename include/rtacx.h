@@ -418,6 +418,17 @@ rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable);
  * ping is then incomplete and rtacx_stream_status returns RTACX_ERR_DEVICE.
  * The context stays usable: the next ping clears its grid. */
 rtacx_status rtacx_diag_drop_accumulation_stage(rtacx_ctx* ctx, uint32_t stage);
+
+/* Diagnostic (no counterpart in the reference): copies the first
+ * min(max_records, capacity) records of the context's sorted scratch, as
+ * left by the last rtacx_bin / rtacx_reduce queued on `stream`, into
+ * `records` (device or pinned host memory, 16 bytes per record): float4
+ * {re, im, travel, bearing} (bearing 0 for 1D sensors; the value after the
+ * echo model when one is set). The first n - (out-of-range count) records
+ * are the binned samples, each once, grouped by composite key (range bin x
+ * bearing sub-bins + bearing sub-bin) in ascending order, in any order
+ * inside a group. */
+rtacx_status rtacx_diag_sorted(rtacx_ctx* ctx, float* records, uint64_t max_records, void* stream);
 int rtacx_stage_times(rtacx_ctx* ctx, float* ms, int max);
 
 /* Diagnostic: synchronous C = A * B^T on the tensor cores (the GEMM of the

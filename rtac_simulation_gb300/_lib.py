@@ -73,6 +73,7 @@ SIGNATURES = {
     "rtacx_stream_status": (_I, [_P, _P]),
     "rtacx_set_tracing": (_I, [_P, _I]),
     "rtacx_diag_drop_accumulation_stage": (_I, [_P, _U32]),
+    "rtacx_diag_sorted": (_I, [_P, _P, _U64, _P]),
     "rtacx_stage_times": (_I, [_P, ctypes.POINTER(ctypes.c_float), _I]),
     "rtacx_reduce_noalloc": (_I, [_I, _P, _P, _U64, _P, _P]),
     "rtacx_gemm_bf16_tn": (_I, [_P, _P, _P, _I, _I, _I, _P]),
@@ -329,6 +330,11 @@ class Context:
         """Failure-path diagnostic: the staged accumulation skips one stage's
         copy (0xFFFFFFFF: none), so its CTA times out and flags the error word."""
         self._check(self._lib.rtacx_diag_drop_accumulation_stage(self._h, stage))
+
+    def diag_sorted(self, records, max_records: int, stream=None) -> None:
+        """Copies the sorted scratch of the last binning (float4 records
+        grouped by composite key) into `records`."""
+        self._check(self._lib.rtacx_diag_sorted(self._h, _ptr(records), max_records, _stream(stream)))
 
     def set_tracing(self, enable: bool) -> None:
         self._check(self._lib.rtacx_set_tracing(self._h, 1 if enable else 0))

@@ -524,6 +524,21 @@ rtacx_status rtacx_diag_drop_accumulation_stage(rtacx_ctx* ctx, uint32_t stage)
     return RTACX_OK;
 }
 
+rtacx_status rtacx_diag_sorted(rtacx_ctx* ctx, float* records, uint64_t max_records, void* stream)
+{
+    if(!ctx || (!records && max_records)) return RTACX_ERR_INVALID_ARGUMENT;
+    Context& c = ctx->impl;
+    if(set_device(c) != RTACX_OK) return RTACX_ERR_CUDA;
+    const uint64_t k = std::min(max_records, c.d_sorted ? c.capacity : 0);
+    if(k && cudaMemcpyAsync(records, c.d_sorted, k * sizeof(float4), cudaMemcpyDefault,
+                            static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+        cudaGetLastError();
+        c.error = "copying the sorted scratch failed";
+        return RTACX_ERR_CUDA;
+    }
+    return RTACX_OK;
+}
+
 rtacx_status rtacx_set_tracing(rtacx_ctx* ctx, int enable)
 {
     if(!ctx) return RTACX_ERR_INVALID_ARGUMENT;

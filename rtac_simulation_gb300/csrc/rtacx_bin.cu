@@ -17,11 +17,13 @@
 //                     bin offsets, and one shared write cursor per bin
 //                     initialised to its offset (k_binscan: the single-CTA
 //                     scan of the batched form and of the split gather).
-//   k_scatter_staged  re-reads the chunk in tiles of 12K records, sorts each
+//   k_scatter_pipe    re-reads the chunk in tiles of 7680 records, sorts each
 //                     tile by bin in shared memory, reserves one run per
 //                     (tile, bin) with a global atomicAdd on the bin's cursor
 //                     and writes the float4 {re, im, travel, bearing} records
-//                     of each run with consecutive lanes (k_scatter: the same
+//                     of each run with consecutive lanes, while the next
+//                     tile's loads are in flight (k_scatter_staged: the same
+//                     without the pipelining, for more bins; k_scatter: the
 //                     reservation without staging, when the per-bin tables do
 //                     not fit next to a tile, and in the batched form).
 //   k_windows         reference windows (do_make_bins, src/Binner.cu:82-106)
@@ -130,9 +132,8 @@ __global__ void k_scatter(const float* __restrict__ samples, uint64_t n, BinPara
 //            shared-memory slot;
 //   write    slot j goes to j + delta[key(j)] (the key recomputed from the
 //            record's travel and bearing, as in pass 1).
-// Shared memory: 16 B x NT U records + 8 B per bin. Shapes, in order of
-// preference: 1024 x 12 (one CTA per SM, longest runs), 512 x 10 (two CTAs
-// per SM), 1024 x 4.
+// Shared memory: 16 B x NT U records + 8 B per bin. Used as 1024 x 4 where
+// the bin tables leave no room for the pipelined scatter's tile.
 size_t staged_smem_bytes(int NT, int U, uint32_t nBins) { return (size_t)NT * U * sizeof(float4) + (size_t)nBins * 8; }
 
 template <int NT, int U>
@@ -332,6 +333,159 @@ bool ensure_capacity(Context& ctx, uint64_t n)
     return true;
 }
 
+namespace {
+
+// Pipelined staged scatter (single ping; one CTA of NT threads per SM). The
+// records of tile t are loaded into registers (U per thread) while the
+// sorted slots of tile t - 1 are written out from shared memory, so each SM
+// reads and writes HBM at the same time instead of in alternating phases,
+// and every record is read from memory once (it goes from its registers
+// straight into its sorted slot). Per tile:
+//   load     U records per thread into registers (tile t)
+//   write    sorted slot j of tile t - 1 -> j + delta[key(j)]
+//   rank     key of every record of tile t, rank among the tile's samples of
+//            the bin (shared histogram)
+//   reserve  block exclusive scan of the histogram = local run starts; one
+//            atomicAdd per non-empty (tile, bin) on the bin's shared cursor,
+//            up to kReserveBatch of them in flight per thread
+//   place    records -> sorted shared-memory slots (echo pre-step applied)
+// Shared memory: 16 B x NT U records + 8 B per bin.
+constexpr int kReserveBatch = 8;
+
+// Placement of one thread's records into their sorted shared-memory slots
+// (echo pre-step applied); rank kOutOfRange marks a skipped record.
+template <int U>
+__device__ __forceinline__ void place_records(const BinParams& p, const float4 (&rec)[U], const uint32_t (&rank)[U],
+                                              const uint32_t* s_start, float4* s_rec)
+{
+#pragma unroll
+    for(int u = 0; u < U; u++) {
+        if(rank[u] == kOutOfRange) continue;
+        float4 r = rec[u];
+        int side;
+        const uint32_t k = sample_key(p, r.z, r.w, side);
+        if(p.echo_flags) {
+            const float2 v = apply_echo(p, make_float2(r.x, r.y), r.z);
+            r.x = v.x; r.y = v.y;
+        }
+        s_rec[s_start[k] + rank[u]] = r;
+    }
+}
+
+template <int NT, int U>
+__global__ void __launch_bounds__(NT, 1)
+k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint32_t* __restrict__ cursor,
+               const uint32_t* __restrict__ offsets, float4* __restrict__ sorted, uint32_t* __restrict__ err)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ uint32_t s_warp[32];
+    const uint32_t nb = p.nBins;
+    float4* s_rec = reinterpret_cast<float4*>(s_raw);
+    uint32_t* s_start = reinterpret_cast<uint32_t*>(s_rec + NT * U);     // histogram, then local run starts
+    uint32_t* s_delta = s_start + nb;                                     // global base - local start
+    const uint32_t tid = threadIdx.x;
+    const uint32_t per = (nb + NT - 1) / NT, b0 = min(tid * per, nb), b1 = min(b0 + per, nb);
+    const uint32_t total = offsets[nb];
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t begin = (uint64_t)blockIdx.x * chunk, end = min(begin + chunk, n);
+    for(uint32_t b = b0; b < b1; b++) s_start[b] = 0u;
+    uint32_t prev = 0;                       // sorted slots of the previous tile
+    for(uint64_t t0 = begin;; t0 += (uint64_t)NT * U) {
+        const bool more = t0 < end;
+        float4 rec[U];
+        if(more) {
+#pragma unroll
+            for(int u = 0; u < U; u++) {
+                const uint64_t i = t0 + (uint64_t)u * NT + tid;
+                rec[u] = i < end ? load_record(samples, i, p) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        for(uint32_t j = tid; j < prev; j += NT) {
+            const float4 r = s_rec[j];
+            int side;
+            const uint32_t pos = j + s_delta[sample_key(p, r.z, r.w, side)];
+            if(pos < total) sorted[pos] = r;
+            else atomicOr(err, kErrScatterOverflow);
+        }
+        if(!more) break;
+        __syncthreads();                     // slots and deltas of tile t - 1 consumed, histogram zeroed
+        uint32_t rank[U];
+#pragma unroll
+        for(int u = 0; u < U; u++) {
+            int side;
+            const bool in = t0 + (uint64_t)u * NT + tid < end;
+            const uint32_t k = in ? sample_key(p, rec[u].z, rec[u].w, side) : kOutOfRange;
+            rank[u] = k != kOutOfRange ? atomicAdd(&s_start[k], 1u) : kOutOfRange;
+        }
+        __syncthreads();
+        uint32_t sum = 0;
+        for(uint32_t b = b0; b < b1; b++) sum += s_start[b];
+        uint32_t tile_total;
+        uint32_t run = block_exclusive_scan(sum, s_warp, tile_total);
+        if(per <= (uint32_t)kReserveBatch) {
+            // The thread's bins in one batch: local run starts now, the
+            // cursor reservations in flight during the placement, the deltas
+            // after it.
+            uint32_t c[kReserveBatch], base[kReserveBatch], start[kReserveBatch];
+#pragma unroll
+            for(int q = 0; q < kReserveBatch; q++) {
+                c[q] = b0 + q < b1 ? s_start[b0 + q] : 0u;
+                start[q] = run;
+                run += c[q];
+            }
+#pragma unroll
+            for(int q = 0; q < kReserveBatch; q++)
+                base[q] = c[q] ? atomicAdd(&cursor[(size_t)(b0 + q) * kCursorStride], c[q]) : 0u;
+#pragma unroll
+            for(int q = 0; q < kReserveBatch; q++)
+                if(b0 + q < b1) s_start[b0 + q] = start[q];
+            __syncthreads();
+            place_records<U>(p, rec, rank, s_start, s_rec);
+#pragma unroll
+            for(int q = 0; q < kReserveBatch; q++)
+                if(c[q]) s_delta[b0 + q] = base[q] - start[q];
+        }
+        else {
+            for(uint32_t g = b0; g < b1; g += kReserveBatch) {
+                uint32_t c[kReserveBatch], base[kReserveBatch];
+#pragma unroll
+                for(int q = 0; q < kReserveBatch; q++) c[q] = g + q < b1 ? s_start[g + q] : 0u;
+#pragma unroll
+                for(int q = 0; q < kReserveBatch; q++)
+                    base[q] = c[q] ? atomicAdd(&cursor[(size_t)(g + q) * kCursorStride], c[q]) : 0u;
+#pragma unroll
+                for(int q = 0; q < kReserveBatch; q++) {
+                    if(g + q < b1) {
+                        s_start[g + q] = run;
+                        if(c[q]) s_delta[g + q] = base[q] - run;
+                        run += c[q];
+                    }
+                }
+            }
+            __syncthreads();
+            place_records<U>(p, rec, rank, s_start, s_rec);
+        }
+        __syncthreads();
+        for(uint32_t b = b0; b < b1; b++) s_start[b] = 0u;   // the next rank follows a barrier
+        prev = tile_total;
+    }
+}
+
+using ScatterFn = void (*)(const float*, uint64_t, BinParams, uint32_t*, const uint32_t*, float4*, uint32_t*);
+struct ScatterShape {
+    ScatterFn fn;
+    int nt, u;
+};
+// In order of preference: pipelined 768 x 10 (bins up to ~13K), unpipelined
+// 1024 x 4 (up to ~20K); more bins take the per-tile k_scatter.
+const ScatterShape kScatterShapes[] = {
+    {k_scatter_pipe<768, 10>, 768, 10},
+    {k_scatter_staged<1024, 4>, 1024, 4},
+};
+constexpr int kNumScatterShapes = sizeof(kScatterShapes) / sizeof(kScatterShapes[0]);
+
+} // namespace
+
 void configure_hist_launch(Context& ctx);
 
 rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStream_t stream)
@@ -359,15 +513,11 @@ rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStre
         RTACX_CUDA(cudaGetLastError());
         ctx.mark(2, true, stream);
         ctx.mark(3, false, stream);
-        if(ctx.staged_U) {
-            const int NT = ctx.staged_U == 10 ? 512 : 1024;
-            const uint32_t g = hist_grid((uint32_t)ctx.sm_count * (NT == 512 ? 2u : 1u), n);
-            const size_t ss = staged_smem_bytes(NT, ctx.staged_U, p.nBins);
-            switch(ctx.staged_U) {
-            case 10: k_scatter_staged<512, 10><<<g, 512, ss, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets, ctx.d_sorted, ctx.d_err); break;
-            case 12: k_scatter_staged<1024, 12><<<g, 1024, ss, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets, ctx.d_sorted, ctx.d_err); break;
-            default: k_scatter_staged<1024, 4><<<g, 1024, ss, stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets, ctx.d_sorted, ctx.d_err); break;
-            }
+        if(ctx.scatter_shape) {
+            const ScatterShape& sh = kScatterShapes[ctx.scatter_shape - 1];
+            const uint32_t g = hist_grid((uint32_t)ctx.sm_count, n);
+            sh.fn<<<g, sh.nt, staged_smem_bytes(sh.nt, sh.u, p.nBins), stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets,
+                                                                              ctx.d_sorted, ctx.d_err);
         }
         else {
             k_scatter<<<hist_grid(ctx.scatter_ctas, n), ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist,
@@ -462,21 +612,18 @@ void configure_hist_launch(Context& ctx)
     };
     ctx.hist_ctas = resident((const void*)k_count);
     ctx.scatter_ctas = resident((const void*)k_scatter);
-    // Staged scatter: the longest runs first (one 1024 x 12 CTA per SM), then
-    // two 512 x 10 CTAs per SM, then 1024 x 4.
-    ctx.staged_U = 0;
+    // Staged scatter: the first shape of kScatterShapes whose shared memory
+    // fits.
+    ctx.scatter_shape = 0;
     int optin = 0, smem_sm = 0;
     if(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device) != cudaSuccess) optin = 0;
     if(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx.device) != cudaSuccess) smem_sm = 0;
-    const int cand_nt[3] = {1024, 512, 1024}, cand_u[3] = {12, 10, 4};   // 1024 x 12 measured fastest
-    const void* fns[3] = {(const void*)k_scatter_staged<1024, 12>, (const void*)k_scatter_staged<512, 10>,
-                          (const void*)k_scatter_staged<1024, 4>};
-    for(int c = 0; c < 3 && !ctx.staged_U; c++) {
-        const size_t need = staged_smem_bytes(cand_nt[c], cand_u[c], ctx.bin.nBins);
-        const size_t resident = cand_nt[c] == 512 ? 2 * (need + 1024) : need + 1024;
-        if(need + 1024 <= (size_t)optin && resident <= (size_t)smem_sm &&
-           raise_smem_limit(fns[c], need) == cudaSuccess)
-            ctx.staged_U = cand_u[c];
+    for(int c = 0; c < kNumScatterShapes && !ctx.scatter_shape; c++) {
+        const ScatterShape& sh = kScatterShapes[c];
+        const size_t need = staged_smem_bytes(sh.nt, sh.u, ctx.bin.nBins);
+        if(need + 1024 <= (size_t)optin && need + 1024 <= (size_t)smem_sm &&
+           raise_smem_limit((const void*)sh.fn, need) == cudaSuccess)
+            ctx.scatter_shape = c + 1;
     }
     cudaGetLastError();
 }

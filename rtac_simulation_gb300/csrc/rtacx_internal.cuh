@@ -373,7 +373,7 @@ struct Context {
     float4* d_sorted = nullptr;
     uint32_t hist_ctas = 0;             // CTAs of the count pass (and of the batched passes)
     uint32_t scatter_ctas = 0;          // CTAs of the scatter pass
-    int staged_U = 0;                   // records per thread of the staged scatter (0: per-tile scatter)
+    int scatter_shape = 0;              // 1 + index of the staged scatter's shape (0: per-tile scatter)
     size_t acc_smem = 0;                // dynamic shared memory of the precision accumulation
     uint32_t acc_blocks_per_sm = 1;
     uint32_t hist_threads = 0;
