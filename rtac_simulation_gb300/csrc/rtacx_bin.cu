@@ -347,14 +347,18 @@ namespace {
 //            the bin (shared histogram)
 //   reserve  block exclusive scan of the histogram = local run starts; one
 //            atomicAdd per non-empty (tile, bin) on the bin's shared cursor,
-//            up to kReserveBatch of them in flight per thread
-//   place    records -> sorted shared-memory slots (echo pre-step applied)
+//            up to kReserveBatch of them in flight per thread; with at most
+//            kReserveBatch bins per thread (ONE_BATCH) they stay in flight
+//            during the placement
+//   place    records -> sorted shared-memory slots (echo pre-step applied;
+//            instantiated with and without it, which keeps the echo-free
+//            form's registers below the launch bound)
 // Shared memory: 16 B x NT U records + 8 B per bin.
 constexpr int kReserveBatch = 8;
 
 // Placement of one thread's records into their sorted shared-memory slots
-// (echo pre-step applied); rank kOutOfRange marks a skipped record.
-template <int U>
+// (echo pre-step applied when ECHO); rank kOutOfRange marks a skipped record.
+template <int U, bool ECHO>
 __device__ __forceinline__ void place_records(const BinParams& p, const float4 (&rec)[U], const uint32_t (&rank)[U],
                                               const uint32_t* s_start, float4* s_rec)
 {
@@ -364,7 +368,7 @@ __device__ __forceinline__ void place_records(const BinParams& p, const float4 (
         float4 r = rec[u];
         int side;
         const uint32_t k = sample_key(p, r.z, r.w, side);
-        if(p.echo_flags) {
+        if(ECHO) {
             const float2 v = apply_echo(p, make_float2(r.x, r.y), r.z);
             r.x = v.x; r.y = v.y;
         }
@@ -372,7 +376,7 @@ __device__ __forceinline__ void place_records(const BinParams& p, const float4 (
     }
 }
 
-template <int NT, int U>
+template <int NT, int U, bool ECHO, bool ONE_BATCH>
 __global__ void __launch_bounds__(NT, 1)
 k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint32_t* __restrict__ cursor,
                const uint32_t* __restrict__ offsets, float4* __restrict__ sorted, uint32_t* __restrict__ err)
@@ -422,28 +426,24 @@ k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint3
         for(uint32_t b = b0; b < b1; b++) sum += s_start[b];
         uint32_t tile_total;
         uint32_t run = block_exclusive_scan(sum, s_warp, tile_total);
-        if(per <= (uint32_t)kReserveBatch) {
-            // The thread's bins in one batch: local run starts now, the
-            // cursor reservations in flight during the placement, the deltas
-            // after it.
-            uint32_t c[kReserveBatch], base[kReserveBatch], start[kReserveBatch];
+        if(ONE_BATCH) {
+            // The thread's bins (at most kReserveBatch) in one batch: local
+            // run starts now, the cursor reservations in flight during the
+            // placement, the deltas after it.
+            uint32_t base[kReserveBatch], nonempty = 0;
 #pragma unroll
             for(int q = 0; q < kReserveBatch; q++) {
-                c[q] = b0 + q < b1 ? s_start[b0 + q] : 0u;
-                start[q] = run;
-                run += c[q];
+                const uint32_t c = b0 + q < b1 ? s_start[b0 + q] : 0u;
+                base[q] = c ? atomicAdd(&cursor[(size_t)(b0 + q) * kCursorStride], c) : 0u;
+                if(c) nonempty |= 1u << q;
+                if(b0 + q < b1) s_start[b0 + q] = run;
+                run += c;
             }
-#pragma unroll
-            for(int q = 0; q < kReserveBatch; q++)
-                base[q] = c[q] ? atomicAdd(&cursor[(size_t)(b0 + q) * kCursorStride], c[q]) : 0u;
-#pragma unroll
-            for(int q = 0; q < kReserveBatch; q++)
-                if(b0 + q < b1) s_start[b0 + q] = start[q];
             __syncthreads();
-            place_records<U>(p, rec, rank, s_start, s_rec);
+            place_records<U, ECHO>(p, rec, rank, s_start, s_rec);
 #pragma unroll
             for(int q = 0; q < kReserveBatch; q++)
-                if(c[q]) s_delta[b0 + q] = base[q] - start[q];
+                if(nonempty & (1u << q)) s_delta[b0 + q] = base[q] - s_start[b0 + q];
         }
         else {
             for(uint32_t g = b0; g < b1; g += kReserveBatch) {
@@ -463,7 +463,7 @@ k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint3
                 }
             }
             __syncthreads();
-            place_records<U>(p, rec, rank, s_start, s_rec);
+            place_records<U, ECHO>(p, rec, rank, s_start, s_rec);
         }
         __syncthreads();
         for(uint32_t b = b0; b < b1; b++) s_start[b] = 0u;   // the next rank follows a barrier
@@ -473,14 +473,16 @@ k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint3
 
 using ScatterFn = void (*)(const float*, uint64_t, BinParams, uint32_t*, const uint32_t*, float4*, uint32_t*);
 struct ScatterShape {
-    ScatterFn fn;
+    ScatterFn fn[2][2];         // [echo pre-step][one reservation batch per thread]
     int nt, u;
 };
 // In order of preference: pipelined 768 x 10 (bins up to ~13K), unpipelined
 // 1024 x 4 (up to ~20K); more bins take the per-tile k_scatter.
 const ScatterShape kScatterShapes[] = {
-    {k_scatter_pipe<768, 10>, 768, 10},
-    {k_scatter_staged<1024, 4>, 1024, 4},
+    {{{k_scatter_pipe<768, 10, false, false>, k_scatter_pipe<768, 10, false, true>},
+      {k_scatter_pipe<768, 10, true, false>, k_scatter_pipe<768, 10, true, true>}}, 768, 10},
+    {{{k_scatter_staged<1024, 4>, k_scatter_staged<1024, 4>}, {k_scatter_staged<1024, 4>, k_scatter_staged<1024, 4>}},
+     1024, 4},
 };
 constexpr int kNumScatterShapes = sizeof(kScatterShapes) / sizeof(kScatterShapes[0]);
 
@@ -516,8 +518,10 @@ rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStre
         if(ctx.scatter_shape) {
             const ScatterShape& sh = kScatterShapes[ctx.scatter_shape - 1];
             const uint32_t g = hist_grid((uint32_t)ctx.sm_count, n);
-            sh.fn<<<g, sh.nt, staged_smem_bytes(sh.nt, sh.u, p.nBins), stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets,
-                                                                              ctx.d_sorted, ctx.d_err);
+            const bool one_batch = (p.nBins + sh.nt - 1) / sh.nt <= (uint32_t)kReserveBatch;
+            const ScatterFn fn = sh.fn[p.echo_flags ? 1 : 0][one_batch ? 1 : 0];
+            fn<<<g, sh.nt, staged_smem_bytes(sh.nt, sh.u, p.nBins), stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets,
+                                                                           ctx.d_sorted, ctx.d_err);
         }
         else {
             k_scatter<<<hist_grid(ctx.scatter_ctas, n), ctx.hist_threads, smem, stream>>>(s, n, p, ctx.d_hist,
@@ -621,9 +625,10 @@ void configure_hist_launch(Context& ctx)
     for(int c = 0; c < kNumScatterShapes && !ctx.scatter_shape; c++) {
         const ScatterShape& sh = kScatterShapes[c];
         const size_t need = staged_smem_bytes(sh.nt, sh.u, ctx.bin.nBins);
-        if(need + 1024 <= (size_t)optin && need + 1024 <= (size_t)smem_sm &&
-           raise_smem_limit((const void*)sh.fn, need) == cudaSuccess)
-            ctx.scatter_shape = c + 1;
+        bool ok = need + 1024 <= (size_t)optin && need + 1024 <= (size_t)smem_sm;
+        for(int e = 0; e < 2 && ok; e++)
+            for(int b = 0; b < 2 && ok; b++) ok = raise_smem_limit((const void*)sh.fn[e][b], need) == cudaSuccess;
+        if(ok) ctx.scatter_shape = c + 1;
     }
     cudaGetLastError();
 }
