@@ -84,7 +84,7 @@ __device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins,
         for(uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
             const uint32_t o = s_seg[scan_pad(i)];
             offsets[s0 + i] = o;
-            if(cursor) cursor[(size_t)(s0 + i) * kCursorStride] = o;
+            if(cursor) cursor[cursor_word(s0 + i)] = o;
         }
         carry += seg_total;
         __syncthreads();
@@ -176,7 +176,7 @@ k_scatter_staged(const float* __restrict__ samples, uint64_t n, BinParams p, uin
         for(uint32_t b = b0; b < b1; b++) {
             const uint32_t c = s_start[b];
             s_start[b] = run;
-            if(c) s_delta[b] = atomicAdd(&cursor[(size_t)b * kCursorStride], c) - run;
+            if(c) s_delta[b] = atomicAdd(&cursor[cursor_word(b)], c) - run;
             run += c;
         }
         __syncthreads();
@@ -346,8 +346,9 @@ namespace {
 //   rank     key of every record of tile t, rank among the tile's samples of
 //            the bin (shared histogram)
 //   reserve  block exclusive scan of the histogram = local run starts; one
-//            atomicAdd per non-empty (tile, bin) on the bin's shared cursor,
-//            up to kReserveBatch of them in flight per thread; with at most
+//            64-bit atomicAdd per (tile, pair of bins) with a non-empty bin on
+//            the pair's shared cursor word, up to kReserveBatch / 2 of them in
+//            flight per thread; with at most
 //            kReserveBatch bins per thread (ONE_BATCH) they stay in flight
 //            during the placement
 //   place    records -> sorted shared-memory slots (echo pre-step applied;
@@ -355,6 +356,22 @@ namespace {
 //            form's registers below the launch bound)
 // Shared memory: 16 B x NT U records + 8 B per bin.
 constexpr int kReserveBatch = 8;
+
+// Bins per thread of the pipelined scatter's reservation: even, so that each
+// thread's bins start a cursor pair.
+__host__ __device__ __forceinline__ uint32_t pipe_bins_per_thread(uint32_t nb, uint32_t nt)
+{
+    return ((nb + nt - 1) / nt + 1u) & ~1u;
+}
+
+// Reserves c0 slots in even bin b and c1 in bin b + 1 with one 64-bit atomic
+// on their shared cursor word; returns the old cursors (low: b, high: b + 1).
+__device__ __forceinline__ unsigned long long reserve_pair(uint32_t* cursor, uint32_t b, uint32_t c0, uint32_t c1)
+{
+    if(!(c0 | c1)) return 0ull;
+    return atomicAdd(reinterpret_cast<unsigned long long*>(cursor + cursor_word(b)),
+                     (unsigned long long)c1 << 32 | c0);
+}
 
 // Placement of one thread's records into their sorted shared-memory slots
 // (echo pre-step applied when ECHO); rank kOutOfRange marks a skipped record.
@@ -388,7 +405,7 @@ k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint3
     uint32_t* s_start = reinterpret_cast<uint32_t*>(s_rec + NT * U);     // histogram, then local run starts
     uint32_t* s_delta = s_start + nb;                                     // global base - local start
     const uint32_t tid = threadIdx.x;
-    const uint32_t per = (nb + NT - 1) / NT, b0 = min(tid * per, nb), b1 = min(b0 + per, nb);
+    const uint32_t per = pipe_bins_per_thread(nb, NT), b0 = min(tid * per, nb), b1 = min(b0 + per, nb);
     const uint32_t total = offsets[nb];
     const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
     const uint64_t begin = (uint64_t)blockIdx.x * chunk, end = min(begin + chunk, n);
@@ -432,12 +449,16 @@ k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint3
             // placement, the deltas after it.
             uint32_t base[kReserveBatch], nonempty = 0;
 #pragma unroll
-            for(int q = 0; q < kReserveBatch; q++) {
-                const uint32_t c = b0 + q < b1 ? s_start[b0 + q] : 0u;
-                base[q] = c ? atomicAdd(&cursor[(size_t)(b0 + q) * kCursorStride], c) : 0u;
-                if(c) nonempty |= 1u << q;
-                if(b0 + q < b1) s_start[b0 + q] = run;
-                run += c;
+            for(int q = 0; q < kReserveBatch; q += 2) {
+                const uint32_t b = b0 + q;
+                const uint32_t c0 = b < b1 ? s_start[b] : 0u, c1 = b + 1 < b1 ? s_start[b + 1] : 0u;
+                const unsigned long long old = reserve_pair(cursor, b, c0, c1);
+                base[q] = (uint32_t)old;
+                base[q + 1] = (uint32_t)(old >> 32);
+                nonempty |= (c0 ? 1u : 0u) << q | (c1 ? 1u : 0u) << (q + 1);
+                if(b < b1) s_start[b] = run;
+                if(b + 1 < b1) s_start[b + 1] = run + c0;
+                run += c0 + c1;
             }
             __syncthreads();
             place_records<U, ECHO>(p, rec, rank, s_start, s_rec);
@@ -447,17 +468,17 @@ k_scatter_pipe(const float* __restrict__ samples, uint64_t n, BinParams p, uint3
         }
         else {
             for(uint32_t g = b0; g < b1; g += kReserveBatch) {
-                uint32_t c[kReserveBatch], base[kReserveBatch];
+                uint32_t c[kReserveBatch];
+                unsigned long long old[kReserveBatch / 2];
 #pragma unroll
                 for(int q = 0; q < kReserveBatch; q++) c[q] = g + q < b1 ? s_start[g + q] : 0u;
 #pragma unroll
-                for(int q = 0; q < kReserveBatch; q++)
-                    base[q] = c[q] ? atomicAdd(&cursor[(size_t)(g + q) * kCursorStride], c[q]) : 0u;
+                for(int q = 0; q < kReserveBatch; q += 2) old[q / 2] = reserve_pair(cursor, g + q, c[q], c[q + 1]);
 #pragma unroll
                 for(int q = 0; q < kReserveBatch; q++) {
                     if(g + q < b1) {
                         s_start[g + q] = run;
-                        if(c[q]) s_delta[g + q] = base[q] - run;
+                        if(c[q]) s_delta[g + q] = (uint32_t)(old[q / 2] >> (32 * (q & 1))) - run;
                         run += c[q];
                     }
                 }
@@ -518,7 +539,7 @@ rtacx_status run_binning(Context& ctx, const void* samples, uint64_t n, cudaStre
         if(ctx.scatter_shape) {
             const ScatterShape& sh = kScatterShapes[ctx.scatter_shape - 1];
             const uint32_t g = hist_grid((uint32_t)ctx.sm_count, n);
-            const bool one_batch = (p.nBins + sh.nt - 1) / sh.nt <= (uint32_t)kReserveBatch;
+            const bool one_batch = pipe_bins_per_thread(p.nBins, sh.nt) <= (uint32_t)kReserveBatch;
             const ScatterFn fn = sh.fn[p.echo_flags ? 1 : 0][one_batch ? 1 : 0];
             fn<<<g, sh.nt, staged_smem_bytes(sh.nt, sh.u, p.nBins), stream>>>(s, n, p, ctx.d_hist, ctx.d_offsets,
                                                                            ctx.d_sorted, ctx.d_err);

@@ -155,7 +155,7 @@ __device__ __forceinline__ void scatter_chunk(const float* __restrict__ samples,
         __syncthreads();
 #pragma unroll
         for(int u = 0; u < kTileLoads; u++)
-            if(rank[u] == 0u) sh[key[u]] = atomicAdd(&cursor[(size_t)key[u] * kCursorStride], sh[key[u]]);
+            if(rank[u] == 0u) sh[key[u]] = atomicAdd(&cursor[cursor_word(key[u])], sh[key[u]]);
         __syncthreads();
 #pragma unroll
         for(int u = 0; u < kTileLoads; u++) {
@@ -254,7 +254,7 @@ __device__ __forceinline__ void scan_bin_block(const uint32_t* __restrict__ tota
         if(b >= nBins) break;
         const uint32_t v = totals[b];
         offsets[b] = o;
-        cursor[(size_t)b * kCursorStride] = o;
+        cursor[cursor_word(b)] = o;
         o += v;
         if(b == nBins - 1) offsets[nBins] = o;
     }
@@ -307,7 +307,7 @@ __device__ __forceinline__ void scatter_chunk_global(const float* __restrict__ s
 #pragma unroll
         for(int u = 0; u < kTileLoads; u++) {
             if(!valid[u] || key[u] == kOutOfRange) continue;
-            const uint32_t pos = atomicAdd(&cursor[(size_t)key[u] * kCursorStride], 1u);
+            const uint32_t pos = atomicAdd(&cursor[cursor_word(key[u])], 1u);
             float4 out = rec[u];
             if(p.echo_flags) {
                 const float2 v = apply_echo(p, make_float2(out.x, out.y), out.z);

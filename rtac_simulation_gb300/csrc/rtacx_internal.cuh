@@ -12,10 +12,16 @@
 
 namespace rtacx {
 
-// Words between two bins' write cursors: one 128-byte L2 line per bin, so the
-// scatter's run reservations spread over all L2 slices.
+// Words between two pairs of bins' write cursors: the cursors of bins 2i and
+// 2i + 1 share one 8-byte word (low and high half) at the start of a 128-byte
+// L2 line, so one 64-bit atomicAdd reserves runs in both bins (positions stay
+// below 2^32, so the low half never carries into the high half) and the
+// reservations spread over all L2 slices.
 constexpr uint32_t kCursorStride = 32;
 constexpr uint32_t kScanBlock = 1024;     // bins per block of the parallel bin scan
+
+// Word index of bin b's write cursor (see kCursorStride).
+__host__ __device__ __forceinline__ size_t cursor_word(uint32_t b) { return (size_t)(b >> 1) * kCursorStride + (b & 1u); }
 constexpr uint32_t kOutOfRange = RTACX_KEY_OUT_OF_RANGE;
 
 // Device error word bits (OR-ed by kernels, read by rtacx_stream_status).
@@ -378,7 +384,7 @@ struct Context {
     uint32_t acc_blocks_per_sm = 1;
     uint32_t hist_threads = 0;
     size_t hist_cols = 0;               // allocated words of d_hist (the write cursors)
-    uint32_t* d_hist = nullptr;         // [nBins][kCursorStride]: the scatter's per-bin write cursors
+    uint32_t* d_hist = nullptr;         // the scatter's per-bin write cursors (cursor_word), nBins x kCursorStride words
 
     // Split persistent gather of 2D pings (see rtacx_reduce.cu).
     uint32_t* d_tile_parts = nullptr;   // [tiles] parts per output tile
