@@ -53,7 +53,7 @@ DEFAULT_CONFIG = "precision_2d"
 NCU_TRAFFIC_BYTES = {
     "k_prec_accumulate_staged": 335.831e6 + 4.377e6,
     "k_gemm_tn": 78.715e6 + 4.004e6,
-    "sort_bin": (268.531e6 + 3.186e6) + (274.855e6 + 223.261e6),   # k_count + k_scatter_staged
+    "sort_bin": (268.531e6 + 3.186e6) + (273.130e6 + 220.672e6),   # k_count + k_scatter_pipe
 }
 # The accumulation's bound is the L2's reduction throughput, not HBM: ncu on
 # the default workload (profiles/k_prec_accumulate_staged_precision_2d.md)
