@@ -15,8 +15,8 @@
 //                     block sums; out-of-range counts.
 //   k_binscan_blocks  one CTA per 1024 bins: exclusive scan of the totals ->
 //                     bin offsets, and one shared write cursor per bin
-//                     initialised to its offset (k_binscan: the single-CTA
-//                     scan of the batched form and of the split gather).
+//                     initialised to its offset (binscan_cta: the
+//                     single-CTA scan of the staged batched form).
 //   k_scatter_pipe    re-reads the chunk in tiles of 7680 records, sorts each
 //                     tile by bin in shared memory, reserves one run per
 //                     (tile, bin) with a global atomicAdd on the bin's cursor
@@ -90,12 +90,6 @@ __device__ void binscan_cta(const uint32_t* __restrict__ totals, uint32_t nBins,
         __syncthreads();
     }
     if(threadIdx.x == 0) offsets[nBins] = carry;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_binscan(const uint32_t* __restrict__ totals, uint32_t nBins,
-                                                           uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursor)
-{
-    binscan_cta(totals, nBins, offsets, cursor);
 }
 
 // Parallel exclusive scan of the bin totals: CTA i scans bins
@@ -607,12 +601,6 @@ rtacx_status launch_bin_batch(std::string& error, const PingDev* pings, uint32_t
     const cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) { error = std::string("batched binning: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;
-}
-
-// Exclusive scan of n u32 values into out[0, n] (out[n] = total), one CTA.
-void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t stream)
-{
-    k_binscan<<<1, kScanThreads, 0, stream>>>(in, n, out, nullptr);
 }
 
 // Launch shape of the count / scatter passes for the configured bin count.

@@ -387,7 +387,7 @@ struct Context {
     uint32_t* d_hist = nullptr;         // the scatter's per-bin write cursors (cursor_word), nBins x kCursorStride words
 
     // Split persistent gather of 2D pings (see rtacx_reduce.cu).
-    uint32_t* d_tile_parts = nullptr;   // [tiles] parts per output tile
+    uint32_t* d_tile_parts = nullptr;   // [tiles] sample-stream length of each output tile
     uint32_t* d_tile_first = nullptr;   // [tiles + 1] first item of each tile; [tiles] = item count
     uint4* d_items = nullptr;           // [tiles * 256] work items
     uint32_t* d_item_counter = nullptr; // work-queue counter
@@ -466,7 +466,6 @@ rtacx_status run_bin_outputs(Context& ctx, const void* samples, uint64_t n,
                              uint32_t* keys, uint32_t* segments, uint32_t* windows,
                              uint32_t* counts, uint64_t* oor, cudaStream_t stream);
 bool ensure_capacity(Context& ctx, uint64_t n);
-void scan_u32(const uint32_t* in, uint32_t n, uint32_t* out, cudaStream_t stream);
 
 // Sparse PSF reduction (rtacx_reduce.cu).
 rtacx_status run_reduce(Context& ctx, float* out, cudaStream_t stream);

@@ -370,44 +370,73 @@ k_gather_tex_1d(const float4* __restrict__ sorted, const uint32_t* __restrict__ 
 }
 
 // ---- split persistent gather of one 2D ping -------------------------------
-// k_tile_parts counts each output tile's sample stream (same definition as
-// gather_tile_2d) and splits it into parts of at most kPartSamples samples
-// (at most kMaxParts); k_tile_items writes one work item per part; the
+// k_tile_plan (one CTA) counts each output tile's sample stream (same
+// definition as gather_tile_2d), picks the part size so that the ping yields
+// about kItemsPerWorker work items per persistent CTA (between
+// kMinPartSamples and kPartSamples samples per part, at most kMaxParts parts
+// per tile), scans the part counts and writes one work item per part; the
 // persistent kernel reduces the parts, accumulating into the zeroed ping with
-// vector atomics. Tiles whose windows hold hot bins are spread over many CTAs.
-constexpr uint32_t kPartSamples = 16384;
+// vector atomics. Tiles whose windows hold hot bins are spread over many
+// CTAs, and a small ping still spreads over the whole GPU.
+constexpr uint32_t kPartSamples = 16384, kMinPartSamples = 512, kItemsPerWorker = 4;
 constexpr uint32_t kMaxParts = 256;
+constexpr int kPlanThreads = 1024;
 
+// counts[t]: stream length of tile t (read by the gathers for their part
+// bounds); first[t]: first item of tile t, first[tiles] = the item count.
 template <int TR>
-__global__ void k_tile_parts(const uint32_t* __restrict__ off, const int2* __restrict__ win,
-                             const int2* __restrict__ bb_tiles, uint32_t nR, uint32_t nBB, uint32_t tiles_b,
-                             uint32_t tiles, uint32_t* __restrict__ parts)
+__global__ void __launch_bounds__(kPlanThreads)
+k_tile_plan(const uint32_t* __restrict__ off, const int2* __restrict__ win, const int2* __restrict__ bb_tiles,
+            uint32_t nR, uint32_t nBB, uint32_t tiles_b, uint32_t tiles, uint32_t workers,
+            uint32_t* __restrict__ counts, uint32_t* __restrict__ first, uint4* __restrict__ items)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if(t >= tiles) return;
-    const uint32_t tb = t % tiles_b, tr = t / tiles_b;
-    int jmin = INT_MAX, jmax = INT_MIN;
-    for(int q = 0; q < TR; q++) {
-        const int r = (int)tr * TR + q;
-        if(r >= (int)nR) break;
-        const int2 w = win[r];
-        if(w.x <= w.y) { jmin = min(jmin, w.x); jmax = max(jmax, w.y); }
+    __shared__ uint32_t s_warp[32];
+    __shared__ unsigned long long s_sum[kPlanThreads / 32];
+    __shared__ uint32_t s_part;
+    unsigned long long mine = 0;
+    for(uint32_t t = threadIdx.x; t < tiles; t += kPlanThreads) {
+        const uint32_t tb = t % tiles_b, tr = t / tiles_b;
+        int jmin = INT_MAX, jmax = INT_MIN;
+        for(int q = 0; q < TR; q++) {
+            const int r = (int)tr * TR + q;
+            if(r >= (int)nR) break;
+            const int2 w = win[r];
+            if(w.x <= w.y) { jmin = min(jmin, w.x); jmax = max(jmax, w.y); }
+        }
+        uint64_t count = 0;
+        const int2 kb = bb_tiles[tb];
+        for(int j = jmin; j <= jmax; j++)
+            count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
+        const uint32_t c = (uint32_t)min(count, (uint64_t)0xFFFFFFFFu);
+        counts[t] = c;
+        mine += c;
     }
-    uint64_t count = 0;
-    const int2 kb = bb_tiles[tb];
-    for(int j = jmin; j <= jmax; j++)
-        count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
-    const uint64_t np = (count + kPartSamples - 1) / kPartSamples;
-    parts[t] = (uint32_t)(np < kMaxParts ? np : kMaxParts);
-}
-
-__global__ void k_tile_items(const uint32_t* __restrict__ parts, const uint32_t* __restrict__ first,
-                             uint32_t tiles_b, uint32_t tiles, uint4* __restrict__ items)
-{
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if(t >= tiles) return;
-    const uint32_t np = parts[t], f = first[t];
-    for(uint32_t p = 0; p < np; p++) items[f + p] = make_uint4(t % tiles_b, t / tiles_b, p, np);
+    for(int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
+    if((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = mine;
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        unsigned long long total = 0;
+        for(int w = 0; w < kPlanThreads / 32; w++) total += s_sum[w];
+        const unsigned long long want = (unsigned long long)max(workers, 1u) * kItemsPerWorker;
+        const unsigned long long part = (total + want - 1) / want;
+        s_part = (uint32_t)min(max(part, (unsigned long long)kMinPartSamples), (unsigned long long)kPartSamples);
+    }
+    __syncthreads();
+    const uint64_t part = s_part;
+    uint32_t carry = 0;
+    for(uint32_t t0 = 0; t0 < tiles; t0 += kPlanThreads) {
+        const uint32_t t = t0 + threadIdx.x;
+        uint32_t np = 0;
+        if(t < tiles) np = (uint32_t)min(((uint64_t)counts[t] + part - 1) / part, (uint64_t)kMaxParts);
+        uint32_t seg_total;
+        const uint32_t f = carry + block_exclusive_scan(np, s_warp, seg_total);
+        if(t < tiles) {
+            first[t] = f;
+            for(uint32_t q = 0; q < np; q++) items[f + q] = make_uint4(t % tiles_b, t / tiles_b, q, np);
+        }
+        carry += seg_total;
+    }
+    if(threadIdx.x == 0) first[tiles] = carry;
 }
 
 template <int TR, int TB>
@@ -418,11 +447,10 @@ k_gather_split(const float4* __restrict__ sorted, const uint32_t* __restrict__ o
                const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
                ReduceParams rp, uint32_t nBB, float2* __restrict__ out,
                const uint4* __restrict__ items, const uint32_t* __restrict__ n_items_ptr,
-               uint32_t* __restrict__ counter)
+               const uint32_t* __restrict__ tile_counts, uint32_t tiles_b, uint32_t* __restrict__ counter)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_item;
-    __shared__ uint64_t s_count;
     const uint32_t n_items = *n_items_ptr;
     for(;;) {
         if(threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
@@ -432,23 +460,8 @@ k_gather_split(const float4* __restrict__ sorted, const uint32_t* __restrict__ o
         const uint4 item = items[it];
         uint32_t g0 = 0, g1 = 0xFFFFFFFFu;
         if(item.w > 1) {
-            // Stream length of this tile, then this part's share of it.
-            if(threadIdx.x == 0) {
-                int jmin = INT_MAX, jmax = INT_MIN;
-                for(int q = 0; q < TR; q++) {
-                    const int r = (int)item.y * TR + q;
-                    if(r >= (int)rp.nR) break;
-                    const int2 w = win[r];
-                    if(w.x <= w.y) { jmin = min(jmin, w.x); jmax = max(jmax, w.y); }
-                }
-                const int2 kb = bb_tiles[item.x];
-                uint64_t count = 0;
-                for(int j = jmin; j <= jmax; j++)
-                    count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
-                s_count = count;
-            }
-            __syncthreads();
-            const uint64_t count = s_count;
+            // This part's share of the tile's stream.
+            const uint64_t count = tile_counts[item.y * tiles_b + item.x];
             g0 = (uint32_t)(count * item.z / item.w);
             g1 = (uint32_t)(count * (item.z + 1) / item.w);
         }
@@ -502,7 +515,6 @@ struct TcSmem {
     uint32_t warp_sums[kTcWarps];
     int jmin, jmax;
     uint32_t item;
-    unsigned long long count;
     unsigned long long bar[2];
     uint32_t tmem;
     int abort;
@@ -543,6 +555,7 @@ k_gather_tc(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
             const float2* __restrict__ pulse_pad, const float* __restrict__ beam_pad,
             ReduceParams rp, uint32_t nBB, float2* __restrict__ out,
             const uint4* __restrict__ items, const uint32_t* __restrict__ n_items_ptr,
+            const uint32_t* __restrict__ tile_counts, uint32_t tiles_b,
             uint32_t* __restrict__ counter, uint32_t* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -622,15 +635,9 @@ k_gather_tc(const float4* __restrict__ sorted, const uint32_t* __restrict__ off,
         // This part's share [g_begin, g_end) of the tile's sample stream.
         uint32_t g_begin = 0, g_end = 0xFFFFFFFFu;
         if(item.w > 1) {
-            if(tid == 0) {
-                unsigned long long count = 0;
-                for(int j = jmin; j <= jmax; j++)
-                    count += off[(size_t)j * nBB + kb.y + 1] - off[(size_t)j * nBB + kb.x];
-                S.count = count;
-            }
-            __syncthreads();
-            g_begin = (uint32_t)(S.count * item.z / item.w);
-            g_end = (uint32_t)(S.count * (item.z + 1) / item.w);
+            const uint64_t count = tile_counts[item.y * tiles_b + item.x];
+            g_begin = (uint32_t)(count * item.z / item.w);
+            g_end = (uint32_t)(count * (item.z + 1) / item.w);
         }
         uint32_t nchunk = 0, chain = 0, base = 0;
         bool stop = false;
@@ -796,11 +803,9 @@ rtacx_status launch_2d_tc(Context& ctx, float2* out, cudaStream_t stream)
     }
     const uint32_t tiles_b = (ctx.nB + kTcBearings - 1) / kTcBearings;
     const uint32_t tiles = tiles_b * ((ctx.nR + kTcRows - 1) / kTcRows);
-    k_tile_parts<kTcRows><<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles128, ctx.nR,
-                                                                   ctx.bin.nBB, tiles_b, tiles, ctx.d_tile_parts);
-    scan_u32(ctx.d_tile_parts, tiles, ctx.d_tile_first, stream);   // d_tile_first[tiles] = item count
-    k_tile_items<<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_tile_parts, ctx.d_tile_first, tiles_b, tiles,
-                                                          ctx.d_items);
+    k_tile_plan<kTcRows><<<1, kPlanThreads, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles128, ctx.nR,
+                                                         ctx.bin.nBB, tiles_b, tiles, (uint32_t)ctx.sm_count,
+                                                         ctx.d_tile_parts, ctx.d_tile_first, ctx.d_items);
     cudaError_t me = cudaMemsetAsync(ctx.d_item_counter, 0, sizeof(uint32_t), stream);
     if(me == cudaSuccess) me = cudaMemsetAsync(out, 0, (size_t)ctx.nR * ctx.nB * sizeof(float2), stream);
     if(me != cudaSuccess) {
@@ -810,7 +815,8 @@ rtacx_status launch_2d_tc(Context& ctx, float2* out, cudaStream_t stream)
     }
     k_gather_tc<<<ctx.sm_count, kTcThreads, smem, stream>>>(
         ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles128, ctx.d_ranges, ctx.d_bearings, ctx.d_pulse,
-        ctx.d_beam, ctx.red, ctx.bin.nBB, out, ctx.d_items, ctx.d_tile_first + tiles, ctx.d_item_counter, ctx.d_err);
+        ctx.d_beam, ctx.red, ctx.bin.nBB, out, ctx.d_items, ctx.d_tile_first + tiles, ctx.d_tile_parts, tiles_b,
+        ctx.d_item_counter, ctx.d_err);
     const cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) { ctx.error = std::string("k_gather_tc: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;
@@ -871,11 +877,13 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
         return RTACX_ERR_UNSUPPORTED;
     }
     const uint32_t tiles = grid.x * grid.y;
-    k_tile_parts<TR><<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles, ctx.nR,
-                                                               ctx.bin.nBB, grid.x, tiles, ctx.d_tile_parts);
-    scan_u32(ctx.d_tile_parts, tiles, ctx.d_tile_first, stream);   // d_tile_first[tiles] = item count
-    k_tile_items<<<(tiles + 255) / 256, 256, 0, stream>>>(ctx.d_tile_parts, ctx.d_tile_first, grid.x, tiles,
-                                                          ctx.d_items);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather_split<TR, TB>, kThreads, smem);
+    per_sm = std::max(1, per_sm);
+    const uint32_t workers = (uint32_t)(ctx.sm_count * per_sm);
+    k_tile_plan<TR><<<1, kPlanThreads, 0, stream>>>(ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles, ctx.nR, ctx.bin.nBB,
+                                                    grid.x, tiles, workers, ctx.d_tile_parts, ctx.d_tile_first,
+                                                    ctx.d_items);
     cudaError_t me = cudaMemsetAsync(ctx.d_item_counter, 0, sizeof(uint32_t), stream);
     if(me == cudaSuccess) me = cudaMemsetAsync(out, 0, (size_t)ctx.nR * ctx.nB * sizeof(float2), stream);
     if(me != cudaSuccess) {
@@ -883,12 +891,10 @@ rtacx_status launch_2d(Context& ctx, float2* out, cudaStream_t stream)
         ctx.error = std::string("clearing the split gather's ping: ") + cudaGetErrorString(me);
         return RTACX_ERR_CUDA;
     }
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather_split<TR, TB>, kThreads, smem);
-    per_sm = std::max(1, per_sm);
-    k_gather_split<TR, TB><<<ctx.sm_count * per_sm, kThreads, smem, stream>>>(
+    k_gather_split<TR, TB><<<workers, kThreads, smem, stream>>>(
         ctx.d_sorted, ctx.d_offsets, ctx.d_win, ctx.d_bb_tiles, ctx.d_ranges, ctx.d_bearings, ctx.d_pulse,
-        ctx.d_beam, ctx.red, ctx.bin.nBB, out, ctx.d_items, ctx.d_tile_first + tiles, ctx.d_item_counter);
+        ctx.d_beam, ctx.red, ctx.bin.nBB, out, ctx.d_items, ctx.d_tile_first + tiles, ctx.d_tile_parts, grid.x,
+        ctx.d_item_counter);
     const cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) { ctx.error = std::string("k_gather_split: ") + cudaGetErrorString(e); return RTACX_ERR_CUDA; }
     return RTACX_OK;
