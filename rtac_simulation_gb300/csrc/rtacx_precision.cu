@@ -82,14 +82,29 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float4 v, uint64_t pol)
                  ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol));
 }
 
-// Adds a sample's share v of one range node to bearing interval q of the
-// node's grid row: (1 - w) v to the interval's left bearing, w v to its
-// right bearing, in one 16-byte vector reduction. The grid is never read by
-// the kernels that reduce into it, so the reductions carry no memory clobber.
-__device__ __forceinline__ void deposit(float4* row, int q, float w, float2 v, uint64_t pol)
+// Grid layout: node rows in pairs. Entry (node row j, bearing interval q)
+// is float4 ((j >> 1) pitch + q) 2 + (j & 1), so the two rows of a pair share
+// the 32-byte sector of each interval: a sample's two deposits (rows jg and
+// jg + 1, one interval) fall into one sector when jg is even.
+__host__ __device__ __forceinline__ size_t grid_at(int j, int q, uint32_t pitch)
+{
+    return ((size_t)(j >> 1) * pitch + (size_t)q) * 2 + (size_t)(j & 1);
+}
+
+// Grid entries of `rows` node rows (an odd last row keeps its pair's space).
+__host__ __device__ __forceinline__ size_t grid_quads(uint32_t rows, uint32_t pitch)
+{
+    return (size_t)((rows + 1) >> 1) * pitch * 2;
+}
+
+// Adds a sample's share v of one range node to one bearing interval entry:
+// (1 - w) v to the interval's left bearing, w v to its right bearing, in one
+// 16-byte vector reduction. The grid is never read by the kernels that
+// reduce into it, so the reductions carry no memory clobber.
+__device__ __forceinline__ void deposit(float4* entry, float w, float2 v, uint64_t pol)
 {
     const float w0 = 1.0f - w;
-    red_add_v4(row + q, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y), pol);
+    red_add_v4(entry, make_float4(w0 * v.x, w0 * v.y, w * v.x, w * v.y), pol);
 }
 
 size_t accumulate_smem_bytes(uint32_t nR)
@@ -112,10 +127,11 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p, Gr
     if(hot) { const int2 h = *hot; hot_lo = h.x; hot_len = h.y; }
     const uint32_t rsel = (blockIdx.x + (threadIdx.x >> 5)) & (kHotReplicas - 1);   // by CTA and warp
     const uint32_t pitch = g.pitch;
-    // Grid row jg: the grid's, or this warp's replica of a hot row.
-    auto grid_row = [&](int jg) -> float4* {
+    // Entry (jg, q): the grid's, or in this warp's replica of a hot row
+    // (replica rows are plain rows of `pitch` entries).
+    auto entry = [&](int jg, int q) -> float4* {
         const uint32_t hj = (uint32_t)(jg - hot_lo);
-        return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * pitch : G + (size_t)jg * pitch;
+        return hj < (uint32_t)hot_len ? rep + ((size_t)hj * kHotReplicas + rsel) * pitch + q : G + grid_at(jg, q, pitch);
     };
     const uint32_t words = (p.key.nR + 31) / 32;
     const uint64_t keep = policy_evict_last();
@@ -141,8 +157,8 @@ k_prec_accumulate(const float* __restrict__ samples, uint64_t n, BinParams p, Gr
             if(!grid_coords(g, rec[u].z, rec[u].w, jg, alpha, q, w)) continue;
             const float2 v = apply_echo(p, make_float2(rec[u].x, rec[u].y), rec[u].z);
             const float a0 = 1.0f - alpha;
-            deposit(grid_row(jg), q, w, make_float2(a0 * v.x, a0 * v.y), keep);
-            deposit(grid_row(jg + 1), q, w, make_float2(alpha * v.x, alpha * v.y), keep);
+            deposit(entry(jg, q), w, make_float2(a0 * v.x, a0 * v.y), keep);
+            deposit(entry(jg + 1, q), w, make_float2(alpha * v.x, alpha * v.y), keep);
         }
     }
     __syncthreads();
@@ -250,13 +266,32 @@ k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinPara
             const uint64_t next = c + (uint64_t)kStages * gridDim.x;
             if(next < stages) issue(next, slot);
         }
+        // Lanes 2k and 2k + 1 deposit together: first the even lane's
+        // sample (row jg from the even lane, jg + 1 from the odd one), then
+        // the odd lane's, so each reduction instruction sends a sample's two
+        // rows of an interval as one sector when jg is even.
+        const bool odd = (threadIdx.x & 1u) != 0u;
 #pragma unroll
         for(int u = 0; u < kStagedPerThread; u++) {
             if(key[u] != kOutOfRange) atomicOr(&s_bits[key[u] >> 5], 1u << (key[u] & 31));
-            if(row[u] >= 0) {
-                float4* r0 = G + (size_t)row[u] * pitch;
-                deposit(r0, cell[u], wgt[u], make_float2(add[u].x, add[u].y), keep);
-                deposit(r0 + pitch, cell[u], wgt[u], make_float2(add[u].z, add[u].w), keep);
+            const int row_p = __shfl_xor_sync(0xffffffffu, row[u], 1);
+            const int cell_p = __shfl_xor_sync(0xffffffffu, cell[u], 1);
+            const float wgt_p = __shfl_xor_sync(0xffffffffu, wgt[u], 1);
+            float4 add_p;
+            add_p.x = __shfl_xor_sync(0xffffffffu, add[u].x, 1);
+            add_p.y = __shfl_xor_sync(0xffffffffu, add[u].y, 1);
+            add_p.z = __shfl_xor_sync(0xffffffffu, add[u].z, 1);
+            add_p.w = __shfl_xor_sync(0xffffffffu, add[u].w, 1);
+#pragma unroll
+            for(int h = 0; h < 2; h++) {
+                // h = 0: the even lane's sample; h = 1: the odd lane's.
+                const bool mine = odd == (h == 1);
+                const int r = mine ? row[u] : row_p;
+                if(r >= 0) {
+                    const float4 a = mine ? add[u] : add_p;
+                    deposit(G + grid_at(r + (odd ? 1 : 0), mine ? cell[u] : cell_p, pitch), mine ? wgt[u] : wgt_p,
+                            odd ? make_float2(a.z, a.w) : make_float2(a.x, a.y), keep);
+                }
             }
         }
         if(aborted) break;
@@ -399,7 +434,7 @@ __global__ void __launch_bounds__(kHotPickThreads) k_hot_pick(uint32_t* __restri
 }
 
 // Adds the replicas of the hot rows into the grid once every sample is in
-// (nothing when the interval is empty). Rows of `pitch` entries.
+// (nothing when the interval is empty). Replica rows of `pitch` entries.
 __global__ void k_hot_fold(const int2* __restrict__ hot, uint32_t pitch, const float4* __restrict__ rep,
                            float4* __restrict__ G)
 {
@@ -408,12 +443,13 @@ __global__ void k_hot_fold(const int2* __restrict__ hot, uint32_t pitch, const f
     for(uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t row = i / pitch, k = i % pitch;
         const float4* rb = rep + row * kHotReplicas * pitch + k;
-        float4 acc = G[((uint64_t)h.x + row) * pitch + k];
+        float4* g = G + grid_at(h.x + (int)row, (int)k, pitch);
+        float4 acc = *g;
         for(int r = 0; r < kHotReplicas; r++) {
             const float4 e = rb[(uint64_t)r * pitch];
             acc.x += e.x; acc.y += e.y; acc.z += e.z; acc.w += e.w;
         }
-        G[((uint64_t)h.x + row) * pitch + k] = acc;
+        *g = acc;
     }
 }
 
@@ -456,11 +492,11 @@ __device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float
 
 // Grid bearing q of a node row: the left share of bearing interval q plus
 // the right share of interval q - 1 (interval cells - 1 is never written).
-__device__ __forceinline__ float2 node_value(const float4* __restrict__ row, uint32_t q)
+__device__ __forceinline__ float2 node_value(const float4* __restrict__ G, uint32_t r, uint32_t q, uint32_t pitch)
 {
-    const float4 a = row[q];
+    const float4 a = G[grid_at((int)r, (int)q, pitch)];
     if(q == 0) return make_float2(a.x, a.y);
-    const float4 b = row[q - 1];
+    const float4 b = G[grid_at((int)r, (int)q - 1, pitch)];
     return make_float2(a.x + b.z, a.y + b.w);
 }
 
@@ -474,8 +510,7 @@ __global__ void k_prec_split(const float4* __restrict__ G, uint32_t rows, uint32
     const uint32_t r = blockIdx.y;
     const uint32_t k2 = blockIdx.x * blockDim.x + threadIdx.x;
     if(r >= rows || 2 * k2 >= cells) return;
-    const float4* grow = G + (size_t)r * pitch;
-    const float2 n0 = node_value(grow, 2 * k2), n1 = node_value(grow, 2 * k2 + 1);
+    const float2 n0 = node_value(G, r, 2 * k2, pitch), n1 = node_value(G, r, 2 * k2 + 1, pitch);
     const float x[4] = {n0.x, n0.y, n1.x, n1.y};     // re0, im0, re1, im1
     uint16_t h[4], l[4];
 #pragma unroll
@@ -513,10 +548,9 @@ k_prec_split_f16(const float4* __restrict__ G, uint32_t rows, uint32_t cells, ui
     __shared__ float s_max[kSplitF16Threads / 32];
     const uint32_t r = blockIdx.x;
     if(r >= rows) return;
-    const float4* grow = G + (size_t)r * pitch;
     float m = 0.0f;
     for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
-        const float2 v = node_value(grow, k);
+        const float2 v = node_value(G, r, k, pitch);
         m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
     }
     for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -529,7 +563,7 @@ k_prec_split_f16(const float4* __restrict__ G, uint32_t rows, uint32_t cells, ui
     if(threadIdx.x == 0) row_scale[r] = __uint_as_float((uint32_t)(127 - se) << 23);
     uint16_t* row = A + (size_t)r * Kp;
     for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
-        const float2 v = node_value(grow, k);
+        const float2 v = node_value(G, r, k, pitch);
         const float xr = v.x * s, xi = v.y * s;
         const __half hr = __float2half_rn(xr), hi = __float2half_rn(xi);
         const __half lr = __float2half_rn(xr - __half2float(hr)), li = __float2half_rn(xi - __half2float(hi));
@@ -1067,7 +1101,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
         if(cudaMalloc(&p, bytes) != cudaSuccess) { cudaGetLastError(); p = nullptr; return false; }
         return true;
     };
-    const size_t grid_bytes = (size_t)ctx.grid_rows * g.pitch * sizeof(float4);
+    const size_t grid_bytes = grid_quads(ctx.grid_rows, g.pitch) * sizeof(float4);
     if(!alloc(ctx.d_G, grid_bytes) || !alloc(ctx.d_flags, (size_t)(nR + 31) / 32 * 4) ||
        !alloc(ctx.d_A, (size_t)ctx.Mpad * ctx.Kp * 2) || !alloc(ctx.d_B, B.size() * 2) ||
        !alloc(ctx.d_taps, taps.size() * sizeof(float)) || !alloc(ctx.d_C, (size_t)ctx.ksplit * ctx.Mpad * ctx.Npad * sizeof(float)) ||
@@ -1107,7 +1141,7 @@ rtacx_status configure_precision(Context& ctx, const rtacx_precision_desc* d)
 // Zeroes the grid and the non-empty bitmap of a new ping.
 rtacx_status precision_begin(Context& ctx, cudaStream_t stream)
 {
-    const uint64_t quads = (uint64_t)ctx.grid_rows * ctx.grid.pitch;
+    const uint64_t quads = grid_quads(ctx.grid_rows, ctx.grid.pitch);
     const uint32_t blocks = (uint32_t)std::min<uint64_t>((quads + 255) / 256, (uint64_t)ctx.sm_count * 32);
     k_prec_clear<<<blocks, 256, 0, stream>>>(ctx.d_G, quads, ctx.d_flags, (ctx.nR + 31) / 32);
     RTACX_CUDA(cudaGetLastError());
