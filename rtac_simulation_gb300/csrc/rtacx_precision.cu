@@ -192,7 +192,7 @@ size_t staged_smem_bytes(uint32_t nR)
 }
 
 template <uint32_t kEcho>
-__global__ void __launch_bounds__(kStagedThreads)
+__global__ void __launch_bounds__(kStagedThreads, 3)
 k_prec_accumulate_staged(const float4* __restrict__ samples, uint64_t n, BinParams p, GridParams g,
                          float4* __restrict__ G, uint32_t* __restrict__ nonempty, uint32_t* __restrict__ err,
                          uint32_t drop_stage)
@@ -490,32 +490,31 @@ __device__ __forceinline__ uint16_t bf16_bits(float x)
 
 __device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
 
-// Grid bearing q of a node row: the left share of bearing interval q plus
-// the right share of interval q - 1 (interval cells - 1 is never written).
-__device__ __forceinline__ float2 node_value(const float4* __restrict__ G, uint32_t r, uint32_t q, uint32_t pitch)
+// Grid bearings q of both node rows of pair m: for each row the left share
+// of bearing interval q plus the right share of interval q - 1 (interval
+// cells - 1 is never written). Entries (2m, q) and (2m + 1, q) are adjacent.
+__device__ __forceinline__ void pair_values(const float4* __restrict__ G, uint32_t m, uint32_t q, uint32_t pitch,
+                                            float2& v0, float2& v1)
 {
-    const float4 a = G[grid_at((int)r, (int)q, pitch)];
-    if(q == 0) return make_float2(a.x, a.y);
-    const float4 b = G[grid_at((int)r, (int)q - 1, pitch)];
-    return make_float2(a.x + b.z, a.y + b.w);
+    const float4* e = G + grid_at((int)(2 * m), (int)q, pitch);
+    const float4 a0 = e[0], a1 = e[1];
+    if(q == 0) { v0 = make_float2(a0.x, a0.y); v1 = make_float2(a1.x, a1.y); return; }
+    const float4 b0 = e[-2], b1 = e[-1];
+    v0 = make_float2(a0.x + b0.z, a0.y + b0.w);
+    v1 = make_float2(a1.x + b1.z, a1.y + b1.w);
 }
 
 // The A operand of the three-term split product: node row r (cells complex
 // values) becomes A row r = [hi(Re) | hi(Im) | hi(Re) | hi(Im) | lo(Re) |
 // lo(Im)], each block `cells` wide, lo = bf16(x - hi). One thread per pair of
-// grid bearings: three 16-byte loads, six 4-byte stores.
-__global__ void k_prec_split(const float4* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t pitch, uint32_t Kp,
-                             uint16_t* __restrict__ A)
+// grid bearings of a pair of node rows: their entries are read once (six
+// 16-byte loads), twelve 4-byte stores.
+__device__ __forceinline__ void split_store(uint16_t* row, uint32_t cells, float2 n0, float2 n1)
 {
-    const uint32_t r = blockIdx.y;
-    const uint32_t k2 = blockIdx.x * blockDim.x + threadIdx.x;
-    if(r >= rows || 2 * k2 >= cells) return;
-    const float2 n0 = node_value(G, r, 2 * k2, pitch), n1 = node_value(G, r, 2 * k2 + 1, pitch);
     const float x[4] = {n0.x, n0.y, n1.x, n1.y};     // re0, im0, re1, im1
     uint16_t h[4], l[4];
 #pragma unroll
     for(int i = 0; i < 4; i++) { h[i] = bf16_bits(x[i]); l[i] = bf16_bits(x[i] - bf16_value(h[i])); }
-    uint16_t* row = A + (size_t)r * Kp + 2 * k2;
     const uint32_t hr = (uint32_t)h[0] | ((uint32_t)h[2] << 16), hi = (uint32_t)h[1] | ((uint32_t)h[3] << 16);
     const uint32_t lr = (uint32_t)l[0] | ((uint32_t)l[2] << 16), li = (uint32_t)l[1] | ((uint32_t)l[3] << 16);
     *reinterpret_cast<uint32_t*>(row) = hr;
@@ -526,12 +525,25 @@ __global__ void k_prec_split(const float4* __restrict__ G, uint32_t rows, uint32
     *reinterpret_cast<uint32_t*>(row + 5 * cells) = li;
 }
 
+__global__ void k_prec_split(const float4* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t pitch, uint32_t Kp,
+                             uint16_t* __restrict__ A)
+{
+    const uint32_t m = blockIdx.y;                   // node rows 2m, 2m + 1
+    const uint32_t k2 = blockIdx.x * blockDim.x + threadIdx.x;
+    if(2 * m >= rows || 2 * k2 >= cells) return;
+    float2 a0, a1, b0, b1;                           // rows 2m, 2m + 1 at grid bearings 2 k2, 2 k2 + 1
+    pair_values(G, m, 2 * k2, pitch, a0, b0);
+    pair_values(G, m, 2 * k2 + 1, pitch, a1, b1);
+    split_store(A + (size_t)(2 * m) * Kp + 2 * k2, cells, a0, a1);
+    if(2 * m + 1 < rows) split_store(A + (size_t)(2 * m + 1) * Kp + 2 * k2, cells, b0, b1);
+}
+
 // FP16 per-row-scaled split: grid row r is scaled by 2^(14 - e), e =
 // floor(log2(max |component|)), so that its largest component lies in
 // [2^14, 2^15), then split into fp16 [hi | hi | lo] (lo = x - hi, so hi + lo
 // carries 22 significant bits); row_scale[r] = 2^(e - 14) undoes the scaling
-// exactly in the GEMM epilogue. One CTA per row: the row's maximum, then the
-// split.
+// exactly in the GEMM epilogue. One CTA per pair of node rows: both rows'
+// maxima, then the split.
 __device__ __forceinline__ int scale_exponent(uint32_t maxbits)
 {
     if(maxbits == 0u) return 0;                       // zero row: scale 1
@@ -545,31 +557,46 @@ __global__ void __launch_bounds__(kSplitF16Threads)
 k_prec_split_f16(const float4* __restrict__ G, uint32_t rows, uint32_t cells, uint32_t pitch, uint32_t Kp,
                  uint16_t* __restrict__ A, float* __restrict__ row_scale)
 {
-    __shared__ float s_max[kSplitF16Threads / 32];
-    const uint32_t r = blockIdx.x;
-    if(r >= rows) return;
-    float m = 0.0f;
+    __shared__ float s_max[2][kSplitF16Threads / 32];
+    const uint32_t m = blockIdx.x;                   // node rows 2m, 2m + 1
+    if(2 * m >= rows) return;
+    const bool second = 2 * m + 1 < rows;
+    float mx0 = 0.0f, mx1 = 0.0f;
     for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
-        const float2 v = node_value(G, r, k, pitch);
-        m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+        float2 v0, v1;
+        pair_values(G, m, k, pitch, v0, v1);
+        mx0 = fmaxf(mx0, fmaxf(fabsf(v0.x), fabsf(v0.y)));
+        mx1 = fmaxf(mx1, fmaxf(fabsf(v1.x), fabsf(v1.y)));
     }
-    for(int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+    for(int o = 16; o > 0; o >>= 1) {
+        mx0 = fmaxf(mx0, __shfl_xor_sync(0xffffffffu, mx0, o));
+        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+    }
+    if((threadIdx.x & 31) == 0) { s_max[0][threadIdx.x >> 5] = mx0; s_max[1][threadIdx.x >> 5] = mx1; }
     __syncthreads();
-    m = 0.0f;
-    for(int w = 0; w < kSplitF16Threads / 32; w++) m = fmaxf(m, s_max[w]);
-    const int se = scale_exponent(__float_as_uint(m));
-    const float s = __uint_as_float((uint32_t)(se + 127) << 23);
-    if(threadIdx.x == 0) row_scale[r] = __uint_as_float((uint32_t)(127 - se) << 23);
-    uint16_t* row = A + (size_t)r * Kp;
-    for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
-        const float2 v = node_value(G, r, k, pitch);
-        const float xr = v.x * s, xi = v.y * s;
+    mx0 = 0.0f; mx1 = 0.0f;
+    for(int w = 0; w < kSplitF16Threads / 32; w++) { mx0 = fmaxf(mx0, s_max[0][w]); mx1 = fmaxf(mx1, s_max[1][w]); }
+    const int se0 = scale_exponent(__float_as_uint(mx0)), se1 = scale_exponent(__float_as_uint(mx1));
+    const float sc0 = __uint_as_float((uint32_t)(se0 + 127) << 23), sc1 = __uint_as_float((uint32_t)(se1 + 127) << 23);
+    if(threadIdx.x == 0) {
+        row_scale[2 * m] = __uint_as_float((uint32_t)(127 - se0) << 23);
+        if(second) row_scale[2 * m + 1] = __uint_as_float((uint32_t)(127 - se1) << 23);
+    }
+    auto store = [&](uint16_t* row, uint32_t k, float2 v, float sc) {
+        const float xr = v.x * sc, xi = v.y * sc;
         const __half hr = __float2half_rn(xr), hi = __float2half_rn(xi);
         const __half lr = __float2half_rn(xr - __half2float(hr)), li = __float2half_rn(xi - __half2float(hi));
         row[k] = __half_as_ushort(hr);             row[cells + k] = __half_as_ushort(hi);
         row[2 * cells + k] = __half_as_ushort(hr); row[3 * cells + k] = __half_as_ushort(hi);
         row[4 * cells + k] = __half_as_ushort(lr); row[5 * cells + k] = __half_as_ushort(li);
+    };
+    uint16_t* row0 = A + (size_t)(2 * m) * Kp;
+    uint16_t* row1 = row0 + Kp;
+    for(uint32_t k = threadIdx.x; k < cells; k += blockDim.x) {
+        float2 v0, v1;
+        pair_values(G, m, k, pitch, v0, v1);
+        store(row0, k, v0, sc0);
+        if(second) store(row1, k, v1, sc1);
     }
 }
 
@@ -1220,11 +1247,11 @@ rtacx_status precision_finish(Context& ctx, float* out, cudaStream_t stream)
     }
     ctx.mark(1, false, stream);
     if(!ctx.prec_f16) {
-        const dim3 sgrid((cells / 2 + 255) / 256, ctx.grid_rows);
+        const dim3 sgrid((cells / 2 + 255) / 256, (ctx.grid_rows + 1) / 2);
         k_prec_split<<<sgrid, 256, 0, stream>>>(ctx.d_G, ctx.grid_rows, cells, ctx.grid.pitch, ctx.Kp, ctx.d_A);
     }
     else {
-        k_prec_split_f16<<<ctx.grid_rows, kSplitF16Threads, 0, stream>>>(ctx.d_G, ctx.grid_rows, cells, ctx.grid.pitch,
+        k_prec_split_f16<<<(ctx.grid_rows + 1) / 2, kSplitF16Threads, 0, stream>>>(ctx.d_G, ctx.grid_rows, cells, ctx.grid.pitch,
                                                                          ctx.Kp, ctx.d_A, ctx.d_row_scale);
     }
     RTACX_CUDA(cudaGetLastError());
