@@ -51,16 +51,16 @@ DEFAULT_CONFIG = "precision_2d"
 #       python bench.py --steps 2 --warmup 3 --no-cpu-baseline [--no-next-rows]
 # on a GB300. Reported as `traffic` beside the live `achieved` numbers.
 NCU_TRAFFIC_BYTES = {
-    "k_prec_accumulate_staged": 335.831e6 + 4.377e6,
+    "k_prec_accumulate_staged": 336.287e6 + 5.313e6,
     "k_gemm_tn": 78.715e6 + 4.004e6,
     "sort_bin": (268.531e6 + 3.186e6) + (273.130e6 + 220.672e6),   # k_count + k_scatter_pipe
 }
 # The accumulation's bound is the L2's reduction throughput, not HBM: ncu on
 # the default workload (profiles/k_prec_accumulate_staged_precision_2d.md)
-# shows 2.00 L2 reduction requests (2.07 sectors) per sample and the L2 at
-# 72 % of its peak throughput while DRAM carries the algorithmic bytes once.
-NCU_ACCUMULATE_L2 = {"l2_throughput_pct": 71.6, "l2_red_sectors_pct": 45.6, "red_sectors_per_sample": 2.07,
-                     "red_requests_per_sample": 2.0}
+# shows 1.50 L2 reduction requests (1.57 sectors) per sample and the L2 at
+# 65 % of its peak throughput while DRAM carries the algorithmic bytes once.
+NCU_ACCUMULATE_L2 = {"l2_throughput_pct": 64.7, "l2_red_sectors_pct": 40.6, "red_sectors_per_sample": 1.57,
+                     "red_requests_per_sample": 1.50}
 
 KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
 PRECISION_KERNELS_PER_PING = 5   # clear, staged accumulate, operand split, tensor-core GEMM, range filter
@@ -749,7 +749,9 @@ def run_ours(args, world, rank, local):
                     "l2_bound": dict(NCU_ACCUMULATE_L2, reductions_per_s=NCU_ACCUMULATE_L2["red_sectors_per_sample"]
                                      * n / (ps["accumulate"] / 1e3),
                                      note="bound by the L2's reduction rate (two 16-byte vector reductions "
-                                          "per sample into a 68 MB L2-resident grid); HBM carries the samples once")}
+                                          "per sample into a 68 MB L2-resident grid, lane pairs sending a sample's "
+                                          "two node rows as one sector when they share it: 1.5 requests per "
+                                          "sample); HBM carries the samples once")}
         roof_gemm = {"bound": "tensor", "achieved": gemm_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                      "frac": gemm_tf / peaks["bf16_tflops"], "traffic": ncu.get("k_gemm_tn"), "kernel": "k_gemm_tn",
                      "peak_source": peaks["source"],
