@@ -108,6 +108,8 @@ def check_sorted(oracle, wk, exact_order: bool):
     lambda: wl.oculus_reference_2d(),
     lambda: wl.oculus_2d(n_samples=1 << 20),
     lambda: wl.precision_2d(n_samples=1 << 20),
+    lambda: wl.echosounder_1d(n_samples=1 << 20, n_ranges=8192),    # pipelined, reservations in two batches
+    lambda: wl.precision_2d(n_samples=1 << 20, n_ranges=12000),     # pipelined, 16 bins per thread
     lambda: wl.oculus_2d(n_samples=1 << 18, n_ranges=512),     # 16384 bins: the unpipelined staged shape
     lambda: wl.oculus_2d(n_samples=1000),
 ])
