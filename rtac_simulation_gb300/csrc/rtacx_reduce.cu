@@ -275,12 +275,18 @@ __device__ __forceinline__ void gather_rows_1d(const float4* __restrict__ sorted
     if(w.x <= w.y) {
         const float R = ranges[r];
         const uint32_t p0 = off[w.x], p1 = off[w.y + 1];
-        for(uint32_t i = p0 + lane; i < p1; i += 32) {
-            const float4 s = sorted[i];
+        auto add = [&](const float4& s) {
             const float2 wv = lerp_cplx(s_pulse, rp.range_axis, s.z - R);
             const float2 u = cmul(make_float2(s.x, s.y), wv);
             acc.x += u.x; acc.y += u.y;
+        };
+        uint32_t i = p0 + lane;
+        // Four records per lane in flight, then the remainder.
+        for(; i + 96 < p1; i += 128) {
+            const float4 s0 = sorted[i], s1 = sorted[i + 32], s2 = sorted[i + 64], s3 = sorted[i + 96];
+            add(s0); add(s1); add(s2); add(s3);
         }
+        for(; i < p1; i += 32) add(sorted[i]);
     }
     for(int o = 16; o > 0; o >>= 1) {
         acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
