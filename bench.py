@@ -62,7 +62,9 @@ NCU_TRAFFIC_BYTES = {
 NCU_ACCUMULATE_L2 = {"l2_throughput_pct": 64.7, "l2_red_sectors_pct": 40.6, "red_sectors_per_sample": 1.57,
                      "red_requests_per_sample": 1.50}
 
-KERNELS_PER_PING = 8   # count, binscan, scatter, windows, tile parts, part scan, work items, split gather
+# Plain form: count, bin scan, scatter, windows, then (2D) the tile plan and
+# the split gather or (1D) the row gather.
+KERNELS_PER_PING = {1: 5, 2: 6}
 PRECISION_KERNELS_PER_PING = 5   # clear, staged accumulate, operand split, tensor-core GEMM, range filter
 
 
@@ -767,7 +769,7 @@ def run_ours(args, world, rank, local):
     r = res[head]
     line["e2e"] = {"value": world * n * args.steps / r["t_e2e"], "unit": "samples/s",
                    "h2d_bytes_per_step": n * rec_in, "d2h_bytes_per_step": int(np.prod(wk.out_shape)) * 8}
-    line["gpu_launches"] = (PRECISION_KERNELS_PER_PING if head == "precision" else KERNELS_PER_PING) * args.steps
+    line["gpu_launches"] = (PRECISION_KERNELS_PER_PING if head == "precision" else KERNELS_PER_PING[wk.dims]) * args.steps
     line["clocks"] = r["clocks"]
     if world == 1 and args.config == DEFAULT_CONFIG and not args.no_next_rows:
         line["next_rows"] = time_next_rows(torch, local, peaks)
