@@ -295,9 +295,9 @@ __global__ void k_reset_batch(const PingDev* __restrict__ pings, uint32_t n_ping
 
 uint32_t hist_grid(uint32_t ctas, uint64_t n)
 {
-    // At least ~2048 samples per CTA so that the per-CTA histogram set-up
+    // At least ~1024 samples per CTA so that the per-CTA histogram set-up
     // stays small relative to the data.
-    const uint64_t want = std::max<uint64_t>(1, (n + 2047) / 2048);
+    const uint64_t want = std::max<uint64_t>(1, (n + 1023) / 1024);
     return (uint32_t)std::min<uint64_t>(ctas, want);
 }
 
