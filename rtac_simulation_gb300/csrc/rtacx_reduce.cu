@@ -488,7 +488,7 @@ k_gather_split(const float4* __restrict__ sorted, const uint32_t* __restrict__ o
 // U], both operands K-major in the 128-byte swizzle layout. FP32 accuracy
 // from TF32 operands: each operand is split into tf32 hi + lo (21 significant
 // bits together) and three MMAs form hi*hi + hi*lo + lo*hi, products exact
-// in the FP32 accumulator. Per chunk the 256 threads write the operands of
+// in the FP32 accumulator. Per chunk the 512 threads write the operands of
 // one of two stages while the MMAs of the other run; one thread issues the
 // MMAs and commits them to the stage's mbarrier. The persistent CTA takes
 // (tile, part) items like k_gather_split and adds each finished tile into
