@@ -11,8 +11,10 @@
 //                      grid bearings around the sample bearing. The grid is
 //                      stored by bearing interval: entry (node, q) holds the
 //                      interval's shares of grid bearings q and q + 1, so each
-//                      sample is exactly two 16-byte vector reductions. No
-//                      sort.
+//                      sample is exactly two 16-byte vector reductions; node
+//                      rows are stored in pairs, so that lane pairs send a
+//                      sample's two reductions as one 32-byte sector request
+//                      when its nodes share a pair. No sort.
 //   k_prec_split       grid bearing q of a node = left share of interval q +
 //                      right share of interval q - 1, as the bf16 A operand
 //                      [hi | hi | lo] of the three-term split product
